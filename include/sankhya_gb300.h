@@ -1,0 +1,178 @@
+/*
+ * sankhya_gb300.h -- the C ABI of the GB300-native restarted-PDHG engine.
+ *
+ * This is the boundary SANKHYA's PDHG path binds to. It replaces the reference's CUDA
+ * engine behind the unchanged C++ seam
+ *     Solution sankhya::gpu::solve_pdhg_gpu(const Model&, const Options&, Logger&,
+ *                                           SolveControl*)          (src/gpu/pdhg_gpu.hpp:19-20)
+ * whose only caller is src/core/solve.cpp:802. The seam (sih-26_gb300/seam/pdhg_gpu.cpp)
+ * converts the Model / Options into the plain structs below and calls these functions.
+ *
+ * Conventions (the reference's C API, include/sankhya/sankhya.h:36-50 and
+ * src/api/c_api.cpp:39,134-150): every function returns an int status, 0 on success; the
+ * message of the last failure on this thread is sankhya_gb300_last_error(). Nothing throws
+ * across this boundary. All pointers are HOST pointers; the engine copies what it needs to
+ * the device and owns every device allocation. There is no CPU fallback: with no usable
+ * GPU the calls fail with SANKHYA_GB300_ERROR_DEVICE.
+ */
+#ifndef SANKHYA_GB300_H
+#define SANKHYA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define SGB_API __attribute__((visibility("default")))
+#else
+#define SGB_API
+#endif
+
+/* Return codes: sankhya_status (include/sankhya/sankhya.h:42-50) plus one for the device. */
+enum {
+  SANKHYA_GB300_OK = 0,
+  SANKHYA_GB300_ERROR_ARGUMENT = 1,
+  SANKHYA_GB300_ERROR_MODEL = 3,
+  SANKHYA_GB300_ERROR_OPTION = 4,
+  SANKHYA_GB300_ERROR_MEMORY = 5,
+  SANKHYA_GB300_ERROR_INTERNAL = 6,
+  SANKHYA_GB300_ERROR_DEVICE = 7 /* no usable CUDA device, or a CUDA call failed */
+};
+
+/* Solve status: the values of sankhya_solve_status (include/sankhya/sankhya.h:53-69). */
+enum {
+  SANKHYA_GB300_NOT_SOLVED = 0,
+  SANKHYA_GB300_OPTIMAL = 1,
+  SANKHYA_GB300_FEASIBLE = 2,
+  SANKHYA_GB300_INFEASIBLE = 3,
+  SANKHYA_GB300_ITERATION_LIMIT = 5,
+  SANKHYA_GB300_TIME_LIMIT = 6,
+  SANKHYA_GB300_NUMERICAL_ERROR = 8,
+  SANKHYA_GB300_MODEL_ERROR = 9,
+  SANKHYA_GB300_INTERRUPTED = 11
+};
+
+/* Arithmetic of the PDHG iterations (new option row `pdhg_precision`). */
+enum {
+  SANKHYA_GB300_FP64 = 0,  /* the reference's method, FP64 throughout */
+  SANKHYA_GB300_MIXED = 1  /* FP32 iterates / values / SpMV, FP64 KKT and refinement */
+};
+
+/* An LP in sankhya::Model's layout (include/sankhya/model.hpp:123-170): CSC, int32 indices
+ * ascending inside each column, FP64 values, rows rl <= Ax <= ru, columns l <= x <= u; an
+ * infinite bound is +-inf or any magnitude >= 1e30. */
+typedef struct sankhya_gb300_lp {
+  int32_t rows;
+  int32_t cols;
+  const int32_t* col_starts; /* cols + 1 */
+  const int32_t* row_index;  /* nnz */
+  const double* values;      /* nnz */
+  const double* col_cost;
+  const double* col_lower;
+  const double* col_upper;
+  const double* row_lower;
+  const double* row_upper;
+  double sense;            /* +1 minimise, -1 maximise (Model::sense_multiplier) */
+  double objective_offset; /* Model::objective_offset */
+} sankhya_gb300_lp;
+
+/* One iteration-table row, the arguments of Logger::iteration (src/pdhg/pdhg.cpp:399). */
+typedef void (*sankhya_gb300_log_fn)(void* user, long long iteration, double objective,
+                                     double primal, double dual, double seconds);
+
+/* The PDHG option rows (src/util/options.cpp) plus the engine's own. */
+typedef struct sankhya_gb300_params {
+  double tolerance;          /* pdhg_tolerance */
+  int64_t iteration_limit;   /* iteration_limit; < 0: the engine's 1e6 ceiling (pdhg.cpp:124) */
+  double time_limit;         /* time_limit in seconds; >= 1e300 means none */
+  int32_t restart;           /* pdhg_restart */
+  int32_t stop_at_request;   /* pdhg_stop_at_request */
+  int64_t random_seed;       /* random_seed (power-iteration start, scaling.cpp:168) */
+  int32_t precision;         /* SANKHYA_GB300_FP64 or SANKHYA_GB300_MIXED */
+  int32_t steps_per_poll;    /* attempted steps per CUDA-graph launch; 0 = default */
+  const volatile int32_t* interrupt; /* SolveControl::interrupt flag, polled; may be NULL */
+  sankhya_gb300_log_fn log;  /* may be NULL */
+  void* log_user;
+} sankhya_gb300_params;
+
+/* sankhya::pdhg::Residuals (src/pdhg/pdhg_evaluate.hpp:19-70). */
+typedef struct sankhya_gb300_residuals {
+  double primal, dual, gap;
+  double primal_objective, dual_objective;
+  double absolute_primal, absolute_dual;
+  double gap_as_verified, complementarity;
+} sankhya_gb300_residuals;
+
+typedef struct sankhya_gb300_result {
+  int32_t status;        /* SANKHYA_GB300_OPTIMAL, ... */
+  int32_t converged;     /* the loop met its stopping test */
+  int64_t iterations;    /* accepted steps (Solution::iterations) */
+  int64_t attempts;      /* attempted steps, accepted or not */
+  int64_t restarts;
+  int64_t evaluations;
+  int64_t refinements;   /* mixed precision: refinement rounds */
+  double objective;      /* objective_offset + col_cost . x at the reported point */
+  double dual_bound;     /* only when optimal, else -+inf (pdhg.cpp:553-557) */
+  sankhya_gb300_residuals final_residuals;
+  double spectral_norm;
+  double scaled_min_abs, scaled_max_abs;
+  double setup_seconds;  /* scaling + power iteration on the device */
+  double loop_seconds;   /* the PDHG loop */
+  double solve_seconds;  /* the whole solve call */
+  char message[512];
+} sankhya_gb300_result;
+
+typedef struct sankhya_gb300_pdhg sankhya_gb300_pdhg; /* opaque engine handle */
+
+/* Message of the last failure on the calling thread ("" if none). c_api.cpp:39. */
+SGB_API const char* sankhya_gb300_last_error(void);
+
+/* Device probes: src/gpu/device.hpp:19-29 (device_available, device_free_memory,
+ * device_compute_capability). description may be NULL. */
+SGB_API int sankhya_gb300_device_available(char* description, int32_t capacity);
+SGB_API int sankhya_gb300_device_free_memory(size_t* free_bytes, size_t* total_bytes);
+SGB_API int sankhya_gb300_device_compute_capability(int32_t* major, int32_t* minor);
+
+/* Device bytes the engine allocates for an LP of this size (replaces
+ * estimate_pdhg_gpu_memory, src/gpu/gpu_memory.hpp:35-44). Pure arithmetic. */
+SGB_API size_t sankhya_gb300_estimate_memory(int32_t rows, int32_t cols, int64_t nonzeros,
+                                             int32_t precision);
+
+/* Create / destroy an engine on a device (the state GpuState held, src/gpu/pdhg_gpu.cu:201). */
+SGB_API int sankhya_gb300_pdhg_create(int32_t device, sankhya_gb300_pdhg** out);
+SGB_API int sankhya_gb300_pdhg_destroy(sankhya_gb300_pdhg* engine);
+
+/* Copy an LP to the device: CSC and a CSR copy, unscaled values kept for the evaluation.
+ * Fails with SANKHYA_GB300_ERROR_MODEL on the numeric defects Model::validate rejects
+ * (src/core/model.cpp:127-240). */
+SGB_API int sankhya_gb300_pdhg_load(sankhya_gb300_pdhg* engine, const sankhya_gb300_lp* lp);
+
+/* Solve the loaded LP: device preconditioning (src/la/scaling.cpp:111-194) and the restarted
+ * PDHG loop (src/pdhg/pdhg.cpp:76-568) with every iterate resident on the device. */
+SGB_API int sankhya_gb300_pdhg_solve(sankhya_gb300_pdhg* engine,
+                                     const sankhya_gb300_params* params,
+                                     sankhya_gb300_result* result);
+
+/* The reported point of the last solve, filled as solve_pdhg fills Solution
+ * (src/pdhg/pdhg.cpp:487-501): col_value = x, col_dual = sense * (c + A^T y),
+ * row_dual = sense * (-y). Any pointer may be NULL. */
+SGB_API int sankhya_gb300_pdhg_solution(sankhya_gb300_pdhg* engine, double* col_value,
+                                        double* col_dual, double* row_dual);
+
+/* Parity hooks for tests: the device preconditioning of the loaded LP (Dr, Dc, the scaled CSC
+ * values and the spectral-norm estimate), and one product with the loaded matrix:
+ * op 0 = A x (x has cols entries), op 1 = A^T y (y has rows entries); scaled != 0 uses the
+ * scaled matrix of the last preconditioning. */
+SGB_API int sankhya_gb300_pdhg_scaling(sankhya_gb300_pdhg* engine, int64_t random_seed,
+                                       double* row_scale, double* col_scale,
+                                       double* scaled_values, double* spectral_norm);
+SGB_API int sankhya_gb300_pdhg_spmv(sankhya_gb300_pdhg* engine, int32_t op, int32_t scaled,
+                                    const double* in, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SANKHYA_GB300_H */

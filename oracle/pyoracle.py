@@ -1,0 +1,226 @@
+"""ctypes binding of the checker libraries (TEST INFRASTRUCTURE ONLY).
+
+``Oracle()`` loads oracle/liboracle.so, the C restatement of the reference PDHG;
+``Oracle(reference=True)`` loads oracle/_ref/libsankhya_ref.so, the reference's own sources
+compiled by ``make -C oracle ref`` (only where the reference tree exists). Both expose the
+same calls, so a test can run them side by side. Only tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg import this module; the GPU engine never does.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libsankhya_ref.so")
+REFERENCE_TREE = os.environ.get("SANKHYA_REFERENCE_TREE", "/root/reference")
+
+STATUS_NAMES = {0: "not_solved", 1: "optimal", 2: "feasible", 3: "infeasible",
+                5: "iteration_limit", 6: "time_limit", 8: "numerical_error", 9: "model_error",
+                11: "interrupted"}
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int32)
+
+
+class CLp(ctypes.Structure):
+    _fields_ = [("rows", ctypes.c_int32), ("cols", ctypes.c_int32), ("col_starts", _I),
+                ("row_index", _I), ("values", _D), ("col_cost", _D), ("col_lower", _D),
+                ("col_upper", _D), ("row_lower", _D), ("row_upper", _D),
+                ("sense", ctypes.c_double), ("objective_offset", ctypes.c_double)]
+
+
+class CParams(ctypes.Structure):
+    _fields_ = [("tolerance", ctypes.c_double), ("iteration_limit", ctypes.c_int64),
+                ("time_limit", ctypes.c_double), ("restart", ctypes.c_int32),
+                ("stop_at_request", ctypes.c_int32), ("random_seed", ctypes.c_int64)]
+
+
+class CResiduals(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in (
+        "primal", "dual", "gap", "primal_objective", "dual_objective", "absolute_primal",
+        "absolute_dual", "gap_as_verified", "complementarity")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class CResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("iterations", ctypes.c_int64), ("restarts", ctypes.c_int64),
+                ("objective", ctypes.c_double), ("dual_bound", ctypes.c_double),
+                ("final_residuals", CResiduals), ("spectral_norm", ctypes.c_double),
+                ("scaled_min_abs", ctypes.c_double), ("scaled_max_abs", ctypes.c_double),
+                ("solve_seconds", ctypes.c_double), ("evaluations", ctypes.c_int64)]
+
+
+@dataclass
+class OracleSolution:
+    status: int
+    status_name: str
+    iterations: int
+    restarts: int
+    objective: float
+    dual_bound: float
+    residuals: dict
+    col_value: np.ndarray
+    col_dual: np.ndarray
+    row_dual: np.ndarray
+    solve_seconds: float
+    spectral_norm: float = float("nan")
+    message: str = ""
+
+
+def build(reference: bool = False) -> None:
+    """Compile the restatement (always) and the reference library (when asked and the
+    reference tree exists)."""
+    src = os.path.join(HERE, "pdhg_oracle.c")
+    if (not os.path.exists(ORACLE_LIB)
+            or os.path.getmtime(ORACLE_LIB) < max(os.path.getmtime(src),
+                                                   os.path.getmtime(src[:-1] + "h"))):
+        subprocess.run(["gcc", "-O2", "-fPIC", "-std=c11", "-ffp-contract=off", "-fopenmp",
+                        "-shared", "-o", ORACLE_LIB, src, "-lm"], check=True)
+    if reference and os.path.isdir(os.path.join(REFERENCE_TREE, "src", "pdhg")):
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", f"REF={REFERENCE_TREE}"],
+                       check=True)
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def _ptr(a, ctype):
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+class Oracle:
+    def __init__(self, reference: bool = False):
+        path = REF_LIB if reference else ORACLE_LIB
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is not built")
+        self.reference = reference
+        self.lib = ctypes.CDLL(path)
+        p = "ref_" if reference else "orc_"
+        self._solve = getattr(self.lib, p + "solve_pdhg")
+        if reference:
+            self._solve.argtypes = [ctypes.POINTER(CLp), ctypes.POINTER(CParams),
+                                    ctypes.POINTER(CResult), _D, _D, _D, ctypes.c_char_p,
+                                    ctypes.c_int32]
+        else:
+            self._solve.argtypes = [ctypes.POINTER(CLp), ctypes.POINTER(CParams),
+                                    ctypes.POINTER(CResult), _D, _D, _D]
+        self._solve.restype = ctypes.c_int32
+        self._scaling = getattr(self.lib, p + "build_scaling")
+        self._scaling.argtypes = [ctypes.POINTER(CLp), _D, ctypes.c_int32] + [_D] * 10
+        self._scaling.restype = None
+        self._evaluate = getattr(self.lib, p + "evaluate")
+        self._evaluate.argtypes = [ctypes.POINTER(CLp), _D, _D, _D, _D]
+        self._evaluate.restype = CResiduals
+        if reference:
+            self._norm = self.lib.ref_spectral_norm
+            self._norm.argtypes = [ctypes.POINTER(CLp), ctypes.c_int32, ctypes.c_uint32]
+        else:
+            self._norm = self.lib.orc_spectral_norm
+            self._norm.argtypes = [ctypes.c_int32, ctypes.c_int32, _I, _I, _D, ctypes.c_int32,
+                                   ctypes.c_uint32]
+            self.lib.orc_multiply.argtypes = [ctypes.c_int32, ctypes.c_int32, _I, _I, _D, _D, _D]
+            self.lib.orc_transpose_multiply.argtypes = [ctypes.c_int32, ctypes.c_int32, _I, _I,
+                                                        _D, _D, _D]
+            self.lib.orc_power_start.argtypes = [ctypes.c_uint32, ctypes.c_int32, _D]
+        self._norm.restype = ctypes.c_double
+
+    @staticmethod
+    def _clp(lp):
+        lp = lp.contiguous()
+        c = CLp(lp.rows, lp.cols, _ptr(lp.col_starts, ctypes.c_int32),
+                _ptr(lp.row_index, ctypes.c_int32), _ptr(lp.values, ctypes.c_double),
+                _ptr(lp.col_cost, ctypes.c_double), _ptr(lp.col_lower, ctypes.c_double),
+                _ptr(lp.col_upper, ctypes.c_double), _ptr(lp.row_lower, ctypes.c_double),
+                _ptr(lp.row_upper, ctypes.c_double), lp.sense, lp.objective_offset)
+        return c, lp  # keep the arrays alive with the struct
+
+    def solve(self, lp, tolerance=1e-8, iteration_limit=-1, time_limit=None, restart=True,
+              stop_at_request=False, random_seed=0) -> OracleSolution:
+        c, keep = self._clp(lp)
+        params = CParams(tolerance, iteration_limit, 1e308 if time_limit is None else time_limit,
+                         int(restart), int(stop_at_request), random_seed)
+        res = CResult()
+        x = np.zeros(lp.cols)
+        d = np.zeros(lp.cols)
+        y = np.zeros(lp.rows)
+        args = [ctypes.byref(c), ctypes.byref(params), ctypes.byref(res), _ptr(x, ctypes.c_double),
+                _ptr(d, ctypes.c_double), _ptr(y, ctypes.c_double)]
+        message = ""
+        if self.reference:
+            buf = ctypes.create_string_buffer(4096)
+            self._solve(*args, buf, 4096)
+            message = buf.value.decode(errors="replace")
+        else:
+            self._solve(*args)
+        del keep
+        return OracleSolution(res.status, STATUS_NAMES.get(res.status, str(res.status)),
+                              res.iterations, res.restarts, res.objective, res.dual_bound,
+                              res.final_residuals.as_dict(), x, d, y, res.solve_seconds,
+                              res.spectral_norm, message)
+
+    def build_scaling(self, lp, ruiz_iterations=10):
+        c, keep = self._clp(lp)
+        m, n = lp.rows, lp.cols
+        out = dict(values=np.zeros(lp.nnz), row=np.zeros(m), col=np.zeros(n), cost=np.zeros(n),
+                   col_lower=np.zeros(n), col_upper=np.zeros(n), row_lower=np.zeros(m),
+                   row_upper=np.zeros(m))
+        mn, mx = ctypes.c_double(), ctypes.c_double()
+        cost = np.ascontiguousarray(lp.sense * np.asarray(lp.col_cost, dtype=np.float64))
+        self._scaling(ctypes.byref(c), _ptr(cost, ctypes.c_double), ruiz_iterations,
+                      *[_ptr(out[k], ctypes.c_double) for k in (
+                          "values", "row", "col", "cost", "col_lower", "col_upper", "row_lower",
+                          "row_upper")], ctypes.byref(mn), ctypes.byref(mx))
+        del keep
+        out["min_abs"], out["max_abs"] = mn.value, mx.value
+        return out
+
+    def spectral_norm(self, lp, iterations=30, seed=1):
+        c, keep = self._clp(lp)
+        if self.reference:
+            return self._norm(ctypes.byref(c), iterations, seed)
+        return self._norm(lp.rows, lp.cols, c.col_starts, c.row_index, c.values, iterations, seed)
+
+    def evaluate(self, lp, x, y):
+        c, keep = self._clp(lp)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        act = np.zeros(lp.rows)
+        red = np.zeros(lp.cols)
+        r = self._evaluate(ctypes.byref(c), _ptr(x, ctypes.c_double), _ptr(y, ctypes.c_double),
+                           _ptr(act, ctypes.c_double), _ptr(red, ctypes.c_double))
+        return r.as_dict(), act, red
+
+    # Restatement-only helpers.
+    def multiply(self, lp, x):
+        lp = lp.contiguous()
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(lp.rows)
+        self.lib.orc_multiply(lp.rows, lp.cols, _ptr(lp.col_starts, ctypes.c_int32),
+                              _ptr(lp.row_index, ctypes.c_int32), _ptr(lp.values, ctypes.c_double),
+                              _ptr(x, ctypes.c_double), _ptr(y, ctypes.c_double))
+        return y
+
+    def transpose_multiply(self, lp, y):
+        lp = lp.contiguous()
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        x = np.zeros(lp.cols)
+        self.lib.orc_transpose_multiply(lp.rows, lp.cols, _ptr(lp.col_starts, ctypes.c_int32),
+                                        _ptr(lp.row_index, ctypes.c_int32),
+                                        _ptr(lp.values, ctypes.c_double), _ptr(y, ctypes.c_double),
+                                        _ptr(x, ctypes.c_double))
+        return x
+
+    def power_start(self, seed, count):
+        out = np.zeros(count)
+        self.lib.orc_power_start(seed, count, _ptr(out, ctypes.c_double))
+        return out

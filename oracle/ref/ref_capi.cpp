@@ -1,0 +1,180 @@
+// ref_capi.cpp -- a C entry layer over the REFERENCE's own PDHG sources, for tests only.
+//
+// oracle/Makefile compiles this file together with the reference's unmodified sources
+// (src/pdhg, src/la/{scaling,sparse}.cpp, src/core/{model,resource_limits}.cpp, src/util/*)
+// into oracle/_ref/libsankhya_ref.so. The functions mirror pdhg_oracle.h one for one so that a
+// test can run the restatement and the reference on identical inputs and compare the bits.
+// Nothing here is linked into the GPU engine.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "la/scaling.hpp"
+#include "pdhg/pdhg_evaluate.hpp"
+#include "sankhya/logging.hpp"
+#include "sankhya/model.hpp"
+#include "sankhya/options.hpp"
+#include "sankhya/pdhg.hpp"
+
+#include "../pdhg_oracle.h"
+
+namespace {
+
+sankhya::Model to_model(const orc_lp* lp) {
+  sankhya::Model model;
+  const auto n = static_cast<std::size_t>(lp->cols);
+  const auto m = static_cast<std::size_t>(lp->rows);
+  model.sense = lp->sense < 0.0 ? sankhya::ObjSense::kMaximize : sankhya::ObjSense::kMinimize;
+  model.objective_offset = lp->objective_offset;
+  model.col_cost.assign(lp->col_cost, lp->col_cost + n);
+  model.col_lower.assign(lp->col_lower, lp->col_lower + n);
+  model.col_upper.assign(lp->col_upper, lp->col_upper + n);
+  model.col_type.assign(n, sankhya::VarType::kContinuous);
+  model.row_lower.assign(lp->row_lower, lp->row_lower + m);
+  model.row_upper.assign(lp->row_upper, lp->row_upper + m);
+  model.matrix.reset(lp->rows, lp->cols);
+  model.matrix.reserve(static_cast<std::size_t>(lp->col_starts[lp->cols]));
+  for (int32_t j = 0; j < lp->cols; ++j) {
+    for (int32_t k = lp->col_starts[j]; k < lp->col_starts[j + 1]; ++k) {
+      model.matrix.add_entry(lp->row_index[k], j, lp->values[k]);
+    }
+  }
+  // Drop tolerance zero keeps every entry the caller passed, explicit zeros included, so the
+  // pattern matches the CSC arrays one for one.
+  model.matrix.finalize(0.0);
+  return model;
+}
+
+int32_t status_code(sankhya::SolveStatus s) {
+  using S = sankhya::SolveStatus;
+  switch (s) {
+    case S::kNotSolved: return ORC_NOT_SOLVED;
+    case S::kOptimal: return ORC_OPTIMAL;
+    case S::kFeasible: return ORC_FEASIBLE;
+    case S::kInfeasible: return ORC_INFEASIBLE;
+    case S::kIterationLimit: return ORC_ITERATION_LIMIT;
+    case S::kTimeLimit: return ORC_TIME_LIMIT;
+    case S::kNumericalError: return ORC_NUMERICAL_ERROR;
+    case S::kModelError: return ORC_MODEL_ERROR;
+    case S::kInterrupted: return ORC_INTERRUPTED;
+    default: return 100 + static_cast<int32_t>(s);
+  }
+}
+
+orc_residuals to_c(const sankhya::pdhg::Residuals& r) {
+  orc_residuals c;
+  c.primal = r.primal;
+  c.dual = r.dual;
+  c.gap = r.gap;
+  c.primal_objective = r.primal_objective;
+  c.dual_objective = r.dual_objective;
+  c.absolute_primal = r.absolute_primal;
+  c.absolute_dual = r.absolute_dual;
+  c.gap_as_verified = r.gap_as_verified;
+  c.complementarity = r.complementarity;
+  return c;
+}
+
+// The restart count is not a Solution field; the engine's message carries it
+// ("... after N iterations and R restarts ...", src/pdhg/pdhg.cpp:519-548).
+long long restarts_from_message(const std::string& message) {
+  const std::size_t at = message.find(" iterations and ");
+  if (at == std::string::npos) return -1;
+  return std::atoll(message.c_str() + at + std::strlen(" iterations and "));
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t ref_solve_pdhg(const orc_lp* lp, const orc_params* params, orc_result* result,
+                       double* col_value, double* col_dual, double* row_dual, char* message,
+                       int32_t message_capacity) {
+  std::memset(result, 0, sizeof(*result));
+  const sankhya::Model model = to_model(lp);
+  sankhya::Options options;
+  options.set_bool("log_to_console", false);
+  options.set_double("pdhg_tolerance", params->tolerance);
+  options.set_int("iteration_limit", params->iteration_limit);
+  if (params->time_limit < 1e300) options.set_double("time_limit", params->time_limit);
+  options.set_bool("pdhg_restart", params->restart != 0);
+  options.set_bool("pdhg_stop_at_request", params->stop_at_request != 0);
+  options.set_int("random_seed", params->random_seed);
+  sankhya::Logger logger(nullptr);
+  const sankhya::Solution s = sankhya::pdhg::solve_pdhg(model, options, logger, nullptr);
+  result->status = status_code(s.status);
+  result->iterations = s.iterations;
+  result->restarts = restarts_from_message(s.message);
+  result->objective = s.objective;
+  result->dual_bound = s.dual_bound;
+  result->solve_seconds = s.solve_seconds;
+  const auto n = static_cast<std::size_t>(lp->cols);
+  const auto m = static_cast<std::size_t>(lp->rows);
+  if (col_value != nullptr && s.col_value.size() == n) {
+    std::memcpy(col_value, s.col_value.data(), n * sizeof(double));
+  }
+  if (col_dual != nullptr && s.col_dual.size() == n) {
+    std::memcpy(col_dual, s.col_dual.data(), n * sizeof(double));
+  }
+  if (row_dual != nullptr && s.row_dual.size() == m) {
+    std::memcpy(row_dual, s.row_dual.data(), m * sizeof(double));
+  }
+  if (message != nullptr && message_capacity > 0) {
+    std::snprintf(message, static_cast<std::size_t>(message_capacity), "%s", s.message.c_str());
+  }
+  return result->status;
+}
+
+void ref_build_scaling(const orc_lp* lp, const double* min_space_cost, int32_t ruiz_iterations,
+                       double* scaled_values, double* row_scale, double* col_scale,
+                       double* scaled_cost, double* scaled_col_lower, double* scaled_col_upper,
+                       double* scaled_row_lower, double* scaled_row_upper, double* min_abs,
+                       double* max_abs) {
+  const sankhya::Model model = to_model(lp);
+  const std::vector<double> cost(min_space_cost, min_space_cost + lp->cols);
+  const sankhya::Scaling s = sankhya::build_scaling(model, cost, ruiz_iterations);
+  std::memcpy(scaled_values, s.matrix.values().data(), s.matrix.values().size() * sizeof(double));
+  std::memcpy(row_scale, s.row.data(), s.row.size() * sizeof(double));
+  std::memcpy(col_scale, s.column.data(), s.column.size() * sizeof(double));
+  std::memcpy(scaled_cost, s.cost.data(), s.cost.size() * sizeof(double));
+  std::memcpy(scaled_col_lower, s.col_lower.data(), s.col_lower.size() * sizeof(double));
+  std::memcpy(scaled_col_upper, s.col_upper.data(), s.col_upper.size() * sizeof(double));
+  std::memcpy(scaled_row_lower, s.row_lower.data(), s.row_lower.size() * sizeof(double));
+  std::memcpy(scaled_row_upper, s.row_upper.data(), s.row_upper.size() * sizeof(double));
+  *min_abs = s.min_abs;
+  *max_abs = s.max_abs;
+}
+
+double ref_spectral_norm(const orc_lp* lp, int32_t iterations, uint32_t seed) {
+  const sankhya::Model model = to_model(lp);
+  return sankhya::estimate_spectral_norm(model.matrix, iterations, seed);
+}
+
+orc_residuals ref_evaluate(const orc_lp* lp, const double* x, const double* y, double* activity,
+                           double* reduced) {
+  const sankhya::Model model = to_model(lp);
+  sankhya::pdhg::Problem problem;
+  problem.model = &model;
+  const auto n = static_cast<std::size_t>(lp->cols);
+  const auto m = static_cast<std::size_t>(lp->rows);
+  problem.cost.resize(n);
+  for (std::size_t j = 0; j < n; ++j) problem.cost[j] = lp->sense * lp->col_cost[j];
+  problem.cost_norm = sankhya::pdhg::euclidean_norm(problem.cost);
+  double bound_square = 0.0;
+  for (std::size_t i = 0; i < m; ++i) {
+    const double rl = lp->row_lower[i], ru = lp->row_upper[i];
+    const double b = sankhya::is_finite_bound(rl) ? rl : (sankhya::is_finite_bound(ru) ? ru : 0.0);
+    bound_square += b * b;
+  }
+  problem.bound_norm = std::sqrt(bound_square);
+  std::vector<double> xs(x, x + n), ys(y, y + m), act, red;
+  const sankhya::pdhg::Residuals r = sankhya::pdhg::evaluate(problem, xs, ys, act, red);
+  if (activity != nullptr) std::memcpy(activity, act.data(), m * sizeof(double));
+  if (reduced != nullptr) std::memcpy(reduced, red.data(), n * sizeof(double));
+  return to_c(r);
+}
+
+}  // extern "C"

@@ -1,0 +1,667 @@
+// engine.cu -- host driver of the GB300 PDHG engine.
+//
+// Follows src/pdhg/pdhg.cpp:76-568 step for step, with every vector on the device:
+//   setup     device Ruiz x10 + Pock-Chambolle (src/la/scaling.cpp:111-159) on both the CSC
+//             and the CSR copy, power iteration (src/la/scaling.cpp:161-194) from the same
+//             std::mt19937 start, x0 = proj(0), y0 = 0 (src/pdhg/pdhg.cpp:140-147);
+//   loop      CUDA graphs of `steps_per_poll` attempted steps, each step = k_primal + k_dual
+//             + the evaluation kernels (which return at once off the evaluation tick); the
+//             host launches graph k+1 before it reads the status snapshot graph k copied
+//             out, so the device never waits on the host;
+//   report    one final evaluation of (best_x, best_y) on the device
+//             (src/pdhg/pdhg.cpp:487-567), status and message assembled here.
+// The reference checks the clock at every step; this engine checks it, and the
+// SolveControl interrupt flag, at every snapshot (every `steps_per_poll` steps).
+#include "engine.hpp"
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstddef>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <random>
+
+namespace sgb {
+
+void cuda_check(cudaError_t err, const char* what, const char* file, int line) {
+  if (err == cudaSuccess) return;
+  char buf[512];
+  std::snprintf(buf, sizeof(buf), "CUDA error %s (%s) in %s at %s:%d", cudaGetErrorName(err),
+                cudaGetErrorString(err), what, file, line);
+  const int code = (err == cudaErrorMemoryAllocation) ? SANKHYA_GB300_ERROR_MEMORY
+                                                      : SANKHYA_GB300_ERROR_DEVICE;
+  throw EngineError{code, buf};
+}
+
+template <typename T>
+void DeviceArray<T>::allocate(size_t n) {
+  release();
+  count = n;
+  if (n > 0) SGB_CUDA(cudaMalloc(&ptr, n * sizeof(T)));
+}
+template <typename T>
+void DeviceArray<T>::upload(const T* host, size_t n, cudaStream_t s) {
+  allocate(n);
+  if (n > 0) SGB_CUDA(cudaMemcpyAsync(ptr, host, n * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+template <typename T>
+void DeviceArray<T>::release() {
+  if (ptr != nullptr) cudaFree(ptr);
+  ptr = nullptr;
+  count = 0;
+}
+template struct DeviceArray<int>;
+template struct DeviceArray<int2>;
+template struct DeviceArray<double>;
+template struct DeviceArray<Ctl>;
+
+namespace {
+
+double now_seconds() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+bool finite_bound_host(double v) { return !(std::isinf(v) || std::fabs(v) >= 1e30); }
+
+// Greedy row tiles: consecutive rows while the tile has at most kTileThreads rows and at
+// most kTileCap nonzeros; a row longer than kTileCap is a tile of its own.
+std::vector<int2> build_tiles(const std::vector<int>& ptr, int lines) {
+  std::vector<int2> tiles;
+  int r = 0;
+  while (r < lines) {
+    const int begin = r;
+    if (ptr[r + 1] - ptr[r] > kTileCap) {
+      tiles.push_back(make_int2(r, r + 1));
+      ++r;
+      continue;
+    }
+    ++r;
+    while (r < lines && r - begin < kTileThreads && ptr[r + 1] - ptr[begin] <= kTileCap) ++r;
+    tiles.push_back(make_int2(begin, r));
+  }
+  return tiles;
+}
+
+std::string format(const char* fmt, ...) __attribute__((format(printf, 1, 2)));
+std::string format(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  return buf;
+}
+
+}  // namespace
+
+size_t estimate_memory(long long rows, long long cols, long long nnz, int precision) {
+  const size_t m = static_cast<size_t>(rows < 0 ? 0 : rows);
+  const size_t n = static_cast<size_t>(cols < 0 ? 0 : cols);
+  const size_t z = static_cast<size_t>(nnz < 0 ? 0 : nnz);
+  size_t bytes = 0;
+  bytes += (m + 1 + n + 1) * sizeof(int) + 2 * z * sizeof(int);  // CSR + CSC pattern
+  bytes += (m + n) * sizeof(int2);                                // tiles (upper bound)
+  bytes += 4 * z * sizeof(double);      // unscaled + scaled values, both layouts
+  bytes += 18 * n * sizeof(double);     // column vectors (see Engine members)
+  bytes += 14 * m * sizeof(double);     // row vectors
+  if (precision == SANKHYA_GB300_MIXED) {
+    bytes += 2 * z * sizeof(float) + (10 * n + 8 * m) * sizeof(float);
+  }
+  bytes += 8u << 20;  // partial-sum buffers and the control block (generous)
+  return bytes;
+}
+
+Engine::Engine(int device) : device_(device) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+    cudaGetLastError();
+    throw EngineError{SANKHYA_GB300_ERROR_DEVICE, "no CUDA device is available"};
+  }
+  if (device < 0 || device >= count) {
+    throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT,
+                      format("device %d does not exist (%d present)", device, count)};
+  }
+  SGB_CUDA(cudaSetDevice(device));
+  SGB_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  SGB_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device));
+  SGB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&snapshot_), 2 * sizeof(Ctl),
+                         cudaHostAllocDefault));
+  for (auto& ev : done_event_) SGB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  ctl_.allocate(1);
+  SGB_CUDA(cudaMemset(ctl_.ptr, 0, sizeof(Ctl)));
+}
+
+Engine::~Engine() {
+  cudaSetDevice(device_);
+  destroy_graphs();
+  for (auto& ev : done_event_) {
+    if (ev != nullptr) cudaEventDestroy(ev);
+  }
+  if (snapshot_ != nullptr) cudaFreeHost(snapshot_);
+  if (stream_ != nullptr) cudaStreamDestroy(stream_);
+}
+
+void Engine::destroy_graphs() {
+  for (auto& g : graph_exec_) {
+    if (g != nullptr) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  graph_steps_ = 0;
+}
+
+void Engine::require_loaded() const {
+  if (!loaded_) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no LP has been loaded"};
+}
+
+void Engine::load(const sankhya_gb300_lp& lp) {
+  if (lp.rows < 0 || lp.cols < 0 || lp.col_starts == nullptr) {
+    throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "bad LP dimensions or null column starts"};
+  }
+  const int m = lp.rows, n = lp.cols;
+  const long long nnz = lp.col_starts[n];
+  if (lp.col_starts[0] != 0 || nnz < 0) {
+    throw EngineError{SANKHYA_GB300_ERROR_MODEL, "column starts must begin at 0"};
+  }
+  for (int j = 0; j < n; ++j) {
+    if (lp.col_starts[j + 1] < lp.col_starts[j]) {
+      throw EngineError{SANKHYA_GB300_ERROR_MODEL, "column starts are not monotone"};
+    }
+  }
+  // Model::validate's numeric checks (src/core/model.cpp:175-183 and the bound checks).
+  for (long long k = 0; k < nnz; ++k) {
+    const int i = lp.row_index[k];
+    if (i < 0 || i >= m) {
+      throw EngineError{SANKHYA_GB300_ERROR_MODEL, format("row index %d out of range", i)};
+    }
+    if (!std::isfinite(lp.values[k])) {
+      throw EngineError{SANKHYA_GB300_ERROR_MODEL,
+                        format("matrix entry %lld is %g, which is not a usable coefficient", k,
+                               lp.values[k])};
+    }
+  }
+  for (int j = 0; j < n; ++j) {
+    if (!std::isfinite(lp.col_cost[j]) || std::isnan(lp.col_lower[j]) ||
+        std::isnan(lp.col_upper[j]) || lp.col_lower[j] > lp.col_upper[j]) {
+      throw EngineError{SANKHYA_GB300_ERROR_MODEL, format("column %d has a bad cost or bound", j)};
+    }
+    for (int k = lp.col_starts[j] + 1; k < lp.col_starts[j + 1]; ++k) {
+      if (lp.row_index[k] <= lp.row_index[k - 1]) {
+        throw EngineError{SANKHYA_GB300_ERROR_MODEL,
+                          format("column %d: row indices are not strictly ascending", j)};
+      }
+    }
+  }
+  for (int i = 0; i < m; ++i) {
+    if (std::isnan(lp.row_lower[i]) || std::isnan(lp.row_upper[i]) ||
+        lp.row_lower[i] > lp.row_upper[i]) {
+      throw EngineError{SANKHYA_GB300_ERROR_MODEL, format("row %d has a bad bound", i)};
+    }
+  }
+  if (nnz > std::numeric_limits<int>::max()) {
+    throw EngineError{SANKHYA_GB300_ERROR_MODEL, "more nonzeros than int32 indices address"};
+  }
+  SGB_CUDA(cudaSetDevice(device_));
+  destroy_graphs();
+  loaded_ = solved_ = scaled_ = false;
+  m_ = m;
+  n_ = n;
+  nnz_ = nnz;
+  sense_ = lp.sense < 0.0 ? -1.0 : 1.0;
+  offset_ = lp.objective_offset;
+
+  // CSC as given; CSR by a counting-sort transpose walking columns in ascending order, so
+  // the column indices come out ascending inside each row (src/la/sparse.cpp:271-302).
+  std::vector<int> cptr(lp.col_starts, lp.col_starts + n + 1);
+  std::vector<int> rptr(static_cast<size_t>(m) + 1, 0);
+  for (long long k = 0; k < nnz; ++k) ++rptr[static_cast<size_t>(lp.row_index[k]) + 1];
+  for (int i = 0; i < m; ++i) rptr[i + 1] += rptr[i];
+  std::vector<int> next(rptr.begin(), rptr.end() - 1);
+  std::vector<int> ridx(static_cast<size_t>(nnz));
+  std::vector<double> rval(static_cast<size_t>(nnz));
+  for (int j = 0; j < n; ++j) {
+    for (int k = cptr[j]; k < cptr[j + 1]; ++k) {
+      const int slot = next[lp.row_index[k]]++;
+      ridx[slot] = j;
+      rval[slot] = lp.values[k];
+    }
+  }
+  const std::vector<int2> ctiles = build_tiles(cptr, n);
+  const std::vector<int2> rtiles = build_tiles(rptr, m);
+  ntiles_csc_ = static_cast<int>(ctiles.size());
+  ntiles_csr_ = static_cast<int>(rtiles.size());
+  const int resident = tile_blocks_per_sm() * num_sms_;
+  grid_csc_ = std::max(1, std::min(ntiles_csc_, resident));
+  grid_csr_ = std::max(1, std::min(ntiles_csr_, resident));
+
+  // Minimise-space cost and the norms of src/pdhg/pdhg.cpp:95-111, summed in the
+  // reference's order on the host (they are computed once).
+  std::vector<double> cost(static_cast<size_t>(n));
+  double cost_sq = 0.0;
+  for (int j = 0; j < n; ++j) {
+    cost[j] = sense_ * lp.col_cost[j];
+    cost_sq += cost[j] * cost[j];
+  }
+  cost_norm_ = std::sqrt(cost_sq);
+  double bound_sq = 0.0;
+  for (int i = 0; i < m; ++i) {
+    const double b = finite_bound_host(lp.row_lower[i])
+                         ? lp.row_lower[i]
+                         : (finite_bound_host(lp.row_upper[i]) ? lp.row_upper[i] : 0.0);
+    bound_sq += b * b;
+  }
+  bound_norm_ = std::sqrt(bound_sq);
+
+  cudaStream_t s = stream_;
+  csc_ptr_.upload(cptr.data(), cptr.size(), s);
+  csc_idx_.upload(lp.row_index, static_cast<size_t>(nnz), s);
+  csc_raw_.upload(lp.values, static_cast<size_t>(nnz), s);
+  csr_ptr_.upload(rptr.data(), rptr.size(), s);
+  csr_idx_.upload(ridx.data(), ridx.size(), s);
+  csr_raw_.upload(rval.data(), rval.size(), s);
+  csc_tiles_.upload(ctiles.data(), ctiles.size(), s);
+  csr_tiles_.upload(rtiles.data(), rtiles.size(), s);
+  csc_s_.allocate(static_cast<size_t>(nnz));
+  csr_s_.allocate(static_cast<size_t>(nnz));
+  cost_.upload(cost.data(), cost.size(), s);
+  col_cost_.upload(lp.col_cost, static_cast<size_t>(n), s);
+  l_.upload(lp.col_lower, static_cast<size_t>(n), s);
+  u_.upload(lp.col_upper, static_cast<size_t>(n), s);
+  rl_.upload(lp.row_lower, static_cast<size_t>(m), s);
+  ru_.upload(lp.row_upper, static_cast<size_t>(m), s);
+  for (DeviceArray<double>* a : {&cs_, &ls_, &us_, &dc_, &col_acc_, &x0_, &x1_, &x_sum_, &x_rst_,
+                                 &xu0_, &xu1_, &reduced_, &best_x_, &power_v_}) {
+    a->allocate(static_cast<size_t>(n));
+  }
+  for (DeviceArray<double>* a : {&rls_, &rus_, &dr_, &row_acc_, &y0_, &y1_, &y_sum_, &y_rst_,
+                                 &yu0_, &yu1_, &best_y_, &power_av_}) {
+    a->allocate(static_cast<size_t>(m));
+  }
+  const int pgrid = std::max(grid_csc_, grid_csr_) + num_sms_ * 8;
+  part_primal_.allocate(static_cast<size_t>(grid_csc_));
+  part_dual_.allocate(static_cast<size_t>(grid_csr_) * 2);
+  part_rows0_.allocate(static_cast<size_t>(grid_csr_) * 8);
+  part_cols_.allocate(static_cast<size_t>(grid_csc_) * 16);
+  part_rows1_.allocate(static_cast<size_t>(grid_csr_) * 8);
+  scalars_.allocate(static_cast<size_t>(pgrid) * 2 + 16);
+  power_norms_.allocate(64);
+  SGB_CUDA(cudaStreamSynchronize(s));
+  fill_buffers();
+  loaded_ = true;
+}
+
+void Engine::fill_buffers() {
+  StepBuffers& b = step_;
+  b.ctl = ctl_.ptr;
+  b.csc = Matrix<double>{csc_ptr_.ptr, csc_idx_.ptr, csc_s_.ptr, csc_tiles_.ptr, ntiles_csc_, n_};
+  b.csr = Matrix<double>{csr_ptr_.ptr, csr_idx_.ptr, csr_s_.ptr, csr_tiles_.ptr, ntiles_csr_, m_};
+  b.x[0] = x0_.ptr;
+  b.x[1] = x1_.ptr;
+  b.y[0] = y0_.ptr;
+  b.y[1] = y1_.ptr;
+  b.x_sum = x_sum_.ptr;
+  b.y_sum = y_sum_.ptr;
+  b.c = cs_.ptr;
+  b.l = ls_.ptr;
+  b.u = us_.ptr;
+  b.rl = rls_.ptr;
+  b.ru = rus_.ptr;
+  b.part_primal = part_primal_.ptr;
+  b.part_dual = part_dual_.ptr;
+  b.grid_primal = grid_csc_;
+  b.grid_dual = grid_csr_;
+
+  EvalBuffers& e = eval_;
+  e.ctl = ctl_.ptr;
+  e.csc = Matrix<double>{csc_ptr_.ptr, csc_idx_.ptr, csc_raw_.ptr, csc_tiles_.ptr, ntiles_csc_, n_};
+  e.csr = Matrix<double>{csr_ptr_.ptr, csr_idx_.ptr, csr_raw_.ptr, csr_tiles_.ptr, ntiles_csr_, m_};
+  e.x[0] = x0_.ptr;
+  e.x[1] = x1_.ptr;
+  e.y[0] = y0_.ptr;
+  e.y[1] = y1_.ptr;
+  e.x_sum = x_sum_.ptr;
+  e.y_sum = y_sum_.ptr;
+  e.x_rst = x_rst_.ptr;
+  e.y_rst = y_rst_.ptr;
+  e.dr = dr_.ptr;
+  e.dc = dc_.ptr;
+  e.cost = cost_.ptr;
+  e.col_cost = col_cost_.ptr;
+  e.l = l_.ptr;
+  e.u = u_.ptr;
+  e.rl = rl_.ptr;
+  e.ru = ru_.ptr;
+  e.bound_norm = bound_norm_;
+  e.cost_norm = cost_norm_;
+  e.sense = sense_;
+  e.xu[0] = xu0_.ptr;
+  e.xu[1] = xu1_.ptr;
+  e.yu[0] = yu0_.ptr;
+  e.yu[1] = yu1_.ptr;
+  e.reduced = reduced_.ptr;
+  e.best_x = best_x_.ptr;
+  e.best_y = best_y_.ptr;
+  e.part_rows0 = part_rows0_.ptr;
+  e.part_cols = part_cols_.ptr;
+  e.part_rows1 = part_rows1_.ptr;
+  e.grid_rows = grid_csr_;
+  e.grid_cols = grid_csc_;
+  e.m = m_;
+  e.n = n_;
+}
+
+void Engine::precondition(long long seed) {
+  (void)seed;
+  cudaStream_t s = stream_;
+  const size_t nb = static_cast<size_t>(nnz_) * sizeof(double);
+  if (nnz_ > 0) {
+    SGB_CUDA(cudaMemcpyAsync(csc_s_.ptr, csc_raw_.ptr, nb, cudaMemcpyDeviceToDevice, s));
+    SGB_CUDA(cudaMemcpyAsync(csr_s_.ptr, csr_raw_.ptr, nb, cudaMemcpyDeviceToDevice, s));
+  }
+  launch_fill(dr_.ptr, m_, 1.0, s);
+  launch_fill(dc_.ptr, n_, 1.0, s);
+  for (int pass = 0; pass < 11; ++pass) {  // 10 Ruiz rounds, then Pock-Chambolle
+    launch_scaling_round(m_, n_, step_.csr, step_.csc, csr_s_.ptr, csc_s_.ptr, row_acc_.ptr,
+                         col_acc_.ptr, dr_.ptr, dc_.ptr, pass == 10 ? 1 : 0, s);
+  }
+  launch_scale_vectors(m_, n_, cost_.ptr, l_.ptr, u_.ptr, rl_.ptr, ru_.ptr, dr_.ptr, dc_.ptr,
+                       cs_.ptr, ls_.ptr, us_.ptr, rls_.ptr, rus_.ptr, s);
+  SGB_CUDA(cudaGetLastError());
+  scaled_ = true;
+}
+
+// src/la/scaling.cpp:161-194 on the device. The start vector is the reference's own
+// std::mt19937(seed) + uniform_real_distribution(-1, 1) stream, drawn on the host.
+double Engine::power_iteration(long long seed) {
+  if (m_ == 0 || n_ == 0 || nnz_ == 0) return 1.0;
+  cudaStream_t s = stream_;
+  std::mt19937 rng(static_cast<unsigned>(seed) + 1u);
+  std::uniform_real_distribution<double> spread(-1.0, 1.0);
+  std::vector<double> v(static_cast<size_t>(n_));
+  for (double& value : v) value = spread(rng);
+  SGB_CUDA(cudaMemcpyAsync(power_v_.ptr, v.data(), v.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, s));
+  const int iterations = 30;
+  const int grid = std::min(num_sms_ * 4, std::max(1, (n_ + 255) / 256));
+  double* norms = power_norms_.ptr;  // [2*step] = length^2, [2*step+1] = next
+  for (int step = 0; step < iterations; ++step) {
+    launch_sumsq(power_v_.ptr, n_, scalars_.ptr, norms + 2 * step, s, grid);
+    launch_scale_div(power_v_.ptr, n_, norms + 2 * step, s);
+    launch_spmv(step_.csr, power_v_.ptr, power_av_.ptr, s, grid_csr_);
+    launch_spmv(step_.csc, power_av_.ptr, power_v_.ptr, s, grid_csc_);
+    launch_sumsq(power_v_.ptr, n_, scalars_.ptr, norms + 2 * step + 1, s, grid);
+  }
+  SGB_CUDA(cudaGetLastError());
+  std::vector<double> host(2 * iterations);
+  SGB_CUDA(cudaMemcpyAsync(host.data(), norms, host.size() * sizeof(double),
+                           cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaStreamSynchronize(s));
+  double norm = 0.0;
+  for (int step = 0; step < iterations; ++step) {
+    if (std::sqrt(host[2 * step]) == 0.0) return 1.0;
+    norm = std::sqrt(std::sqrt(host[2 * step + 1]));
+  }
+  return norm > 0.0 ? norm * 1.01 : 1.0;
+}
+
+void Engine::scaling(long long seed, double* row_scale, double* col_scale, double* scaled_values,
+                     double* spectral_norm) {
+  require_loaded();
+  SGB_CUDA(cudaSetDevice(device_));
+  precondition(seed);
+  const double norm = power_iteration(seed);
+  cudaStream_t s = stream_;
+  if (row_scale) SGB_CUDA(cudaMemcpyAsync(row_scale, dr_.ptr, m_ * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (col_scale) SGB_CUDA(cudaMemcpyAsync(col_scale, dc_.ptr, n_ * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (scaled_values && nnz_ > 0) {
+    SGB_CUDA(cudaMemcpyAsync(scaled_values, csc_s_.ptr, nnz_ * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+  }
+  SGB_CUDA(cudaStreamSynchronize(s));
+  if (spectral_norm) *spectral_norm = norm;
+}
+
+void Engine::spmv(int op, int scaled, const double* in, double* out) {
+  require_loaded();
+  if (scaled && !scaled_) {
+    throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no preconditioning has run yet"};
+  }
+  SGB_CUDA(cudaSetDevice(device_));
+  cudaStream_t s = stream_;
+  const int in_len = op == 0 ? n_ : m_;
+  const int out_len = op == 0 ? m_ : n_;
+  DeviceArray<double> din, dout;
+  din.upload(in, static_cast<size_t>(in_len), s);
+  dout.allocate(static_cast<size_t>(out_len));
+  Matrix<double> a = op == 0 ? step_.csr : step_.csc;
+  if (!scaled) a.val = op == 0 ? csr_raw_.ptr : csc_raw_.ptr;
+  launch_spmv(a, din.ptr, dout.ptr, s, op == 0 ? grid_csr_ : grid_csc_);
+  SGB_CUDA(cudaGetLastError());
+  if (out_len > 0) {
+    SGB_CUDA(cudaMemcpyAsync(out, dout.ptr, out_len * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
+  SGB_CUDA(cudaStreamSynchronize(s));
+}
+
+void Engine::init_iterates(const sankhya_gb300_params& p) {
+  cudaStream_t s = stream_;
+  launch_project_start(n_, ls_.ptr, us_.ptr, x0_.ptr, s);
+  launch_fill(y0_.ptr, m_, 0.0, s);
+  launch_fill(x_sum_.ptr, n_, 0.0, s);
+  launch_fill(y_sum_.ptr, m_, 0.0, s);
+  launch_fill(y_rst_.ptr, m_, 0.0, s);
+  launch_fill(best_y_.ptr, m_, 0.0, s);
+  if (n_ > 0) {
+    SGB_CUDA(cudaMemcpyAsync(x_rst_.ptr, x0_.ptr, n_ * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    // best_x starts as the SCALED start point, as the reference's does (pdhg.cpp:190).
+    SGB_CUDA(cudaMemcpyAsync(best_x_.ptr, x0_.ptr, n_ * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  }
+  (void)p;
+}
+
+void Engine::build_graphs(int steps) {
+  if (graph_steps_ == steps && graph_exec_[0] != nullptr) return;
+  destroy_graphs();
+  for (int slot = 0; slot < 2; ++slot) {
+    cudaGraph_t graph = nullptr;
+    SGB_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < steps; ++k) {
+      launch_pdhg_step(step_, stream_);
+      launch_evaluation(eval_, step_, stream_);
+    }
+    cudaMemcpyAsync(snapshot_ + slot, ctl_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_);
+    const cudaError_t end = cudaStreamEndCapture(stream_, &graph);
+    SGB_CUDA(end);
+    const cudaError_t inst = cudaGraphInstantiate(&graph_exec_[slot], graph, 0);
+    cudaGraphDestroy(graph);
+    SGB_CUDA(inst);
+  }
+  graph_steps_ = steps;
+}
+
+void Engine::run_loop(const sankhya_gb300_params& p, double t0, int* stop_status) {
+  const int steps = p.steps_per_poll > 0 ? p.steps_per_poll : 32;
+  build_graphs(steps);
+  const bool has_time_limit = p.time_limit < 1e300;
+  long long logged = 0;
+  auto launch = [&](int slot) {
+    SGB_CUDA(cudaGraphLaunch(graph_exec_[slot], stream_));
+    SGB_CUDA(cudaEventRecord(done_event_[slot], stream_));
+  };
+  *stop_status = SANKHYA_GB300_ITERATION_LIMIT;
+  // The time limit is checked once before any step, as the reference's loop does.
+  if (has_time_limit && (p.time_limit <= 0.0 || now_seconds() - t0 > p.time_limit)) {
+    *stop_status = SANKHYA_GB300_TIME_LIMIT;
+    return;
+  }
+  launch(0);
+  launch(1);
+  for (long long k = 0;; ++k) {
+    const int slot = static_cast<int>(k & 1);
+    SGB_CUDA(cudaEventSynchronize(done_event_[slot]));
+    const Ctl& snap = snapshot_[slot];
+    if (p.log != nullptr && snap.log_count > logged) {
+      const double elapsed = now_seconds() - t0;
+      long long first = std::max(logged, snap.log_count - kLogRing);
+      for (long long r = first; r < snap.log_count; ++r) {
+        const EvalRecord& rec = snap.log[r % kLogRing];
+        p.log(p.log_user, rec.iteration, sense_ * rec.primal_objective + offset_, rec.primal,
+              rec.dual, elapsed);
+      }
+      logged = snap.log_count;
+    }
+    if (snap.done != kRunning) break;
+    if (has_time_limit && now_seconds() - t0 > p.time_limit) {
+      *stop_status = SANKHYA_GB300_TIME_LIMIT;
+      break;
+    }
+    if (p.interrupt != nullptr && *p.interrupt != 0) {
+      *stop_status = SANKHYA_GB300_INTERRUPTED;
+      break;
+    }
+    launch(slot);
+  }
+  SGB_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void Engine::final_evaluation() {
+  // final_mode = 1: the evaluation kernels evaluate (best_x, best_y) only.
+  const int one = 1;
+  SGB_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(ctl_.ptr) + offsetof(Ctl, final_mode), &one,
+                           sizeof(int), cudaMemcpyHostToDevice, stream_));
+  launch_evaluation(eval_, step_, stream_);
+  SGB_CUDA(cudaGetLastError());
+}
+
+void Engine::solve(const sankhya_gb300_params& p, sankhya_gb300_result* r) {
+  require_loaded();
+  const double t0 = now_seconds();
+  std::memset(r, 0, sizeof(*r));
+  if (p.precision != SANKHYA_GB300_FP64) {
+    throw EngineError{SANKHYA_GB300_ERROR_OPTION, "this build solves pdhg_precision=fp64 only"};
+  }
+  SGB_CUDA(cudaSetDevice(device_));
+  cudaStream_t s = stream_;
+
+  precondition(p.random_seed);
+  const double norm = power_iteration(p.random_seed);
+  {
+    // Scaled entry magnitudes, for the log line of src/pdhg/pdhg.cpp:132-133.
+    const int grid = std::min(num_sms_ * 4, std::max(1, static_cast<int>((nnz_ + 255) / 256)));
+    launch_abs_minmax(csc_s_.ptr, static_cast<int>(nnz_), scalars_.ptr, scalars_.ptr + 2 * grid + 2,
+                      s, grid);
+    double mm[2] = {0.0, 0.0};
+    SGB_CUDA(cudaMemcpyAsync(mm, scalars_.ptr + 2 * grid + 2, 2 * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+    SGB_CUDA(cudaStreamSynchronize(s));
+    r->scaled_max_abs = mm[0];
+    r->scaled_min_abs = mm[1];
+  }
+  r->spectral_norm = norm;
+  init_iterates(p);
+
+  Ctl c;
+  std::memset(&c, 0, sizeof(c));
+  c.eta = norm > 0.0 ? 1.0 / norm : 1.0;
+  c.omega = 1.0;
+  c.spectral_norm = norm;
+  c.eta_ceiling = 1.0e3 / std::max(norm, 1e-12);
+  c.restart_kkt = std::numeric_limits<double>::infinity();
+  c.tolerance = p.tolerance;
+  c.iteration_limit = p.iteration_limit < 0 ? 1000000 : p.iteration_limit;
+  c.use_restarts = p.restart != 0;
+  c.stop_at_request = p.stop_at_request != 0;
+  c.best.primal = c.best.dual = c.best.gap = std::numeric_limits<double>::infinity();
+  SGB_CUDA(cudaMemcpyAsync(ctl_.ptr, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+  SGB_CUDA(cudaStreamSynchronize(s));
+  const double t_loop = now_seconds();
+  r->setup_seconds = t_loop - t0;
+
+  int stop_status = SANKHYA_GB300_ITERATION_LIMIT;
+  run_loop(p, t0, &stop_status);
+  const double t_end_loop = now_seconds();
+  final_evaluation();
+  SGB_CUDA(cudaMemcpyAsync(&c, ctl_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaStreamSynchronize(s));
+  r->loop_seconds = t_end_loop - t_loop;
+
+  const Residuals& f = c.final_residuals;
+  r->final_residuals = sankhya_gb300_residuals{f.primal,          f.dual,           f.gap,
+                                              f.primal_objective, f.dual_objective,
+                                              f.absolute_primal,  f.absolute_dual,
+                                              f.gap_as_verified,  f.complementarity};
+  r->iterations = c.iteration;
+  r->attempts = c.attempts;
+  r->restarts = c.restarts;
+  r->evaluations = c.evaluations;
+  r->converged = c.done == kConverged;
+  const bool converged = c.done == kConverged;
+  const bool verifiable = converged && meets_project_standard(f);
+  std::string message;
+  if (verifiable) {
+    r->status = SANKHYA_GB300_OPTIMAL;
+    message = format(
+        "converged after %lld iterations and %lld restarts; absolute primal %.3e, dual %.3e, "
+        "relative gap %.3e",
+        c.iteration, c.restarts, f.absolute_primal, f.absolute_dual, f.gap_as_verified);
+  } else if (converged) {
+    r->status = SANKHYA_GB300_FEASIBLE;
+    message = format(
+        "met the requested relative tolerance %.1e after %lld iterations, but NOT the absolute "
+        "standard this project verifies against (primal %.3e vs 1.0e-07, dual %.3e vs 1.0e-07, "
+        "relative gap %.3e vs 1.0e-09). Reported as feasible, not optimal. %s",
+        p.tolerance, c.iteration, f.absolute_primal, f.absolute_dual, f.gap_as_verified,
+        p.stop_at_request ? "pdhg_stop_at_request is on, so this is the cheap answer that was "
+                            "asked for; turn it off to run on to the standard"
+                          : "Tighten --option pdhg_tolerance to close it");
+  } else {
+    r->status = stop_status == SANKHYA_GB300_TIME_LIMIT || stop_status == SANKHYA_GB300_INTERRUPTED
+                    ? stop_status
+                    : SANKHYA_GB300_ITERATION_LIMIT;
+    message = format(
+        "stopped at relative primal %.3e, dual %.3e, gap %.3e after %lld iterations and %lld "
+        "restarts (target %.1e)",
+        f.primal, f.dual, f.gap, c.iteration, c.restarts, p.tolerance);
+  }
+  if (verifiable) {
+    r->dual_bound = sense_ * f.dual_objective + offset_;
+  } else {
+    r->dual_bound = sense_ < 0.0 ? std::numeric_limits<double>::infinity()
+                                 : -std::numeric_limits<double>::infinity();
+  }
+  r->objective = offset_ + c.model_objective;
+  std::snprintf(r->message, sizeof(r->message), "%s", message.c_str());
+  solved_ = true;
+  r->solve_seconds = now_seconds() - t0;
+}
+
+void Engine::solution(double* col_value, double* col_dual, double* row_dual) {
+  require_loaded();
+  if (!solved_) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no solve has run"};
+  SGB_CUDA(cudaSetDevice(device_));
+  cudaStream_t s = stream_;
+  std::vector<double> red, by;
+  if (col_value && n_ > 0) {
+    SGB_CUDA(cudaMemcpyAsync(col_value, best_x_.ptr, n_ * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
+  if (col_dual && n_ > 0) {
+    red.resize(static_cast<size_t>(n_));
+    SGB_CUDA(cudaMemcpyAsync(red.data(), reduced_.ptr, n_ * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
+  if (row_dual && m_ > 0) {
+    by.resize(static_cast<size_t>(m_));
+    SGB_CUDA(cudaMemcpyAsync(by.data(), best_y_.ptr, m_ * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
+  SGB_CUDA(cudaStreamSynchronize(s));
+  if (col_dual) {
+    for (int j = 0; j < n_; ++j) col_dual[j] = sense_ * red[j];
+  }
+  if (row_dual) {
+    for (int i = 0; i < m_; ++i) row_dual[i] = sense_ * (-by[i]);
+  }
+}
+
+}  // namespace sgb

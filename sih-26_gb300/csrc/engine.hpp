@@ -1,0 +1,105 @@
+// engine.hpp -- host side of the GB300 PDHG engine (one LP, one device).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "sankhya_gb300.h"
+
+namespace sgb {
+
+// Raised inside the engine and turned into a status code at the C boundary.
+struct EngineError {
+  int code;
+  std::string message;
+};
+
+// Throws EngineError on any CUDA failure, with the call site in the message.
+void cuda_check(cudaError_t err, const char* what, const char* file, int line);
+#define SGB_CUDA(call) ::sgb::cuda_check((call), #call, __FILE__, __LINE__)
+
+template <typename T>
+struct DeviceArray {
+  T* ptr = nullptr;
+  size_t count = 0;
+  DeviceArray() = default;
+  DeviceArray(const DeviceArray&) = delete;
+  DeviceArray& operator=(const DeviceArray&) = delete;
+  ~DeviceArray() { release(); }
+  void allocate(size_t n);
+  void upload(const T* host, size_t n, cudaStream_t s);
+  void release();
+};
+
+class Engine {
+ public:
+  explicit Engine(int device);
+  ~Engine();
+
+  void load(const sankhya_gb300_lp& lp);
+  void solve(const sankhya_gb300_params& params, sankhya_gb300_result* result);
+  void solution(double* col_value, double* col_dual, double* row_dual);
+  void scaling(long long seed, double* row_scale, double* col_scale, double* scaled_values,
+               double* spectral_norm);
+  void spmv(int op, int scaled, const double* in, double* out);
+
+  int device() const { return device_; }
+
+ private:
+  void require_loaded() const;
+  void precondition(long long seed);
+  double power_iteration(long long seed);
+  void init_iterates(const sankhya_gb300_params& p);
+  void build_graphs(int steps);
+  void destroy_graphs();
+  void fill_buffers();
+  void run_loop(const sankhya_gb300_params& p, double t0, int* stop_status);
+  void final_evaluation();
+
+  int device_ = 0;
+  cudaStream_t stream_ = nullptr;
+  int num_sms_ = 0;
+  bool loaded_ = false;
+  bool solved_ = false;
+  bool scaled_ = false;
+
+  // Problem dimensions and host-side scalars.
+  int m_ = 0, n_ = 0;
+  long long nnz_ = 0;
+  double sense_ = 1.0, offset_ = 0.0;
+  double bound_norm_ = 0.0, cost_norm_ = 0.0;
+  int ntiles_csr_ = 0, ntiles_csc_ = 0;
+  int grid_csr_ = 1, grid_csc_ = 1;
+
+  // Pattern (shared by scaled and unscaled values).
+  DeviceArray<int> csc_ptr_, csc_idx_, csr_ptr_, csr_idx_;
+  DeviceArray<int2> csc_tiles_, csr_tiles_;
+  // Values: unscaled (evaluation) and scaled (iterations), both layouts.
+  DeviceArray<double> csc_raw_, csr_raw_, csc_s_, csr_s_;
+  // Unscaled vectors.
+  DeviceArray<double> cost_, col_cost_, l_, u_, rl_, ru_;
+  // Scaled vectors and scaling.
+  DeviceArray<double> cs_, ls_, us_, rls_, rus_, dr_, dc_, row_acc_, col_acc_;
+  // Iterates.
+  DeviceArray<double> x0_, x1_, y0_, y1_, x_sum_, y_sum_, x_rst_, y_rst_;
+  DeviceArray<double> xu0_, xu1_, yu0_, yu1_, reduced_, best_x_, best_y_;
+  // Reductions.
+  DeviceArray<double> part_primal_, part_dual_, part_rows0_, part_cols_, part_rows1_;
+  DeviceArray<double> scalars_, power_v_, power_av_, power_norms_;
+  DeviceArray<Ctl> ctl_;
+
+  Ctl* snapshot_ = nullptr;  // pinned host, two slots
+  cudaGraphExec_t graph_exec_[2] = {nullptr, nullptr};
+  int graph_steps_ = 0;
+  cudaEvent_t done_event_[2] = {nullptr, nullptr};
+
+  StepBuffers step_{};
+  EvalBuffers eval_{};
+};
+
+size_t estimate_memory(long long rows, long long cols, long long nnz, int precision);
+
+}  // namespace sgb

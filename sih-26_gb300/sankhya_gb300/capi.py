@@ -1,0 +1,299 @@
+"""ctypes binding of include/sankhya_gb300.h (lib/libsankhya_gb300.so).
+
+There is no CPU fallback: if the library is missing or no GPU is usable, every call raises
+``EngineError``. ``solve_pdhg_gpu(lp, options)`` mirrors the reference seam
+``sankhya::gpu::solve_pdhg_gpu(model, options, logger, control)`` (src/gpu/pdhg_gpu.hpp:19)
+and takes the reference's option names (src/util/options.cpp): ``pdhg_tolerance``,
+``iteration_limit``, ``time_limit``, ``pdhg_restart``, ``pdhg_stop_at_request``,
+``random_seed``, plus the engine's ``pdhg_precision`` ("fp64" | "mixed").
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+from dataclasses import dataclass, field
+from typing import Callable, Optional
+
+import numpy as np
+
+from . import _paths
+from .model import LP
+
+OK = 0
+STATUS_NAMES = {0: "not_solved", 1: "optimal", 2: "feasible", 3: "infeasible",
+                5: "iteration_limit", 6: "time_limit", 8: "numerical_error", 9: "model_error",
+                11: "interrupted"}
+PRECISIONS = {"fp64": 0, "mixed": 1}
+
+_D = ctypes.POINTER(ctypes.c_double)
+_I = ctypes.POINTER(ctypes.c_int32)
+LOG_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_double,
+                          ctypes.c_double, ctypes.c_double, ctypes.c_double)
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+class CLp(ctypes.Structure):
+    _fields_ = [("rows", ctypes.c_int32), ("cols", ctypes.c_int32), ("col_starts", _I),
+                ("row_index", _I), ("values", _D), ("col_cost", _D), ("col_lower", _D),
+                ("col_upper", _D), ("row_lower", _D), ("row_upper", _D),
+                ("sense", ctypes.c_double), ("objective_offset", ctypes.c_double)]
+
+
+class CParams(ctypes.Structure):
+    _fields_ = [("tolerance", ctypes.c_double), ("iteration_limit", ctypes.c_int64),
+                ("time_limit", ctypes.c_double), ("restart", ctypes.c_int32),
+                ("stop_at_request", ctypes.c_int32), ("random_seed", ctypes.c_int64),
+                ("precision", ctypes.c_int32), ("steps_per_poll", ctypes.c_int32),
+                ("interrupt", ctypes.POINTER(ctypes.c_int32)), ("log", LOG_FN),
+                ("log_user", ctypes.c_void_p)]
+
+
+class CResiduals(ctypes.Structure):
+    _fields_ = [(k, ctypes.c_double) for k in (
+        "primal", "dual", "gap", "primal_objective", "dual_objective", "absolute_primal",
+        "absolute_dual", "gap_as_verified", "complementarity")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class CResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("converged", ctypes.c_int32),
+                ("iterations", ctypes.c_int64), ("attempts", ctypes.c_int64),
+                ("restarts", ctypes.c_int64), ("evaluations", ctypes.c_int64),
+                ("refinements", ctypes.c_int64), ("objective", ctypes.c_double),
+                ("dual_bound", ctypes.c_double), ("final_residuals", CResiduals),
+                ("spectral_norm", ctypes.c_double), ("scaled_min_abs", ctypes.c_double),
+                ("scaled_max_abs", ctypes.c_double), ("setup_seconds", ctypes.c_double),
+                ("loop_seconds", ctypes.c_double), ("solve_seconds", ctypes.c_double),
+                ("message", ctypes.c_char * 512)]
+
+
+EXPORTS = [
+    "sankhya_gb300_last_error", "sankhya_gb300_device_available",
+    "sankhya_gb300_device_free_memory", "sankhya_gb300_device_compute_capability",
+    "sankhya_gb300_estimate_memory", "sankhya_gb300_pdhg_create", "sankhya_gb300_pdhg_destroy",
+    "sankhya_gb300_pdhg_load", "sankhya_gb300_pdhg_solve", "sankhya_gb300_pdhg_solution",
+    "sankhya_gb300_pdhg_scaling", "sankhya_gb300_pdhg_spmv",
+]
+
+_lib = None
+_lock = threading.Lock()
+
+
+def library_path() -> str:
+    return _paths.ENGINE_LIB
+
+
+def load_library():
+    """Load the engine library (raises if it is not built: there is no fallback)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(_paths.ENGINE_LIB):
+            raise EngineError(7, f"{_paths.ENGINE_LIB} is not built; run __graft_entry__.build()")
+        lib = ctypes.CDLL(_paths.ENGINE_LIB)
+        lib.sankhya_gb300_last_error.restype = ctypes.c_char_p
+        lib.sankhya_gb300_last_error.argtypes = []
+        lib.sankhya_gb300_device_available.argtypes = [ctypes.c_char_p, ctypes.c_int32]
+        lib.sankhya_gb300_device_free_memory.argtypes = [ctypes.POINTER(ctypes.c_size_t)] * 2
+        lib.sankhya_gb300_device_compute_capability.argtypes = [ctypes.POINTER(ctypes.c_int32)] * 2
+        lib.sankhya_gb300_estimate_memory.argtypes = [ctypes.c_int32, ctypes.c_int32,
+                                                      ctypes.c_int64, ctypes.c_int32]
+        lib.sankhya_gb300_estimate_memory.restype = ctypes.c_size_t
+        lib.sankhya_gb300_pdhg_create.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]
+        lib.sankhya_gb300_pdhg_destroy.argtypes = [ctypes.c_void_p]
+        lib.sankhya_gb300_pdhg_load.argtypes = [ctypes.c_void_p, ctypes.POINTER(CLp)]
+        lib.sankhya_gb300_pdhg_solve.argtypes = [ctypes.c_void_p, ctypes.POINTER(CParams),
+                                                 ctypes.POINTER(CResult)]
+        lib.sankhya_gb300_pdhg_solution.argtypes = [ctypes.c_void_p, _D, _D, _D]
+        lib.sankhya_gb300_pdhg_scaling.argtypes = [ctypes.c_void_p, ctypes.c_int64, _D, _D, _D, _D]
+        lib.sankhya_gb300_pdhg_spmv.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                                _D, _D]
+        for name in EXPORTS:
+            if name not in ("sankhya_gb300_last_error", "sankhya_gb300_estimate_memory"):
+                getattr(lib, name).restype = ctypes.c_int
+        _lib = lib
+        return lib
+
+
+def _check(code: int):
+    if code != OK:
+        msg = load_library().sankhya_gb300_last_error().decode(errors="replace")
+        raise EngineError(code, msg)
+
+
+def _ptr(a, ctype=ctypes.c_double):
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def device_available() -> tuple[bool, str]:
+    lib = load_library()
+    buf = ctypes.create_string_buffer(256)
+    ok = lib.sankhya_gb300_device_available(buf, 256) == OK
+    return ok, buf.value.decode(errors="replace")
+
+
+def estimate_memory(rows: int, cols: int, nnz: int, precision: str = "fp64") -> int:
+    return int(load_library().sankhya_gb300_estimate_memory(rows, cols, nnz,
+                                                            PRECISIONS[precision]))
+
+
+@dataclass
+class Result:
+    status: int
+    status_name: str
+    converged: bool
+    iterations: int
+    attempts: int
+    restarts: int
+    evaluations: int
+    refinements: int
+    objective: float
+    dual_bound: float
+    residuals: dict
+    spectral_norm: float
+    scaled_min_abs: float
+    scaled_max_abs: float
+    setup_seconds: float
+    loop_seconds: float
+    solve_seconds: float
+    message: str
+
+
+class PdhgEngine:
+    """One engine on one device: load an LP once, solve it any number of times."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self._lib.sankhya_gb300_pdhg_create(device, ctypes.byref(h)))
+        self._h = h
+        self._lp: Optional[LP] = None
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.sankhya_gb300_pdhg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def load(self, lp: LP):
+        lp = lp.contiguous()
+        c = CLp(lp.rows, lp.cols, _ptr(lp.col_starts, ctypes.c_int32),
+                _ptr(lp.row_index, ctypes.c_int32), _ptr(lp.values), _ptr(lp.col_cost),
+                _ptr(lp.col_lower), _ptr(lp.col_upper), _ptr(lp.row_lower), _ptr(lp.row_upper),
+                lp.sense, lp.objective_offset)
+        _check(self._lib.sankhya_gb300_pdhg_load(self._h, ctypes.byref(c)))
+        self._lp = lp
+
+    def solve(self, tolerance: float = 1e-4, iteration_limit: int = -1,
+              time_limit: Optional[float] = None, restart: bool = True,
+              stop_at_request: bool = False, random_seed: int = 0, precision: str = "fp64",
+              steps_per_poll: int = 0, interrupt: Optional[np.ndarray] = None,
+              log: Optional[Callable] = None) -> Result:
+        cb = LOG_FN(lambda user, it, obj, p, d, s: log(it, obj, p, d, s)) if log else LOG_FN()
+        intr = (interrupt.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+                if interrupt is not None else ctypes.POINTER(ctypes.c_int32)())
+        params = CParams(tolerance, iteration_limit,
+                         1e308 if time_limit is None else float(time_limit), int(restart),
+                         int(stop_at_request), random_seed, PRECISIONS[precision],
+                         steps_per_poll, intr, cb, None)
+        r = CResult()
+        _check(self._lib.sankhya_gb300_pdhg_solve(self._h, ctypes.byref(params), ctypes.byref(r)))
+        return Result(r.status, STATUS_NAMES.get(r.status, str(r.status)), bool(r.converged),
+                      r.iterations, r.attempts, r.restarts, r.evaluations, r.refinements,
+                      r.objective, r.dual_bound, r.final_residuals.as_dict(), r.spectral_norm,
+                      r.scaled_min_abs, r.scaled_max_abs, r.setup_seconds, r.loop_seconds,
+                      r.solve_seconds, r.message.decode(errors="replace"))
+
+    def solution(self):
+        lp = self._lp
+        x = np.zeros(lp.cols)
+        d = np.zeros(lp.cols)
+        y = np.zeros(lp.rows)
+        _check(self._lib.sankhya_gb300_pdhg_solution(self._h, _ptr(x), _ptr(d), _ptr(y)))
+        return x, d, y
+
+    def scaling(self, random_seed: int = 0):
+        lp = self._lp
+        dr = np.zeros(lp.rows)
+        dc = np.zeros(lp.cols)
+        vals = np.zeros(lp.nnz)
+        norm = ctypes.c_double()
+        _check(self._lib.sankhya_gb300_pdhg_scaling(self._h, random_seed, _ptr(dr), _ptr(dc),
+                                                    _ptr(vals), ctypes.byref(norm)))
+        return dr, dc, vals, norm.value
+
+    def spmv(self, op: int, vec, scaled: bool = False):
+        lp = self._lp
+        vec = np.ascontiguousarray(vec, dtype=np.float64)
+        out = np.zeros(lp.rows if op == 0 else lp.cols)
+        _check(self._lib.sankhya_gb300_pdhg_spmv(self._h, op, int(scaled), _ptr(vec), _ptr(out)))
+        return out
+
+
+@dataclass
+class Solution:
+    """The fields of sankhya::Solution that solve_pdhg fills (src/pdhg/pdhg.cpp:487-558)."""
+    status: str
+    objective: float
+    dual_bound: float
+    col_value: np.ndarray
+    col_dual: np.ndarray
+    row_dual: np.ndarray
+    iterations: int
+    message: str
+    algorithm: str = "pdhg-gpu"
+    result: Optional[Result] = None
+    extra: dict = field(default_factory=dict)
+
+
+def solve_pdhg_gpu(lp: LP, options: Optional[dict] = None, device: int = 0,
+                   engine: Optional[PdhgEngine] = None, log: Optional[Callable] = None,
+                   interrupt: Optional[np.ndarray] = None) -> Solution:
+    """The GPU PDHG behind the reference seam's contract: never falls back to the CPU; a
+    model defect is status "model_error", a device failure raises EngineError."""
+    o = {"pdhg_tolerance": 1e-4, "iteration_limit": -1, "time_limit": None,
+         "pdhg_restart": True, "pdhg_stop_at_request": False, "random_seed": 0,
+         "pdhg_precision": "fp64", "steps_per_poll": 0}
+    o.update(options or {})
+    own = engine is None
+    eng = engine or PdhgEngine(device)
+    try:
+        try:
+            eng.load(lp)
+        except EngineError as e:
+            if e.code == 3:
+                z = np.zeros
+                return Solution("model_error", 0.0, float("nan"), z(lp.cols), z(lp.cols),
+                                z(lp.rows), 0, str(e))
+            raise
+        r = eng.solve(tolerance=o["pdhg_tolerance"], iteration_limit=o["iteration_limit"],
+                      time_limit=o["time_limit"], restart=o["pdhg_restart"],
+                      stop_at_request=o["pdhg_stop_at_request"], random_seed=o["random_seed"],
+                      precision=o["pdhg_precision"], steps_per_poll=o["steps_per_poll"],
+                      interrupt=interrupt, log=log)
+        x, d, y = eng.solution()
+        return Solution(r.status_name, r.objective, r.dual_bound, x, d, y, r.iterations,
+                        r.message, "pdhg-gpu", r)
+    finally:
+        if own:
+            eng.close()

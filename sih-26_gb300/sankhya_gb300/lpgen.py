@@ -1,0 +1,110 @@
+"""Seeded planted-optimum LP generators (ctypes over lpgen/lpgen.c).
+
+The shapes follow the synthetic workloads this engine is measured on:
+
+* ``planted_uniform(m, n, k, seed)`` -- m x n, exactly k distinct uniform rows per column,
+  N(0,1) values, equality rows, 0 <= x <= 10 (the 2,000 x 5,000 parity case, the batched
+  and the differentiation cases).
+* ``planted_blocks(blocks, R, C, k, seed)`` -- block-angular multi-period structure with one
+  +-1 inventory link per column into the next period (64 x 15,625 x 31,250 with k = 9 is the
+  1,000,000 x 2,000,000 headline case).
+* ``planted_general(m, n, k, seed)`` -- every row and column kind, for coverage.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _paths
+from .model import LP
+
+_lib = None
+
+
+class _CLp(ctypes.Structure):
+    _fields_ = [
+        ("rows", ctypes.c_int32), ("cols", ctypes.c_int32), ("nnz", ctypes.c_int64),
+        ("col_starts", ctypes.c_void_p), ("row_index", ctypes.c_void_p),
+        ("values", ctypes.c_void_p), ("col_cost", ctypes.c_void_p),
+        ("col_lower", ctypes.c_void_p), ("col_upper", ctypes.c_void_p),
+        ("row_lower", ctypes.c_void_p), ("row_upper", ctypes.c_void_p),
+        ("x0", ctypes.c_void_p), ("lam", ctypes.c_void_p), ("fstar", ctypes.c_double),
+    ]
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_paths.LPGEN_LIB):
+            raise RuntimeError(f"{_paths.LPGEN_LIB} is not built; run __graft_entry__.build()")
+        lib = ctypes.CDLL(_paths.LPGEN_LIB)
+        for name in ("lpgen_planted_uniform", "lpgen_planted_general"):
+            getattr(lib, name).argtypes = [ctypes.c_int32] * 3 + [ctypes.c_uint64,
+                                                                  ctypes.POINTER(_CLp)]
+            getattr(lib, name).restype = ctypes.c_int32
+            getattr(lib, name + "_nnz").argtypes = [ctypes.c_int32] * 3
+            getattr(lib, name + "_nnz").restype = ctypes.c_int64
+        lib.lpgen_planted_blocks.argtypes = [ctypes.c_int32] * 4 + [ctypes.c_uint64,
+                                                                    ctypes.POINTER(_CLp)]
+        lib.lpgen_planted_blocks.restype = ctypes.c_int32
+        lib.lpgen_planted_blocks_nnz.argtypes = [ctypes.c_int32] * 4
+        lib.lpgen_planted_blocks_nnz.restype = ctypes.c_int64
+        _lib = lib
+    return _lib
+
+
+def _alloc(m, n, nnz):
+    arrays = dict(
+        col_starts=np.zeros(n + 1, np.int32), row_index=np.zeros(nnz, np.int32),
+        values=np.zeros(nnz), col_cost=np.zeros(n), col_lower=np.zeros(n),
+        col_upper=np.zeros(n), row_lower=np.zeros(m), row_upper=np.zeros(m), x0=np.zeros(n),
+        lam=np.zeros(m))
+    c = _CLp()
+    for key, arr in arrays.items():
+        setattr(c, key, arr.ctypes.data)
+    return arrays, c
+
+
+def _finish(arrays, c, name, sense=1.0):
+    a = arrays
+    return LP(int(c.rows), int(c.cols), a["col_starts"], a["row_index"], a["values"],
+              a["col_cost"], a["col_lower"], a["col_upper"], a["row_lower"], a["row_upper"],
+              sense, 0.0, a["x0"], a["lam"], float(c.fstar), name)
+
+
+def planted_uniform(m: int, n: int, k: int = 5, seed: int = 1) -> LP:
+    lib = _load()
+    nnz = lib.lpgen_planted_uniform_nnz(m, n, k)
+    arrays, c = _alloc(m, n, nnz)
+    if lib.lpgen_planted_uniform(m, n, k, seed, ctypes.byref(c)) != 0:
+        raise ValueError(f"planted_uniform: bad shape m={m} n={n} k={k}")
+    return _finish(arrays, c, f"planted_uniform_{m}x{n}_k{k}_s{seed}")
+
+
+def planted_blocks(blocks: int, rows_per_block: int, cols_per_block: int, k: int = 9,
+                   seed: int = 1) -> LP:
+    lib = _load()
+    nnz = lib.lpgen_planted_blocks_nnz(blocks, rows_per_block, cols_per_block, k)
+    m, n = blocks * rows_per_block, blocks * cols_per_block
+    arrays, c = _alloc(m, n, nnz)
+    if lib.lpgen_planted_blocks(blocks, rows_per_block, cols_per_block, k, seed,
+                                ctypes.byref(c)) != 0:
+        raise ValueError("planted_blocks: bad shape")
+    return _finish(arrays, c, f"planted_blocks_{blocks}x{rows_per_block}x{cols_per_block}")
+
+
+def planted_general(m: int, n: int, k: int = 4, seed: int = 1, maximize: bool = False) -> LP:
+    """Mixed row and column kinds. With ``maximize`` the cost is negated and the sense set
+    to maximise, so the optimum point is unchanged and the objective is ``-fstar``."""
+    lib = _load()
+    nnz = lib.lpgen_planted_general_nnz(m, n, k)
+    arrays, c = _alloc(m, n, nnz)
+    if lib.lpgen_planted_general(m, n, k, seed, ctypes.byref(c)) != 0:
+        raise ValueError("planted_general: bad shape")
+    lp = _finish(arrays, c, f"planted_general_{m}x{n}_s{seed}")
+    if maximize:
+        lp.col_cost = -lp.col_cost
+        lp.sense = -1.0
+    return lp

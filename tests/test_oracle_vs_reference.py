@@ -1,0 +1,65 @@
+"""The oracle (oracle/pdhg_oracle.c) against the reference's own PDHG, compiled from its
+sources into oracle/_ref/, on identical inputs: every result must be bit-identical
+(src/pdhg/pdhg.cpp, src/la/scaling.cpp, src/pdhg/pdhg_evaluate.cpp)."""
+import numpy as np
+import pytest
+
+from sankhya_gb300 import lpgen
+from sankhya_gb300.model import from_dense
+
+INF = np.inf
+
+
+def _cases():
+    yield "uniform_200x500", lpgen.planted_uniform(200, 500, 5, seed=3), dict(tolerance=1e-8)
+    for s in range(3):
+        yield (f"general_{s}", lpgen.planted_general(40, 60, 3, seed=s, maximize=s == 1),
+               dict(tolerance=1e-8, iteration_limit=20000))
+    yield "sum", from_dense([[1, 1]], [2], [INF], [1, 1]), dict(tolerance=1e-8)
+    yield ("max_3x2", from_dense([[1, 0], [0, 2], [3, 2]], [-INF] * 3, [4, 12, 18], [3, 5],
+                                 sense=-1), dict(tolerance=1e-8))
+    yield "big_rhs", from_dense([[1, 1]], [1e5], [INF], [1, 1]), dict(tolerance=1e-4)
+    yield ("iteration_limit", from_dense([[1, 1]], [2], [INF], [1, 1]),
+           dict(tolerance=1e-12, iteration_limit=20))
+    yield ("stop_at_request", lpgen.planted_uniform(100, 250, 5, seed=9),
+           dict(tolerance=1e-6, stop_at_request=True))
+    yield ("no_restarts", lpgen.planted_uniform(100, 250, 5, seed=9),
+           dict(tolerance=1e-8, restart=False, iteration_limit=3000))
+    yield ("seed_5", lpgen.planted_uniform(100, 250, 5, seed=9),
+           dict(tolerance=1e-6, random_seed=5))
+
+
+@pytest.mark.parametrize("name,lp,kw", list(_cases()), ids=[c[0] for c in _cases()])
+def test_solve_is_bit_identical(reference, oracle, name, lp, kw):
+    a = oracle.solve(lp, **kw)
+    b = reference.solve(lp, **kw)
+    assert a.status == b.status, (a.status_name, b.status_name, b.message)
+    assert a.iterations == b.iterations
+    if b.restarts >= 0:  # the feasible-status message carries no restart count
+        assert a.restarts == b.restarts
+    assert a.objective == b.objective
+    assert a.dual_bound == b.dual_bound or (np.isinf(a.dual_bound) and np.isinf(b.dual_bound))
+    assert np.array_equal(a.col_value, b.col_value)
+    assert np.array_equal(a.col_dual, b.col_dual)
+    assert np.array_equal(a.row_dual, b.row_dual)
+
+
+def test_scaling_and_norm_are_bit_identical(reference, oracle):
+    lp = lpgen.planted_blocks(4, 60, 120, 9, seed=11)
+    a = oracle.build_scaling(lp)
+    b = reference.build_scaling(lp)
+    for k in ("values", "row", "col", "cost", "col_lower", "col_upper", "row_lower", "row_upper",
+              "min_abs", "max_abs"):
+        assert np.array_equal(a[k], b[k]), k
+    assert oracle.spectral_norm(lp, 30, 1) == reference.spectral_norm(lp, 30, 1)
+
+
+def test_evaluate_is_bit_identical(reference, oracle):
+    lp = lpgen.planted_general(50, 80, 3, seed=4)
+    rng = np.random.default_rng(0)
+    x = rng.normal(size=lp.cols)
+    y = rng.normal(size=lp.rows)
+    ra, aa, da = oracle.evaluate(lp, x, y)
+    rb, ab, db = reference.evaluate(lp, x, y)
+    assert ra == rb
+    assert np.array_equal(aa, ab) and np.array_equal(da, db)
