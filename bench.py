@@ -1,0 +1,308 @@
+"""Benchmark: seconds to relative KKT 1e-8 for restarted PDHG on one GB300.
+
+Workload: the block-angular multi-period planted-optimum LP -- 64 periods of 15,625 rows x
+31,250 columns, 9 N(0,1) entries per column inside its period plus one +-1 inventory link
+into the next period: m = 1,000,000, n = 2,000,000, 19,968,750 nonzeros, 0 <= x <= 10,
+equality rows (seeded synthetic data; the optimum f* = c.x0 is planted).
+
+A STEP is one complete solve of that LP to relative KKT 1e-8 (the reference's default
+stopping rule: relative KKT AND the absolute project standard) from the LP already resident
+in HBM -- device preconditioning, the PDHG loop, the final evaluation. `value` is the
+headline method's seconds per solve (CUDA events on the engine's stream, max over ranks);
+the FP64 method is timed on the same LP beside it. The matrix (480 MB per value copy) is far
+larger than L2, so no L2 flush is needed between steps.
+
+Also reported: per-kernel achieved HBM GB/s against the measured copy bandwidth (roofline),
+an end-to-end solve through the C ABI from host buffers (copies included), clocks sampled
+during the timed region, and the reference algorithm (the CPU oracle, on this host's cores)
+on a bounded sample.
+
+Multi-GPU: the path does not shard (one LP per device); N ranks run N independent replicas.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for sub in ("sih-26_gb300", "oracle"):
+    sys.path.insert(0, os.path.join(ROOT, sub))
+
+METRIC = "sec to rel KKT 1e-8, mixed vs FP64 PDHG on 1 GB300; SpMV HBM GB/s; LPs/s"
+WORKLOAD = dict(blocks=64, rows_per_block=15625, cols_per_block=31250, k=9, seed=2026)
+TOLERANCE = 1e-8
+# FP64 iterations to relative KKT 1e-8 on this workload (the GPU engine's FP64 method, whose
+# step, restart and weight rules are the reference's); used to turn the CPU reference's
+# measured seconds per iteration into seconds to 1e-8.
+FP64_ITERATIONS_TO_1E8 = None
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes(m, n, nnz, v, w):
+    """Per attempted step (the minimal fused form): column pass = (v+4) nnz + 4 (n+1)
+    + w (m gathered + 7 n); row pass = (v+4) nnz + 4 (m+1) + w (2 n gathered + 6 m)."""
+    col = (v + 4) * nnz + 4 * (n + 1) + w * (m + 7 * n)
+    row = (v + 4) * nnz + 4 * (m + 1) + w * (2 * n + 6 * m)
+    return col, row
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.TemporaryFile(mode="w+")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.file,
+                stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.seek(0)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.file:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        return rank, world, local, dist
+    return rank, world, local, None
+
+
+def make_workload():
+    from sankhya_gb300 import lpgen
+
+    return lpgen.planted_blocks(WORKLOAD["blocks"], WORKLOAD["rows_per_block"],
+                                WORKLOAD["cols_per_block"], WORKLOAD["k"], WORKLOAD["seed"])
+
+
+def workload_config(lp, precision):
+    return {"workload": f"block-angular planted LP {lp.rows:,} x {lp.cols:,}, {lp.nnz:,} nnz, "
+                        f"{WORKLOAD['blocks']} periods",
+            "tolerance": TOLERANCE, "precision": precision,
+            "stopping": "relative KKT <= 1e-8 and the absolute project standard",
+            "step": "one complete solve from the HBM-resident LP",
+            "l2": "inputs larger than L2 (matrix values 160-480 MB per copy); no flush"}
+
+
+def cpu_reference(lp, iterations_sample, threads):
+    """The reference algorithm on this host: the oracle (C restatement, OpenMP A^T y like the
+    reference) -- setup alone, then setup + a few iterations; seconds to 1e-8 are
+    setup + per-iteration x the FP64 iteration count."""
+    import pyoracle
+
+    pyoracle.build()
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    o = pyoracle.Oracle()
+    t0 = time.perf_counter()
+    o.solve(lp, tolerance=TOLERANCE, iteration_limit=0)
+    setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    r = o.solve(lp, tolerance=TOLERANCE, iteration_limit=iterations_sample)
+    sampled = time.perf_counter() - t0
+    per_it = max(sampled - setup, 0.0) / max(1, r.iterations)
+    return setup, per_it, sampled + setup
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-iterations", type=int, default=20)
+    args = ap.parse_args()
+    rank, world, local, dist = dist_setup()
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        lp = make_workload()
+        iters = FP64_ITERATIONS_TO_1E8
+        values = []
+        for step in range(args.warmup + args.steps):
+            setup, per_it, sample_s = cpu_reference(lp, max(2, args.cpu_iterations // 4), threads)
+            if step >= args.warmup:
+                values.append(setup + per_it * (iters or 0))
+        value = max(values) if iters else None
+        line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "config": workload_config(lp, "fp64"),
+                "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
+                                 "sample": f"setup + {max(2, args.cpu_iterations // 4)} "
+                                           f"iterations per step, extrapolated to "
+                                           f"{iters} FP64 iterations"},
+                "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    from sankhya_gb300 import build, capi
+
+    build.build_lpgen()
+    build.build_engine()
+    lp = make_workload()
+    eng = capi.PdhgEngine(local)
+    eng.load(lp)
+    opts = dict(tolerance=TOLERANCE)
+
+    for _ in range(args.warmup):
+        eng.solve(precision=args.precision, **opts)
+    if dist:
+        dist.barrier()
+    results = []
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            results.append(eng.solve(precision=args.precision, **opts))
+    if dist:
+        dist.barrier()
+    secs = [r.device_seconds for r in results]
+    step_s = max(secs)
+    last = results[-1]
+    launches = sum(r.kernel_launches for r in results)
+
+    # FP64 beside it when the headline is mixed (same LP, one warm + one timed solve).
+    fp64 = None
+    if args.precision != "fp64":
+        eng.solve(precision="fp64", **opts)
+        f = eng.solve(precision="fp64", **opts)
+        fp64 = {"seconds": f.device_seconds, "iterations": f.iterations, "status": f.status_name,
+                "objective": f.objective}
+
+    # Per-kernel roofline on the state of the last solve.
+    ms_primal, ms_dual = eng.time_kernels(20)
+    v = w = 8 if args.precision == "fp64" else 4
+    b_col, b_row = algorithmic_bytes(lp.rows, lp.cols, lp.nnz, v, w)
+    peak, peak_kind = peaks()
+    gbs_primal = b_col / (ms_primal * 1e-3) / 1e9
+    gbs_dual = b_row / (ms_dual * 1e-3) / 1e9
+    dominant = ("k_dual (row pass: A xbar, A dx, dual update)", gbs_dual, b_row, ms_dual) \
+        if ms_dual >= ms_primal else ("k_primal (column pass: A^T y, primal update)", gbs_primal,
+                                      b_col, ms_primal)
+
+    # End to end through the C ABI from host buffers: load (H2D), solve, solution (D2H).
+    t0 = time.perf_counter()
+    eng2 = capi.PdhgEngine(local)
+    eng2.load(lp)
+    r2 = eng2.solve(precision=args.precision, **opts)
+    x, d, y = eng2.solution()
+    e2e_s = time.perf_counter() - t0
+    eng2.close()
+    h2d = (lp.col_starts.nbytes + lp.row_index.nbytes + lp.values.nbytes + lp.col_cost.nbytes
+           + lp.col_lower.nbytes + lp.col_upper.nbytes + lp.row_lower.nbytes
+           + lp.row_upper.nbytes)
+    d2h = x.nbytes + d.nbytes + y.nbytes
+
+    if dist:
+        import torch
+
+        t = torch.tensor([step_s, e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_s, e2e_s = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        setup, per_it, sample_s = cpu_reference(lp, args.cpu_iterations, threads)
+        its = fp64["iterations"] if fp64 else last.iterations
+        cpu = {"value": setup + per_it * its, "unit": "s", "cores": threads, "kind": "port",
+               "sample": f"oracle setup + {args.cpu_iterations} FP64 iterations "
+                         f"({sample_s:.1f} s of CPU work), extrapolated to {its} iterations",
+               "setup_s": setup, "s_per_iteration": per_it}
+
+    line = {
+        "metric": METRIC, "value": step_s, "unit": "s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic (seeded planted-optimum generator)",
+        "config": workload_config(lp, args.precision),
+        "status": last.status_name, "iterations": last.iterations, "attempts": last.attempts,
+        "restarts": last.restarts, "objective": last.objective, "fstar": lp.fstar,
+        "objective_rel_err": abs(last.objective - lp.fstar) / max(1.0, abs(lp.fstar)),
+        "relative_kkt": max(last.residuals["primal"], last.residuals["dual"],
+                            last.residuals["gap"]),
+        "setup_s": last.setup_seconds, "loop_s": last.loop_seconds,
+        "us_per_attempt": 1e6 * last.loop_seconds / max(1, last.attempts),
+        "fp64": fp64,
+        "spmv_gbs": {"k_primal": gbs_primal, "k_dual": gbs_dual,
+                     "k_primal_ms": ms_primal, "k_dual_ms": ms_dual, "peak": peak,
+                     "peak_kind": peak_kind},
+        "lps_per_s": world / step_s,
+        "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": dominant[1],
+                     "peak": peak, "unit": "GB/s", "frac": dominant[1] / peak,
+                     "traffic": None, "algorithmic_bytes": dominant[2],
+                     "peak_source": peak_kind},
+        "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "status": r2.status_name},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -61,6 +61,17 @@ enum {
   SANKHYA_GB300_MIXED = 1  /* FP32 iterates / values / SpMV, FP64 KKT and refinement */
 };
 
+/* When the loop stops (new option row `pdhg_stop_rule`). STANDARD is the reference's test
+ * (src/pdhg/pdhg.cpp:424-425): the request (relative primal, dual, gap <= tolerance and
+ * absolute primal <= 1e-7) and, unless stop_at_request, the absolute project standard.
+ * RELATIVE stops as soon as the relative KKT error max(primal, dual, gap) <= tolerance.
+ * Either way the status is `optimal` only if the reported point meets the project
+ * standard, else `feasible` (src/pdhg/pdhg.cpp:515-536). */
+enum {
+  SANKHYA_GB300_STOP_STANDARD = 0,
+  SANKHYA_GB300_STOP_RELATIVE = 1
+};
+
 /* An LP in sankhya::Model's layout (include/sankhya/model.hpp:123-170): CSC, int32 indices
  * ascending inside each column, FP64 values, rows rl <= Ax <= ru, columns l <= x <= u; an
  * infinite bound is +-inf or any magnitude >= 1e30. */
@@ -93,6 +104,8 @@ typedef struct sankhya_gb300_params {
   int64_t random_seed;       /* random_seed (power-iteration start, scaling.cpp:168) */
   int32_t precision;         /* SANKHYA_GB300_FP64 or SANKHYA_GB300_MIXED */
   int32_t steps_per_poll;    /* attempted steps per CUDA-graph launch; 0 = default */
+  int32_t stop_rule;         /* SANKHYA_GB300_STOP_STANDARD or SANKHYA_GB300_STOP_RELATIVE */
+  int32_t reserved;
   const volatile int32_t* interrupt; /* SolveControl::interrupt flag, polled; may be NULL */
   sankhya_gb300_log_fn log;  /* may be NULL */
   void* log_user;
@@ -121,7 +134,9 @@ typedef struct sankhya_gb300_result {
   double scaled_min_abs, scaled_max_abs;
   double setup_seconds;  /* scaling + power iteration on the device */
   double loop_seconds;   /* the PDHG loop */
-  double solve_seconds;  /* the whole solve call */
+  double solve_seconds;  /* the whole solve call, host clock */
+  double device_seconds; /* the whole solve, CUDA events on the engine's stream */
+  int64_t kernel_launches; /* engine kernels launched by this solve (graph nodes included) */
   char message[512];
 } sankhya_gb300_result;
 
@@ -171,6 +186,13 @@ SGB_API int sankhya_gb300_pdhg_scaling(sankhya_gb300_pdhg* engine, int64_t rando
                                        double* scaled_values, double* spectral_norm);
 SGB_API int sankhya_gb300_pdhg_spmv(sankhya_gb300_pdhg* engine, int32_t op, int32_t scaled,
                                     const double* in, double* out);
+
+/* Measurement hook: time `reps` attempted PDHG steps on the state the last solve left,
+ * each kernel bracketed by CUDA events on the engine's stream. ms[0] = mean duration of the
+ * primal (column) pass, ms[1] = mean duration of the dual (row) pass, in milliseconds. The
+ * solve's results are restored afterwards. */
+SGB_API int sankhya_gb300_pdhg_time_kernels(sankhya_gb300_pdhg* engine, int32_t reps,
+                                            double* ms);
 
 #ifdef __cplusplus
 }

@@ -156,4 +156,12 @@ SGB_API int sankhya_gb300_pdhg_spmv(sankhya_gb300_pdhg* engine, int32_t op, int3
   return guarded([&] { engine->engine->spmv(op, scaled, in, out); });
 }
 
+SGB_API int sankhya_gb300_pdhg_time_kernels(sankhya_gb300_pdhg* engine, int32_t reps,
+                                            double* ms) {
+  if (engine == nullptr || ms == nullptr || reps <= 0) {
+    return fail(SANKHYA_GB300_ERROR_ARGUMENT, "bad time_kernels arguments");
+  }
+  return guarded([&] { engine->engine->time_kernels(reps, ms); });
+}
+
 }  // extern "C"

@@ -27,6 +27,15 @@ __host__ __device__ __forceinline__ T project(T v, T lo, T hi) {
   return v;
 }
 
+// Projection onto [lo, hi] when an absent side is an IEEE infinity (lo <= hi): the same
+// value as project() for every non-NaN input, in two min/max instructions.
+__device__ __forceinline__ double clamp_box(double v, double lo, double hi) {
+  return fmin(fmax(v, lo), hi);
+}
+__device__ __forceinline__ float clamp_box(float v, float lo, float hi) {
+  return fminf(fmaxf(v, lo), hi);
+}
+
 // std::max / std::min semantics (comparison order matters for NaN).
 __host__ __device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }
 __host__ __device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }

@@ -48,6 +48,17 @@ void DeviceArray<T>::upload(const T* host, size_t n, cudaStream_t s) {
   if (n > 0) SGB_CUDA(cudaMemcpyAsync(ptr, host, n * sizeof(T), cudaMemcpyHostToDevice, s));
 }
 template <typename T>
+void DeviceArray<T>::allocate_padded(size_t n, size_t pad, cudaStream_t s) {
+  allocate(n + pad);
+  if (n + pad > 0) SGB_CUDA(cudaMemsetAsync(ptr, 0, (n + pad) * sizeof(T), s));
+  count = n;
+}
+template <typename T>
+void DeviceArray<T>::upload_padded(const T* host, size_t n, size_t pad, cudaStream_t s) {
+  allocate_padded(n, pad, s);
+  if (n > 0) SGB_CUDA(cudaMemcpyAsync(ptr, host, n * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+template <typename T>
 void DeviceArray<T>::release() {
   if (ptr != nullptr) cudaFree(ptr);
   ptr = nullptr;
@@ -55,6 +66,9 @@ void DeviceArray<T>::release() {
 }
 template struct DeviceArray<int>;
 template struct DeviceArray<int2>;
+template struct DeviceArray<Tile>;
+template struct DeviceArray<LongRow>;
+template struct DeviceArray<unsigned int>;
 template struct DeviceArray<double>;
 template struct DeviceArray<Ctl>;
 
@@ -67,24 +81,43 @@ double now_seconds() {
 
 bool finite_bound_host(double v) { return !(std::isinf(v) || std::fabs(v) >= 1e30); }
 
+}  // namespace
+
 // Greedy row tiles: consecutive rows while the tile has at most kTileThreads rows and at
-// most kTileCap nonzeros; a row longer than kTileCap is a tile of its own.
-std::vector<int2> build_tiles(const std::vector<int>& ptr, int lines) {
-  std::vector<int2> tiles;
+// most kCap nonzeros; a row longer than kCap becomes chunk tiles of kCap entries each,
+// listed as a LongRow so its chunk partials can be combined in chunk order.
+void build_tiles(const std::vector<int>& ptr, int lines, int lanes, std::vector<Tile>* tiles,
+                 std::vector<LongRow>* longs, int* nchunks) {
+  tiles->clear();
+  longs->clear();
+  *nchunks = 0;
+  const int max_rows = kTileThreads / lanes;
   int r = 0;
   while (r < lines) {
-    const int begin = r;
-    if (ptr[r + 1] - ptr[r] > kTileCap) {
-      tiles.push_back(make_int2(r, r + 1));
+    const int len = ptr[r + 1] - ptr[r];
+    if (len > kCap) {
+      LongRow lr{r, *nchunks, 0};
+      for (int k = ptr[r]; k < ptr[r + 1]; k += kCap) {
+        const int k1 = std::min(k + kCap, ptr[r + 1]);
+        tiles->push_back(Tile{r, -(*nchunks) - 1, k, k1});
+        ++*nchunks;
+        ++lr.nchunks;
+      }
+      longs->push_back(lr);
       ++r;
       continue;
     }
+    const int begin = r;
     ++r;
-    while (r < lines && r - begin < kTileThreads && ptr[r + 1] - ptr[begin] <= kTileCap) ++r;
-    tiles.push_back(make_int2(begin, r));
+    while (r < lines && r - begin < max_rows && ptr[r + 1] - ptr[r] <= kCap &&
+           ptr[r + 1] - ptr[begin] <= kCap) {
+      ++r;
+    }
+    tiles->push_back(Tile{begin, r, ptr[begin], ptr[r]});
   }
-  return tiles;
 }
+
+namespace {
 
 std::string format(const char* fmt, ...) __attribute__((format(printf, 1, 2)));
 std::string format(const char* fmt, ...) {
@@ -131,6 +164,7 @@ Engine::Engine(int device) : device_(device) {
   SGB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&snapshot_), 2 * sizeof(Ctl),
                          cudaHostAllocDefault));
   for (auto& ev : done_event_) SGB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  for (auto& ev : timing_) SGB_CUDA(cudaEventCreate(&ev));
   ctl_.allocate(1);
   SGB_CUDA(cudaMemset(ctl_.ptr, 0, sizeof(Ctl)));
 }
@@ -139,6 +173,9 @@ Engine::~Engine() {
   cudaSetDevice(device_);
   destroy_graphs();
   for (auto& ev : done_event_) {
+    if (ev != nullptr) cudaEventDestroy(ev);
+  }
+  for (auto& ev : timing_) {
     if (ev != nullptr) cudaEventDestroy(ev);
   }
   if (snapshot_ != nullptr) cudaFreeHost(snapshot_);
@@ -229,10 +266,16 @@ void Engine::load(const sankhya_gb300_lp& lp) {
       rval[slot] = lp.values[k];
     }
   }
-  const std::vector<int2> ctiles = build_tiles(cptr, n);
-  const std::vector<int2> rtiles = build_tiles(rptr, m);
+  std::vector<Tile> ctiles, rtiles;
+  std::vector<LongRow> clongs, rlongs;
+  lanes_csc_ = choose_lanes(n > 0 ? static_cast<double>(nnz) / n : 1.0);
+  lanes_csr_ = choose_lanes(m > 0 ? static_cast<double>(nnz) / m : 1.0);
+  build_tiles(cptr, n, lanes_csc_, &ctiles, &clongs, &nchunks_csc_);
+  build_tiles(rptr, m, lanes_csr_, &rtiles, &rlongs, &nchunks_csr_);
   ntiles_csc_ = static_cast<int>(ctiles.size());
   ntiles_csr_ = static_cast<int>(rtiles.size());
+  nlong_csc_ = static_cast<int>(clongs.size());
+  nlong_csr_ = static_cast<int>(rlongs.size());
   const int resident = tile_blocks_per_sm() * num_sms_;
   grid_csc_ = std::max(1, std::min(ntiles_csc_, resident));
   grid_csr_ = std::max(1, std::min(ntiles_csr_, resident));
@@ -256,16 +299,21 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   bound_norm_ = std::sqrt(bound_sq);
 
   cudaStream_t s = stream_;
+  const size_t z = static_cast<size_t>(nnz);
   csc_ptr_.upload(cptr.data(), cptr.size(), s);
-  csc_idx_.upload(lp.row_index, static_cast<size_t>(nnz), s);
-  csc_raw_.upload(lp.values, static_cast<size_t>(nnz), s);
   csr_ptr_.upload(rptr.data(), rptr.size(), s);
-  csr_idx_.upload(ridx.data(), ridx.size(), s);
-  csr_raw_.upload(rval.data(), rval.size(), s);
+  // Index and value arrays carry kPad zero entries: a tile copy widened to 16-byte
+  // boundaries may read up to 3 entries past the last nonzero.
+  csc_idx_.upload_padded(lp.row_index, z, kPad, s);
+  csc_raw_.upload_padded(lp.values, z, kPad, s);
+  csr_idx_.upload_padded(ridx.data(), z, kPad, s);
+  csr_raw_.upload_padded(rval.data(), z, kPad, s);
+  csc_s_.allocate_padded(z, kPad, s);
+  csr_s_.allocate_padded(z, kPad, s);
   csc_tiles_.upload(ctiles.data(), ctiles.size(), s);
   csr_tiles_.upload(rtiles.data(), rtiles.size(), s);
-  csc_s_.allocate(static_cast<size_t>(nnz));
-  csr_s_.allocate(static_cast<size_t>(nnz));
+  csc_longs_.upload(clongs.data(), clongs.size(), s);
+  csr_longs_.upload(rlongs.data(), rlongs.size(), s);
   cost_.upload(cost.data(), cost.size(), s);
   col_cost_.upload(lp.col_cost, static_cast<size_t>(n), s);
   l_.upload(lp.col_lower, static_cast<size_t>(n), s);
@@ -273,7 +321,7 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   rl_.upload(lp.row_lower, static_cast<size_t>(m), s);
   ru_.upload(lp.row_upper, static_cast<size_t>(m), s);
   for (DeviceArray<double>* a : {&cs_, &ls_, &us_, &dc_, &col_acc_, &x0_, &x1_, &x_sum_, &x_rst_,
-                                 &xu0_, &xu1_, &reduced_, &best_x_, &power_v_}) {
+                                 &xu0_, &xu1_, &reduced_, &best_x_, &power_v_, &xbar_, &dx_}) {
     a->allocate(static_cast<size_t>(n));
   }
   for (DeviceArray<double>* a : {&rls_, &rus_, &dr_, &row_acc_, &y0_, &y1_, &y_sum_, &y_rst_,
@@ -283,27 +331,42 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   const int pgrid = std::max(grid_csc_, grid_csr_) + num_sms_ * 8;
   part_primal_.allocate(static_cast<size_t>(grid_csc_));
   part_dual_.allocate(static_cast<size_t>(grid_csr_) * 2);
-  part_rows0_.allocate(static_cast<size_t>(grid_csr_) * 8);
-  part_cols_.allocate(static_cast<size_t>(grid_csc_) * 16);
-  part_rows1_.allocate(static_cast<size_t>(grid_csr_) * 8);
+  part_rows0_.allocate(static_cast<size_t>(grid_csr_) * kEvalRowSlots);
+  part_cols_.allocate(static_cast<size_t>(grid_csc_ + 1) * kEvalColSlots);
+  part_rows1_.allocate(static_cast<size_t>(grid_csr_) * kEvalRowSlots);
+  chunk_primal_.allocate(static_cast<size_t>(nchunks_csc_) + 1);
+  chunk_cols_.allocate(2 * static_cast<size_t>(nchunks_csc_) + 2);
+  chunk_dual_.allocate(2 * static_cast<size_t>(nchunks_csr_) + 2);
+  chunk_rows_.allocate(2 * static_cast<size_t>(nchunks_csr_) + 2);
+  chunk_spmv_.allocate(static_cast<size_t>(std::max(nchunks_csc_, nchunks_csr_)) + 1);
   scalars_.allocate(static_cast<size_t>(pgrid) * 2 + 16);
   power_norms_.allocate(64);
+  tickets_.allocate(4);
+  SGB_CUDA(cudaMemsetAsync(tickets_.ptr, 0, 4 * sizeof(unsigned int), s));
   SGB_CUDA(cudaStreamSynchronize(s));
   fill_buffers();
   loaded_ = true;
 }
 
 void Engine::fill_buffers() {
+  const TileSet<double> csc{csc_ptr_.ptr,   csc_idx_.ptr, csc_s_.ptr,   csc_tiles_.ptr,
+                            csc_longs_.ptr, ntiles_csc_,  nlong_csc_,   nchunks_csc_,
+                            n_,             lanes_csc_};
+  const TileSet<double> csr{csr_ptr_.ptr,   csr_idx_.ptr, csr_s_.ptr,   csr_tiles_.ptr,
+                            csr_longs_.ptr, ntiles_csr_,  nlong_csr_,   nchunks_csr_,
+                            m_,             lanes_csr_};
   StepBuffers& b = step_;
   b.ctl = ctl_.ptr;
-  b.csc = Matrix<double>{csc_ptr_.ptr, csc_idx_.ptr, csc_s_.ptr, csc_tiles_.ptr, ntiles_csc_, n_};
-  b.csr = Matrix<double>{csr_ptr_.ptr, csr_idx_.ptr, csr_s_.ptr, csr_tiles_.ptr, ntiles_csr_, m_};
+  b.csc = csc;
+  b.csr = csr;
   b.x[0] = x0_.ptr;
   b.x[1] = x1_.ptr;
   b.y[0] = y0_.ptr;
   b.y[1] = y1_.ptr;
   b.x_sum = x_sum_.ptr;
   b.y_sum = y_sum_.ptr;
+  b.xbar = xbar_.ptr;
+  b.dx = dx_.ptr;
   b.c = cs_.ptr;
   b.l = ls_.ptr;
   b.u = us_.ptr;
@@ -311,13 +374,17 @@ void Engine::fill_buffers() {
   b.ru = rus_.ptr;
   b.part_primal = part_primal_.ptr;
   b.part_dual = part_dual_.ptr;
+  b.chunk_primal = chunk_primal_.ptr;
+  b.chunk_dual = chunk_dual_.ptr;
   b.grid_primal = grid_csc_;
   b.grid_dual = grid_csr_;
 
   EvalBuffers& e = eval_;
   e.ctl = ctl_.ptr;
-  e.csc = Matrix<double>{csc_ptr_.ptr, csc_idx_.ptr, csc_raw_.ptr, csc_tiles_.ptr, ntiles_csc_, n_};
-  e.csr = Matrix<double>{csr_ptr_.ptr, csr_idx_.ptr, csr_raw_.ptr, csr_tiles_.ptr, ntiles_csr_, m_};
+  e.csc = csc;
+  e.csc.val = csc_raw_.ptr;
+  e.csr = csr;
+  e.csr.val = csr_raw_.ptr;
   e.x[0] = x0_.ptr;
   e.x[1] = x1_.ptr;
   e.y[0] = y0_.ptr;
@@ -344,6 +411,8 @@ void Engine::fill_buffers() {
   e.reduced = reduced_.ptr;
   e.best_x = best_x_.ptr;
   e.best_y = best_y_.ptr;
+  e.chunk_cols = chunk_cols_.ptr;
+  e.chunk_rows = chunk_rows_.ptr;
   e.part_rows0 = part_rows0_.ptr;
   e.part_cols = part_cols_.ptr;
   e.part_rows1 = part_rows1_.ptr;
@@ -388,11 +457,13 @@ double Engine::power_iteration(long long seed) {
   const int grid = std::min(num_sms_ * 4, std::max(1, (n_ + 255) / 256));
   double* norms = power_norms_.ptr;  // [2*step] = length^2, [2*step+1] = next
   for (int step = 0; step < iterations; ++step) {
-    launch_sumsq(power_v_.ptr, n_, scalars_.ptr, norms + 2 * step, s, grid);
+    launch_sumsq(power_v_.ptr, n_, scalars_.ptr, norms + 2 * step, tickets_.ptr, s, grid);
     launch_scale_div(power_v_.ptr, n_, norms + 2 * step, s);
-    launch_spmv(step_.csr, power_v_.ptr, power_av_.ptr, s, grid_csr_);
-    launch_spmv(step_.csc, power_av_.ptr, power_v_.ptr, s, grid_csc_);
-    launch_sumsq(power_v_.ptr, n_, scalars_.ptr, norms + 2 * step + 1, s, grid);
+    launch_spmv(step_.csr, power_v_.ptr, power_av_.ptr, chunk_spmv_.ptr, tickets_.ptr + 1, s,
+                grid_csr_);
+    launch_spmv(step_.csc, power_av_.ptr, power_v_.ptr, chunk_spmv_.ptr, tickets_.ptr + 1, s,
+                grid_csc_);
+    launch_sumsq(power_v_.ptr, n_, scalars_.ptr, norms + 2 * step + 1, tickets_.ptr, s, grid);
   }
   SGB_CUDA(cudaGetLastError());
   std::vector<double> host(2 * iterations);
@@ -436,9 +507,10 @@ void Engine::spmv(int op, int scaled, const double* in, double* out) {
   DeviceArray<double> din, dout;
   din.upload(in, static_cast<size_t>(in_len), s);
   dout.allocate(static_cast<size_t>(out_len));
-  Matrix<double> a = op == 0 ? step_.csr : step_.csc;
+  TileSet<double> a = op == 0 ? step_.csr : step_.csc;
   if (!scaled) a.val = op == 0 ? csr_raw_.ptr : csc_raw_.ptr;
-  launch_spmv(a, din.ptr, dout.ptr, s, op == 0 ? grid_csr_ : grid_csc_);
+  launch_spmv(a, din.ptr, dout.ptr, chunk_spmv_.ptr, tickets_.ptr + 1, s,
+              op == 0 ? grid_csr_ : grid_csc_);
   SGB_CUDA(cudaGetLastError());
   if (out_len > 0) {
     SGB_CUDA(cudaMemcpyAsync(out, dout.ptr, out_len * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -470,7 +542,7 @@ void Engine::build_graphs(int steps) {
     SGB_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < steps; ++k) {
       launch_pdhg_step(step_, stream_);
-      launch_evaluation(eval_, step_, stream_);
+      launch_evaluation(eval_, stream_);
     }
     cudaMemcpyAsync(snapshot_ + slot, ctl_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_);
     const cudaError_t end = cudaStreamEndCapture(stream_, &graph);
@@ -488,6 +560,7 @@ void Engine::run_loop(const sankhya_gb300_params& p, double t0, int* stop_status
   const bool has_time_limit = p.time_limit < 1e300;
   long long logged = 0;
   auto launch = [&](int slot) {
+    ++graphs_launched_;
     SGB_CUDA(cudaGraphLaunch(graph_exec_[slot], stream_));
     SGB_CUDA(cudaEventRecord(done_event_[slot], stream_));
   };
@@ -532,7 +605,7 @@ void Engine::final_evaluation() {
   const int one = 1;
   SGB_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(ctl_.ptr) + offsetof(Ctl, final_mode), &one,
                            sizeof(int), cudaMemcpyHostToDevice, stream_));
-  launch_evaluation(eval_, step_, stream_);
+  launch_evaluation(eval_, stream_);
   SGB_CUDA(cudaGetLastError());
 }
 
@@ -545,6 +618,9 @@ void Engine::solve(const sankhya_gb300_params& p, sankhya_gb300_result* r) {
   }
   SGB_CUDA(cudaSetDevice(device_));
   cudaStream_t s = stream_;
+  SGB_CUDA(cudaEventRecord(timing_[0], s));
+  const long long launches_before = kernel_launch_count();
+  graphs_launched_ = 0;
 
   precondition(p.random_seed);
   const double norm = power_iteration(p.random_seed);
@@ -552,7 +628,7 @@ void Engine::solve(const sankhya_gb300_params& p, sankhya_gb300_result* r) {
     // Scaled entry magnitudes, for the log line of src/pdhg/pdhg.cpp:132-133.
     const int grid = std::min(num_sms_ * 4, std::max(1, static_cast<int>((nnz_ + 255) / 256)));
     launch_abs_minmax(csc_s_.ptr, static_cast<int>(nnz_), scalars_.ptr, scalars_.ptr + 2 * grid + 2,
-                      s, grid);
+                      tickets_.ptr, s, grid);
     double mm[2] = {0.0, 0.0};
     SGB_CUDA(cudaMemcpyAsync(mm, scalars_.ptr + 2 * grid + 2, 2 * sizeof(double),
                              cudaMemcpyDeviceToHost, s));
@@ -574,6 +650,7 @@ void Engine::solve(const sankhya_gb300_params& p, sankhya_gb300_result* r) {
   c.iteration_limit = p.iteration_limit < 0 ? 1000000 : p.iteration_limit;
   c.use_restarts = p.restart != 0;
   c.stop_at_request = p.stop_at_request != 0;
+  c.stop_rule = p.stop_rule == SANKHYA_GB300_STOP_RELATIVE ? 1 : 0;
   c.best.primal = c.best.dual = c.best.gap = std::numeric_limits<double>::infinity();
   SGB_CUDA(cudaMemcpyAsync(ctl_.ptr, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
   SGB_CUDA(cudaStreamSynchronize(s));
@@ -581,12 +658,28 @@ void Engine::solve(const sankhya_gb300_params& p, sankhya_gb300_result* r) {
   r->setup_seconds = t_loop - t0;
 
   int stop_status = SANKHYA_GB300_ITERATION_LIMIT;
+  const long long launches_setup = kernel_launch_count() - launches_before;
+  {
+    // Capturing a graph issues no launch; keep the capture out of the count.
+    const int steps = p.steps_per_poll > 0 ? p.steps_per_poll : 32;
+    const long long before_capture = kernel_launch_count();
+    build_graphs(steps);
+    (void)before_capture;
+  }
+  const long long count_after_capture = kernel_launch_count();
   run_loop(p, t0, &stop_status);
   const double t_end_loop = now_seconds();
   final_evaluation();
+  SGB_CUDA(cudaEventRecord(timing_[1], s));
   SGB_CUDA(cudaMemcpyAsync(&c, ctl_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
   SGB_CUDA(cudaStreamSynchronize(s));
   r->loop_seconds = t_end_loop - t_loop;
+  float device_ms = 0.0f;
+  SGB_CUDA(cudaEventElapsedTime(&device_ms, timing_[0], timing_[1]));
+  r->device_seconds = 1e-3 * device_ms;
+  launches_ = launches_setup + (kernel_launch_count() - count_after_capture) +
+              graphs_launched_ * static_cast<long long>(graph_steps_) * kKernelsPerStep;
+  r->kernel_launches = launches_;
 
   const Residuals& f = c.final_residuals;
   r->final_residuals = sankhya_gb300_residuals{f.primal,          f.dual,           f.gap,
@@ -636,6 +729,45 @@ void Engine::solve(const sankhya_gb300_params& p, sankhya_gb300_result* r) {
   std::snprintf(r->message, sizeof(r->message), "%s", message.c_str());
   solved_ = true;
   r->solve_seconds = now_seconds() - t0;
+}
+
+void Engine::time_kernels(int reps, double* ms) {
+  require_loaded();
+  if (!solved_) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no solve has run"};
+  SGB_CUDA(cudaSetDevice(device_));
+  cudaStream_t s = stream_;
+  Ctl saved;
+  SGB_CUDA(cudaMemcpyAsync(&saved, ctl_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaStreamSynchronize(s));
+  Ctl run = saved;
+  run.done = kRunning;
+  run.final_mode = 0;
+  run.iteration_limit = std::numeric_limits<long long>::max();
+  SGB_CUDA(cudaMemcpyAsync(ctl_.ptr, &run, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+  std::vector<cudaEvent_t> ev(3 * static_cast<size_t>(reps));
+  for (auto& e : ev) SGB_CUDA(cudaEventCreate(&e));
+  for (int r = 0; r < reps; ++r) {
+    SGB_CUDA(cudaEventRecord(ev[3 * r], s));
+    launch_primal_pass(step_, s);
+    SGB_CUDA(cudaEventRecord(ev[3 * r + 1], s));
+    launch_dual_pass(step_, s);
+    SGB_CUDA(cudaEventRecord(ev[3 * r + 2], s));
+  }
+  SGB_CUDA(cudaGetLastError());
+  SGB_CUDA(cudaStreamSynchronize(s));
+  double primal = 0.0, dual = 0.0;
+  for (int r = 0; r < reps; ++r) {
+    float a = 0.0f, b = 0.0f;
+    SGB_CUDA(cudaEventElapsedTime(&a, ev[3 * r], ev[3 * r + 1]));
+    SGB_CUDA(cudaEventElapsedTime(&b, ev[3 * r + 1], ev[3 * r + 2]));
+    primal += a;
+    dual += b;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  SGB_CUDA(cudaMemcpyAsync(ctl_.ptr, &saved, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+  SGB_CUDA(cudaStreamSynchronize(s));
+  ms[0] = primal / reps;
+  ms[1] = dual / reps;
 }
 
 void Engine::solution(double* col_value, double* col_dual, double* row_dual) {

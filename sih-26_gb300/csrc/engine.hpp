@@ -31,6 +31,9 @@ struct DeviceArray {
   ~DeviceArray() { release(); }
   void allocate(size_t n);
   void upload(const T* host, size_t n, cudaStream_t s);
+  // n entries followed by `pad` zeroed ones (count stays n).
+  void allocate_padded(size_t n, size_t pad, cudaStream_t s);
+  void upload_padded(const T* host, size_t n, size_t pad, cudaStream_t s);
   void release();
 };
 
@@ -45,6 +48,7 @@ class Engine {
   void scaling(long long seed, double* row_scale, double* col_scale, double* scaled_values,
                double* spectral_norm);
   void spmv(int op, int scaled, const double* in, double* out);
+  void time_kernels(int reps, double* ms);
 
   int device() const { return device_; }
 
@@ -72,11 +76,15 @@ class Engine {
   double sense_ = 1.0, offset_ = 0.0;
   double bound_norm_ = 0.0, cost_norm_ = 0.0;
   int ntiles_csr_ = 0, ntiles_csc_ = 0;
+  int nlong_csr_ = 0, nlong_csc_ = 0;
+  int nchunks_csr_ = 0, nchunks_csc_ = 0;
+  int lanes_csr_ = 1, lanes_csc_ = 1;
   int grid_csr_ = 1, grid_csc_ = 1;
 
   // Pattern (shared by scaled and unscaled values).
   DeviceArray<int> csc_ptr_, csc_idx_, csr_ptr_, csr_idx_;
-  DeviceArray<int2> csc_tiles_, csr_tiles_;
+  DeviceArray<Tile> csc_tiles_, csr_tiles_;
+  DeviceArray<LongRow> csc_longs_, csr_longs_;
   // Values: unscaled (evaluation) and scaled (iterations), both layouts.
   DeviceArray<double> csc_raw_, csr_raw_, csc_s_, csr_s_;
   // Unscaled vectors.
@@ -85,21 +93,30 @@ class Engine {
   DeviceArray<double> cs_, ls_, us_, rls_, rus_, dr_, dc_, row_acc_, col_acc_;
   // Iterates.
   DeviceArray<double> x0_, x1_, y0_, y1_, x_sum_, y_sum_, x_rst_, y_rst_;
-  DeviceArray<double> xu0_, xu1_, yu0_, yu1_, reduced_, best_x_, best_y_;
+  DeviceArray<double> xu0_, xu1_, yu0_, yu1_, reduced_, best_x_, best_y_, xbar_, dx_;
   // Reductions.
   DeviceArray<double> part_primal_, part_dual_, part_rows0_, part_cols_, part_rows1_;
+  DeviceArray<double> chunk_primal_, chunk_dual_, chunk_cols_, chunk_rows_, chunk_spmv_;
   DeviceArray<double> scalars_, power_v_, power_av_, power_norms_;
+  DeviceArray<unsigned int> tickets_;  // setup-kernel last-block counters
   DeviceArray<Ctl> ctl_;
 
   Ctl* snapshot_ = nullptr;  // pinned host, two slots
   cudaGraphExec_t graph_exec_[2] = {nullptr, nullptr};
   int graph_steps_ = 0;
   cudaEvent_t done_event_[2] = {nullptr, nullptr};
+  cudaEvent_t timing_[2] = {nullptr, nullptr};
+  long long launches_ = 0;  // engine kernels launched by the current solve
+  long long graphs_launched_ = 0;
 
   StepBuffers step_{};
   EvalBuffers eval_{};
 };
 
 size_t estimate_memory(long long rows, long long cols, long long nnz, int precision);
+
+// Row tiles of a CSR / CSC pattern (see tiles.cuh).
+void build_tiles(const std::vector<int>& ptr, int lines, int lanes, std::vector<Tile>* tiles,
+                 std::vector<LongRow>* longs, int* nchunks);
 
 }  // namespace sgb

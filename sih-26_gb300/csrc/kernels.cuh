@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "tiles.cuh"
+
 namespace sgb {
 
 // Mirrors sankhya::pdhg::Residuals (src/pdhg/pdhg_evaluate.hpp:19-70).
@@ -37,7 +39,7 @@ __host__ __device__ inline bool meets_project_standard(const Residuals& r) {
          r.complementarity <= 1e-6;
 }
 
-enum DoneCode : int { kRunning = 0, kConverged = 1, kIterationLimit = 2 };
+enum DoneCode : int { kRunning = 0, kConverged = 1, kIterationLimit = 2, kFault = 3 };
 
 constexpr int kLogRing = 64;
 
@@ -47,6 +49,10 @@ struct EvalRecord {
   double primal_objective;  // minimise space, unscaled
   double primal, dual, gap;
 };
+
+// Ticket slots (last-block counters), one per reducing kernel.
+enum Ticket : int { kTicketDual = 0, kTicketEvalRows = 1, kTicketPrimal = 2, kTicketEvalCols = 3,
+                    kTicketCount = 4 };
 
 struct Ctl {
   // Step size and primal weight, src/pdhg/pdhg.cpp:181-186.
@@ -61,94 +67,100 @@ struct Ctl {
   int copy_best;    // 0: nothing; 1: the current candidate; 2: the average candidate
   int do_restart;
   int final_mode;   // the evaluation kernels evaluate (best_x, best_y) only
+  int stop_rule;    // 0: the reference's stopping test; 1: relative KKT only
+  int error;        // a bounded wait gave up (nonzero: the host stops with an error)
   int pad0;
   double movement, interaction;  // of the last attempted step
+  double mv_primal;              // primal half of the movement, from k_primal's last block
   Residuals best;
   Residuals final_residuals;
   double model_objective;  // sum of the original-sense costs times best_x (final mode)
   long long log_count;
   EvalRecord log[kLogRing];
-  unsigned int ticket[4];  // last-block counters of the reducing kernels
+  unsigned int ticket[kTicketCount];
 };
 
-// Device arrays of one loaded LP. Index arrays are shared by the scaled and unscaled value
-// arrays: scaling never changes the pattern (src/la/scaling.cpp:29-31).
-template <typename V>
-struct Matrix {
-  const int* ptr;      // rows + 1 (CSR) or cols + 1 (CSC)
-  const int* idx;      // nnz
-  const V* val;        // nnz
-  const int2* tiles;   // row (or column) tiles: [begin, end)
-  int ntiles;
-  int nrows;           // rows of this layout (m for CSR, n for CSC)
-};
+constexpr int kEvalColSlots = 16;  // doubles per block in the column-evaluation partials
+constexpr int kEvalRowSlots = 8;
 
-// Tile capacity: the products of one tile are staged in shared memory.
-constexpr int kTileThreads = 256;
-constexpr int kTileCap = 2048;
-
-// ---- Launchers (pdhg_kernels.cu) ---------------------------------------------------------
 struct StepBuffers {
   Ctl* ctl;
-  Matrix<double> csc, csr;      // scaled
+  TileSet<double> csc, csr;  // scaled
   double* x[2];
   double* y[2];
   double* x_sum;
   double* y_sum;
+  double* xbar;  // 2 x' - x of the step, written by k_primal, gathered by k_dual
+  double* dx;    // x' - x
   const double *c, *l, *u, *rl, *ru;  // scaled problem
-  double* part_primal;  // [grid]
-  double* part_dual;    // [grid * 2]
+  double* part_primal;   // [grid_primal]
+  double* part_dual;     // [grid_dual * 2]
+  double* chunk_primal;  // [csc.nchunks]
+  double* chunk_dual;    // [csr.nchunks * 2]
   int grid_primal, grid_dual;
 };
 
 struct EvalBuffers {
   Ctl* ctl;
-  Matrix<double> csc, csr;      // UNSCALED values
+  TileSet<double> csc, csr;  // UNSCALED values
   const double* x[2];
   const double* y[2];
-  const double* x_sum;
-  const double* y_sum;
-  const double *x_rst, *y_rst;
-  const double *dr, *dc;        // row / column scale (Dr, Dc)
-  const double *cost;           // minimise-space unscaled cost
-  const double *col_cost;       // original-sense cost (for the model objective)
+  double* x_sum;
+  double* y_sum;
+  double *x_rst, *y_rst;
+  const double *dr, *dc;          // row / column scale (Dr, Dc)
+  const double* cost;             // minimise-space unscaled cost
+  const double* col_cost;         // original-sense cost (for the model objective)
   const double *l, *u, *rl, *ru;  // unscaled bounds
   double bound_norm, cost_norm, sense;
-  double *xu[2], *yu[2];        // unscaled candidates (current, average)
-  double* reduced;              // reduced cost of candidate 0
+  double *xu[2], *yu[2];  // unscaled candidates (current, average)
+  double* reduced;        // reduced cost of candidate 0
   double* best_x;
   double* best_y;
-  double* part_rows0;  // [grid_rows * 8]
-  double* part_cols;   // [grid_cols * 16]
-  double* part_rows1;  // [grid_rows * 8]
+  double* part_rows0;  // [grid_rows * kEvalRowSlots]
+  double* part_cols;   // [(grid_cols + 1) * kEvalColSlots]; the last slot holds long columns
+  double* part_rows1;  // [grid_rows * kEvalRowSlots]
+  double* chunk_cols;  // [csc.nchunks * 2]
+  double* chunk_rows;  // [csr.nchunks * 2]
   int grid_rows, grid_cols;
   int m, n;
 };
 
-// One attempted PDHG step: primal column pass then dual row pass with the step decision.
+// ---- Launchers (pdhg_kernels.cu) ---------------------------------------------------------
 void launch_pdhg_step(const StepBuffers& b, cudaStream_t s);
+void launch_primal_pass(const StepBuffers& b, cudaStream_t s);
+void launch_dual_pass(const StepBuffers& b, cudaStream_t s);
+// Kernels launched per attempted step inside a graph (2 step + 4 evaluation kernels).
+constexpr int kKernelsPerStep = 6;
+// Running count of kernel launches issued by the launchers of this file (host side).
+long long kernel_launch_count();
 // The evaluation tick (no-op on the device unless ctl->eval_now or ctl->final_mode).
-void launch_evaluation(const EvalBuffers& e, const StepBuffers& b, cudaStream_t s);
+void launch_evaluation(const EvalBuffers& e, cudaStream_t s);
 
 // Setup kernels.
-void launch_scaling_round(int m, int n, Matrix<double> csr, Matrix<double> csc, double* csr_val,
+void launch_scaling_round(int m, int n, TileSet<double> csr, TileSet<double> csc, double* csr_val,
                           double* csc_val, double* row_acc, double* col_acc, double* dr,
                           double* dc, int sum_mode, cudaStream_t s);
 void launch_scale_vectors(int m, int n, const double* cost, const double* l, const double* u,
                           const double* rl, const double* ru, const double* dr, const double* dc,
                           double* cs, double* ls, double* us, double* rls, double* rus,
                           cudaStream_t s);
-// y = A x with the tile kernel (CSR gives A x; CSC gives A^T x).
-void launch_spmv(Matrix<double> a, const double* x, double* y, cudaStream_t s, int grid);
+// y = A x with the tile kernel (CSR gives A x; CSC gives A^T x). chunk holds a.nchunks
+// doubles; ticket is one device counter that is zero on entry and on exit.
+void launch_spmv(TileSet<double> a, const double* x, double* y, double* chunk,
+                 unsigned int* ticket, cudaStream_t s, int grid);
 // out[0] = sum v^2, deterministic; part holds grid doubles.
-void launch_sumsq(const double* v, int count, double* part, double* out, cudaStream_t s,
-                  int grid);
+void launch_sumsq(const double* v, int count, double* part, double* out, unsigned int* ticket,
+                  cudaStream_t s, int grid);
 void launch_scale_div(double* v, int count, const double* by_sqrt_of, cudaStream_t s);
-void launch_abs_minmax(const double* v, int count, double* part, double* out, cudaStream_t s,
-                       int grid);
+void launch_abs_minmax(const double* v, int count, double* part, double* out,
+                       unsigned int* ticket, cudaStream_t s, int grid);
 void launch_project_start(int n, const double* l, const double* u, double* x, cudaStream_t s);
 void launch_fill(double* v, int count, double value, cudaStream_t s);
 
+// Resident tile blocks per SM of the step kernels (occupancy query).
 int tile_blocks_per_sm();
+// Sets the dynamic shared-memory limit of the tile kernels once per process.
+void configure_tile_kernels();
 
 }  // namespace sgb

@@ -1,27 +1,25 @@
-// pdhg_kernels.cu -- the hot path of the GB300 PDHG engine.
+// pdhg_kernels.cu -- the FP64 hot path of the GB300 PDHG engine.
 //
 // Per attempted step (src/pdhg/pdhg.cpp:220-335) there are TWO kernels:
 //   k_primal  one pass over the CSC copy of Ahat: A^T y gathered per column, fused with the
-//             projected primal update x' = proj(x - tau (c + A^T y)) and the primal half of
-//             the movement; it also folds the previous accepted iterate into x_sum.
-//   k_dual    one pass over the CSR copy: A xbar and A dx from ONE read of each row (x' and x
-//             gathered, xbar = 2x' - x, dx = x' - x), fused with the Moreau dual update, the
-//             dual movement and the interaction dy^T A dx; its last block sums every block's
-//             partials in a fixed order and takes the step-size decision on the device.
+//             projected primal update x' = proj(x - tau (c + A^T y)), xbar = 2x' - x and
+//             dx = x' - x (written once per column so the row pass needs one FMA per entry
+//             and product), the primal half of the movement, and the deferred x_sum update.
+//   k_dual    one pass over the CSR copy: A xbar and A dx from ONE read of each row, fused
+//             with the Moreau dual update, the dual movement and the interaction dy^T A dx;
+//             its last block sums every block's partials in a fixed order and takes the
+//             step-size decision on the device.
 // The evaluation tick (src/pdhg/pdhg.cpp:341-483, src/pdhg/pdhg_evaluate.cpp) is three
 // fused passes over the UNSCALED values plus one vector pass; it runs only when the step
 // decision asks for it and otherwise returns at once.
 //
-// Sparse products use row TILES: a tile is a run of consecutive rows whose nonzeros fit in
-// shared memory. The block loads the tile's indices and values with coalesced accesses,
-// gathers the vector entries and stages the products in shared memory; thread r then sums
-// row r of the tile sequentially in ascending index order -- the order the reference's own
-// SparseMatrix::multiply / transpose_multiply accumulate in (src/la/sparse.cpp:232-259), so
-// the products of A x and A^T y match the reference's bits. A row with more nonzeros than a
-// tile holds is summed by the whole block. Every sum of a scalar over rows or columns uses
-// a fixed grid and a fixed reduction tree, so runs are bit-reproducible.
+// GB300 executes FP64 at about 1/64 of its FP32 rate, so this method is bound by the FP64
+// pipe rather than by HBM: the kernels are written to spend as few FP64 instructions per
+// entry as the method allows (one FMA per entry and product), to divide only where a row
+// is not an equality, and to keep every reduction deterministic.
 #include "common.cuh"
 #include "kernels.cuh"
+#include "tiles.cuh"
 
 #include <cstdio>
 
@@ -29,90 +27,15 @@ namespace sgb {
 
 namespace {
 
-constexpr int kUnroll = kTileCap / kTileThreads;
+long long g_launches = 0;
+int g_tile_blocks_per_sm = 0;
+int g_num_sms = 0;
 
-__device__ __forceinline__ double ldcg(const double* p) { return __ldcg(p); }
+constexpr int kScratch = 16 * (kTileThreads / 32);
 
-// Visit every tile of `mat` assigned to this block. prod(k, index, value, p[NP]) fills the
-// NP products of nonzero k; epi(row, s[NP]) consumes a row's sums on one thread.
-template <int NP, typename Prod, typename Epi>
-__device__ __forceinline__ void tile_loop(const Matrix<double>& mat, double* smem, Prod prod,
-                                          Epi epi) {
-  for (int t = blockIdx.x; t < mat.ntiles; t += gridDim.x) {
-    const int2 tile = mat.tiles[t];
-    const int k0 = mat.ptr[tile.x];
-    const int k1 = mat.ptr[tile.y];
-    if (k1 - k0 > kTileCap) {
-      // One long row: strided over the whole block, then a block reduction.
-      double acc[NP];
-#pragma unroll
-      for (int q = 0; q < NP; ++q) acc[q] = 0.0;
-      for (int k = k0 + threadIdx.x; k < k1; k += blockDim.x) {
-        double p[NP];
-        prod(k, mat.idx[k], mat.val[k], p);
-#pragma unroll
-        for (int q = 0; q < NP; ++q) acc[q] += p[q];
-      }
-      double out[NP];
-      block_sum<NP>(acc, smem, out);
-      if (threadIdx.x == 0) epi(tile.x, out);
-      __syncthreads();
-      continue;
-    }
-    int ci[kUnroll];
-    double vv[kUnroll];
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-      const int k = k0 + threadIdx.x + u * kTileThreads;
-      if (k < k1) {
-        ci[u] = __ldcs(mat.idx + k);
-        vv[u] = __ldcs(mat.val + k);
-      }
-    }
-#pragma unroll
-    for (int u = 0; u < kUnroll; ++u) {
-      const int k = k0 + threadIdx.x + u * kTileThreads;
-      if (k < k1) {
-        double p[NP];
-        prod(k, ci[u], vv[u], p);
-#pragma unroll
-        for (int q = 0; q < NP; ++q) smem[q * kTileCap + (k - k0)] = p[q];
-      }
-    }
-    __syncthreads();
-    const int r = tile.x + threadIdx.x;
-    if (r < tile.y) {
-      const int a = mat.ptr[r] - k0, b = mat.ptr[r + 1] - k0;
-      double s[NP];
-#pragma unroll
-      for (int q = 0; q < NP; ++q) s[q] = 0.0;
-      for (int k = a; k < b; ++k) {
-#pragma unroll
-        for (int q = 0; q < NP; ++q) s[q] += smem[q * kTileCap + k];
-      }
-      epi(r, s);
-    }
-    __syncthreads();
-  }
-}
-
-// Block-level partial write plus "am I the last block" ticket (threadfence reduction).
-template <int NV>
-__device__ __forceinline__ bool publish_partials(double (&v)[NV], double* scratch, double* part,
-                                                 unsigned int* ticket) {
-  double out[NV];
-  block_sum<NV>(v, scratch, out);
-  __shared__ bool is_last;
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int q = 0; q < NV; ++q) part[blockIdx.x * NV + q] = out[q];
-    __threadfence();
-    const unsigned int t = atomicAdd(ticket, 1u);
-    is_last = (t == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (is_last) __threadfence();
-  return is_last;
+__device__ __forceinline__ void raise_error(Ctl* c) {
+  c->error = 1;
+  c->done = kFault;
 }
 
 // ---- Step decision, src/pdhg/pdhg.cpp:252-335 (one thread) --------------------------------
@@ -149,7 +72,8 @@ __device__ void step_decision(Ctl* c, double movement, double interaction) {
 
 // ---- k_primal ----------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTileThreads) k_primal(StepBuffers b) {
-  __shared__ double smem[kTileCap];
+  extern __shared__ __align__(16) unsigned char dsmem[];
+  __shared__ double scratch[kScratch];
   Ctl* ctl = b.ctl;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     // The evaluation flags of the previous step are consumed; no kernel of this step reads
@@ -170,67 +94,90 @@ __global__ void __launch_bounds__(kTileThreads) k_primal(StepBuffers b) {
   const double omega = ctl->omega;
   const double tau = ctl->eta / omega;
   const bool add = ctl->pending_add != 0;
-  double mv[1] = {0.0};
-  tile_loop<1>(
-      b.csc, smem, [&](int, int row, double v, double* p) { p[0] = v * __ldg(y + row); },
-      [&](int j, const double* s) {
-        const double xj = x[j];
-        if (add) b.x_sum[j] += xj;
-        const double gradient = b.c[j] + s[0];
-        const double xnj = project(xj - tau * gradient, b.l[j], b.u[j]);
-        xn[j] = xnj;
-        const double d = xnj - xj;
-        mv[0] += 0.5 * omega * d * d;
-      });
-  double out[1];
-  block_sum<1>(mv, smem, out);
-  if (threadIdx.x == 0) b.part_primal[blockIdx.x] = out[0];
+  double mv[1] = {0.0};  // sum of dx^2
+  auto gather = [&](int row, double v, double* acc) { acc[0] = fma(v, __ldg(y + row), acc[0]); };
+  auto epi = [&](int j, const double* s) {
+    const double xj = x[j];
+    if (add) b.x_sum[j] += xj;
+    const double gradient = b.c[j] + s[0];
+    // Unfused, as src/pdhg/pdhg.cpp:232-233 rounds it.
+    const double xnj = clamp_box(__dsub_rn(xj, __dmul_rn(tau, gradient)), b.l[j], b.u[j]);
+    xn[j] = xnj;
+    const double d = xnj - xj;
+    b.dx[j] = d;
+    b.xbar[j] = fma(2.0, xnj, -xj);  // 2 x' is exact: one rounding, as 2.0 * x' - x
+    mv[0] = fma(d, d, mv[0]);
+  };
+  TilePipe<double> pipe;
+  pipe.setup(dsmem);
+  if (!run_tiles<1, double>(pipe, b.csc, b.chunk_primal, scratch, gather, epi) &&
+      threadIdx.x == 0) {
+    raise_error(ctl);
+  }
+  if (!arrive_last<1>(mv, scratch, b.part_primal, &ctl->ticket[kTicketPrimal])) return;
+  mv[0] = 0.0;
+  run_long_rows<1>(b.csc, b.chunk_primal, epi);
+  double longs[1], total[1];
+  block_sum<1>(mv, scratch, longs);
+  sum_partials<1>(b.part_primal, gridDim.x, scratch, total);
+  if (threadIdx.x == 0) {
+    ctl->mv_primal = 0.5 * omega * (total[0] + longs[0]);
+    ctl->ticket[kTicketPrimal] = 0;
+  }
 }
 
 // ---- k_dual ------------------------------------------------------------------------------
 __global__ void __launch_bounds__(kTileThreads) k_dual(StepBuffers b) {
-  __shared__ double smem[2 * kTileCap];
+  extern __shared__ __align__(16) unsigned char dsmem[];
+  __shared__ double scratch[kScratch];
   Ctl* ctl = b.ctl;
   if (ctl->done != kRunning) return;
   const int cur = ctl->cur;
-  const double* __restrict__ x = b.x[cur];
-  const double* __restrict__ xn = b.x[cur ^ 1];
   const double* __restrict__ y = b.y[cur];
   double* __restrict__ yn = b.y[cur ^ 1];
+  const double* __restrict__ xbar = b.xbar;
+  const double* __restrict__ dx = b.dx;
   const double omega = ctl->omega;
   const double sigma = ctl->eta * omega;
   const bool add = ctl->pending_add != 0;
-  double acc[2] = {0.0, 0.0};  // dual movement, interaction
-  tile_loop<2>(
-      b.csr, smem,
-      [&](int, int col, double v, double* p) {
-        const double xo = __ldg(x + col), xnew = __ldg(xn + col);
-        p[0] = v * (2.0 * xnew - xo);
-        p[1] = v * (xnew - xo);
-      },
-      [&](int i, const double* s) {
-        const double yi = y[i];
-        if (add) b.y_sum[i] += yi;
-        const double v = yi + sigma * s[0];
-        const double yni = v - sigma * project(v / sigma, b.rl[i], b.ru[i]);
-        yn[i] = yni;
-        const double d = yni - yi;
-        acc[0] += 0.5 * d * d / omega;
-        acc[1] += d * s[1];
-      });
-  if (!publish_partials<2>(acc, smem, b.part_dual, &ctl->ticket[0])) return;
-  // Last block: fixed-order sums of every block's partials, then the step decision.
-  double a[3] = {0.0, 0.0, 0.0};
-  for (int q = threadIdx.x; q < b.grid_primal; q += blockDim.x) a[0] += ldcg(b.part_primal + q);
-  for (int q = threadIdx.x; q < b.grid_dual; q += blockDim.x) {
-    a[1] += ldcg(b.part_dual + 2 * q);
-    a[2] += ldcg(b.part_dual + 2 * q + 1);
+  double acc2[2] = {0.0, 0.0};  // sum dy^2, sum dy (A dx)
+  auto gather = [&](int col, double v, double* acc) {
+    acc[0] = fma(v, __ldg(xbar + col), acc[0]);
+    acc[1] = fma(v, __ldg(dx + col), acc[1]);
+  };
+  auto epi = [&](int i, const double* s) {
+    const double yi = y[i];
+    if (add) b.y_sum[i] += yi;
+    const double rl = b.rl[i], ru = b.ru[i];
+    // Unfused, as the reference rounds it (src/pdhg/pdhg.cpp:244-245): a fused
+    // v - sigma * (v / sigma) would leave the division's rounding error on a free row. On
+    // an equality row the projection is the bound whatever v is, so no division is needed.
+    const double v = __dadd_rn(yi, __dmul_rn(sigma, s[0]));
+    const double p = rl == ru ? rl : clamp_box(v / sigma, rl, ru);
+    const double yni = __dsub_rn(v, __dmul_rn(sigma, p));
+    yn[i] = yni;
+    const double d = yni - yi;
+    acc2[0] = fma(d, d, acc2[0]);
+    acc2[1] = fma(d, s[1], acc2[1]);
+  };
+  TilePipe<double> pipe;
+  pipe.setup(dsmem);
+  if (!run_tiles<2, double>(pipe, b.csr, b.chunk_dual, scratch, gather, epi) &&
+      threadIdx.x == 0) {
+    raise_error(ctl);
   }
-  double out[3];
-  block_sum<3>(a, smem, out);
+  if (!arrive_last<2>(acc2, scratch, b.part_dual, &ctl->ticket[kTicketDual])) return;
+  acc2[0] = acc2[1] = 0.0;
+  run_long_rows<2>(b.csr, b.chunk_dual, epi);
+  double longs[2], total[2];
+  block_sum<2>(acc2, scratch, longs);
+  sum_partials<2>(b.part_dual, gridDim.x, scratch, total);
   if (threadIdx.x == 0) {
-    ctl->ticket[0] = 0;
-    step_decision(ctl, out[0] + out[1], fabs(out[2]));
+    ctl->ticket[kTicketDual] = 0;
+    if (ctl->done == kRunning) {
+      const double movement = ctl->mv_primal + (0.5 * (total[0] + longs[0])) / omega;
+      step_decision(ctl, movement, fabs(total[1] + longs[1]));
+    }
   }
 }
 
@@ -242,7 +189,7 @@ __device__ __forceinline__ bool eval_active(const Ctl* c) {
 // E0: rows, no matrix. Unscaled y candidates, the row half of the dual objective and dual
 // violation (src/pdhg/pdhg_evaluate.cpp:80-98), and |y - y_restart|^2.
 __global__ void __launch_bounds__(kTileThreads) k_eval_rows0(EvalBuffers e) {
-  __shared__ double scratch[8 * (kTileThreads / 32)];
+  __shared__ double scratch[kScratch];
   const Ctl* c = e.ctl;
   if (!eval_active(c)) return;
   const bool fin = c->final_mode != 0;
@@ -281,7 +228,7 @@ __global__ void __launch_bounds__(kTileThreads) k_eval_rows0(EvalBuffers e) {
   double out[5];
   block_sum<5>(acc, scratch, out);
   if (threadIdx.x == 0) {
-    for (int q = 0; q < 5; ++q) e.part_rows0[blockIdx.x * 8 + q] = out[q];
+    for (int q = 0; q < 5; ++q) e.part_rows0[blockIdx.x * kEvalRowSlots + q] = out[q];
   }
 }
 
@@ -289,67 +236,91 @@ __global__ void __launch_bounds__(kTileThreads) k_eval_rows0(EvalBuffers e) {
 // column half of the dual violation / dual objective / complementarity, the primal objective
 // (src/pdhg/pdhg_evaluate.cpp:54-78,111-139) and |x - x_restart|^2.
 __global__ void __launch_bounds__(kTileThreads) k_eval_cols(EvalBuffers e) {
-  __shared__ double smem[2 * kTileCap];
-  const Ctl* c = e.ctl;
+  extern __shared__ __align__(16) unsigned char dsmem[];
+  __shared__ double scratch[kScratch];
+  Ctl* c = e.ctl;
   if (!eval_active(c)) return;
   const bool fin = c->final_mode != 0;
   const int cur = c->cur;
   const bool avg = !fin && c->averaged > 0;
   const bool pend = c->pending_add != 0;
   const double count = static_cast<double>(c->averaged);
-  const double* yu0 = e.yu[0];
-  const double* yu1 = e.yu[1];
+  const double* __restrict__ yu0 = e.yu[0];
+  const double* __restrict__ yu1 = e.yu[1];
   // sums: viol0, bc0, pobj0, viol1, bc1, pobj1, dx^2, model objective; maxes: comp0, comp1
   double acc[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
   double cmax[2] = {0.0, 0.0};
-  tile_loop<2>(
-      e.csc, smem,
-      [&](int, int row, double v, double* p) {
-        p[0] = v * yu0[row];
-        p[1] = avg ? v * yu1[row] : 0.0;
-      },
-      [&](int j, const double* s) {
-        const double cj = e.cost[j], lj = e.l[j], uj = e.u[j];
-        double xc[2];
-        const int nc = avg ? 2 : 1;
-        if (fin) {
-          xc[0] = e.best_x[j];
-          acc[7] += e.col_cost[j] * xc[0];
-        } else {
-          const double xj = e.x[cur][j];
-          xc[0] = xj * e.dc[j];
-          if (avg) {
-            const double sum = pend ? e.x_sum[j] + xj : e.x_sum[j];
-            xc[1] = (sum / count) * e.dc[j];
-          }
-          const double d = xj - e.x_rst[j];
-          acc[6] += d * d;
-        }
-        for (int q = 0; q < nc; ++q) {
-          const double d = cj + s[q];
-          if (q == 0) e.reduced[j] = d;
-          e.xu[q][j] = xc[q];
-          if (d > 0.0) {
-            if (finite_bound(lj)) acc[3 * q + 1] += d * lj; else acc[3 * q] += d * d;
-          } else if (d < 0.0) {
-            if (finite_bound(uj)) acc[3 * q + 1] += d * uj; else acc[3 * q] += d * d;
-          }
-          if (lj != uj) {
-            const double ls = finite_bound(lj) ? xc[q] - lj : HUGE_VAL;
-            const double us = finite_bound(uj) ? uj - xc[q] : HUGE_VAL;
-            cmax[q] = dmax(cmax[q], fabs(d) * dmin(ls, us));
-          }
-          acc[3 * q + 2] += cj * xc[q];
-        }
-      });
-  double out[8];
-  block_sum<8>(acc, smem, out);
-  double mout[2];
-  block_max<2>(cmax, smem, mout);
+  auto gather = [&](int row, double v, double* a) {
+    a[0] = fma(v, yu0[row], a[0]);
+    if (avg) a[1] = fma(v, yu1[row], a[1]);
+  };
+  auto epi = [&](int j, const double* s) {
+    const double cj = e.cost[j], lj = e.l[j], uj = e.u[j];
+    double xc[2];
+    const int nc = avg ? 2 : 1;
+    if (fin) {
+      xc[0] = e.best_x[j];
+      acc[7] += e.col_cost[j] * xc[0];
+    } else {
+      const double xj = e.x[cur][j];
+      xc[0] = xj * e.dc[j];
+      if (avg) {
+        const double sum = pend ? e.x_sum[j] + xj : e.x_sum[j];
+        xc[1] = (sum / count) * e.dc[j];
+      }
+      const double d = xj - e.x_rst[j];
+      acc[6] += d * d;
+    }
+    for (int q = 0; q < nc; ++q) {
+      const double d = cj + s[q];
+      if (q == 0) e.reduced[j] = d;
+      e.xu[q][j] = xc[q];
+      if (d > 0.0) {
+        if (finite_bound(lj)) acc[3 * q + 1] += d * lj; else acc[3 * q] += d * d;
+      } else if (d < 0.0) {
+        if (finite_bound(uj)) acc[3 * q + 1] += d * uj; else acc[3 * q] += d * d;
+      }
+      if (lj != uj) {
+        const double ls = finite_bound(lj) ? xc[q] - lj : HUGE_VAL;
+        const double us = finite_bound(uj) ? uj - xc[q] : HUGE_VAL;
+        cmax[q] = dmax(cmax[q], fabs(d) * dmin(ls, us));
+      }
+      acc[3 * q + 2] += cj * xc[q];
+    }
+  };
+  TilePipe<double> pipe;
+  pipe.setup(dsmem);
+  if (!run_tiles<2, double>(pipe, e.csc, e.chunk_cols, scratch, gather, epi) &&
+      threadIdx.x == 0) {
+    raise_error(c);
+  }
+  double out[8], mout[2];
+  block_sum<8>(acc, scratch, out);
+  block_max<2>(cmax, scratch, mout);
+  __shared__ int s_last;
   if (threadIdx.x == 0) {
-    for (int q = 0; q < 8; ++q) e.part_cols[blockIdx.x * 16 + q] = out[q];
-    e.part_cols[blockIdx.x * 16 + 8] = mout[0];
-    e.part_cols[blockIdx.x * 16 + 9] = mout[1];
+    double* p = e.part_cols + blockIdx.x * kEvalColSlots;
+    for (int q = 0; q < 8; ++q) p[q] = out[q];
+    p[8] = mout[0];
+    p[9] = mout[1];
+    __threadfence();
+    s_last = atomicAdd(&c->ticket[kTicketEvalCols], 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  // Last block: long columns into the extra slot e.part_cols[grid_cols].
+  for (int q = 0; q < 8; ++q) acc[q] = 0.0;
+  cmax[0] = cmax[1] = 0.0;
+  run_long_rows<2>(e.csc, e.chunk_cols, epi);
+  block_sum<8>(acc, scratch, out);
+  block_max<2>(cmax, scratch, mout);
+  if (threadIdx.x == 0) {
+    double* p = e.part_cols + e.grid_cols * kEvalColSlots;
+    for (int q = 0; q < 8; ++q) p[q] = out[q];
+    p[8] = mout[0];
+    p[9] = mout[1];
+    c->ticket[kTicketEvalCols] = 0;
   }
 }
 
@@ -373,89 +344,87 @@ __device__ Residuals assemble(double pviol, double cviol, double rviol, double b
 // row complementarity (src/pdhg/pdhg_evaluate.cpp:29-45,99-110). The last block assembles
 // the Residuals and takes the best / stop / restart decisions (src/pdhg/pdhg.cpp:349-483).
 __global__ void __launch_bounds__(kTileThreads) k_eval_rows1(EvalBuffers e) {
-  __shared__ double smem[2 * kTileCap];
+  extern __shared__ __align__(16) unsigned char dsmem[];
+  __shared__ double scratch[kScratch];
   Ctl* c = e.ctl;
   if (!eval_active(c)) return;
   const bool fin = c->final_mode != 0;
   const bool avg = !fin && c->averaged > 0;
-  const double* xu0 = e.xu[0];
-  const double* xu1 = e.xu[1];
+  const double* __restrict__ xu0 = e.xu[0];
+  const double* __restrict__ xu1 = e.xu[1];
   double acc[2] = {0.0, 0.0};
   double cmax[2] = {0.0, 0.0};
-  tile_loop<2>(
-      e.csr, smem,
-      [&](int, int col, double v, double* p) {
-        p[0] = v * xu0[col];
-        p[1] = avg ? v * xu1[col] : 0.0;
-      },
-      [&](int i, const double* s) {
-        const double rl = e.rl[i], ru = e.ru[i];
-        const int nc = avg ? 2 : 1;
-        for (int q = 0; q < nc; ++q) {
-          const double a = s[q];
-          double violation = 0.0;
-          if (finite_bound(rl)) violation = dmax(violation, rl - a);
-          if (finite_bound(ru)) violation = dmax(violation, a - ru);
-          acc[q] += violation * violation;
-          if (rl != ru) {
-            const double ls = finite_bound(rl) ? a - rl : HUGE_VAL;
-            const double us = finite_bound(ru) ? ru - a : HUGE_VAL;
-            cmax[q] = dmax(cmax[q], fabs(e.yu[q][i]) * dmin(ls, us));
-          }
-        }
-      });
-  double mout[2];
-  block_max<2>(cmax, smem, mout);
-  double packed[4] = {acc[0], acc[1], 0.0, 0.0};
-  __shared__ double mx[2];
-  if (threadIdx.x == 0) {
-    mx[0] = mout[0];
-    mx[1] = mout[1];
+  auto gather = [&](int col, double v, double* a) {
+    a[0] = fma(v, xu0[col], a[0]);
+    if (avg) a[1] = fma(v, xu1[col], a[1]);
+  };
+  auto epi = [&](int i, const double* s) {
+    const double rl = e.rl[i], ru = e.ru[i];
+    const int nc = avg ? 2 : 1;
+    for (int q = 0; q < nc; ++q) {
+      const double a = s[q];
+      double violation = 0.0;
+      if (finite_bound(rl)) violation = dmax(violation, rl - a);
+      if (finite_bound(ru)) violation = dmax(violation, a - ru);
+      acc[q] += violation * violation;
+      if (rl != ru) {
+        const double ls = finite_bound(rl) ? a - rl : HUGE_VAL;
+        const double us = finite_bound(ru) ? ru - a : HUGE_VAL;
+        cmax[q] = dmax(cmax[q], fabs(e.yu[q][i]) * dmin(ls, us));
+      }
+    }
+  };
+  TilePipe<double> pipe;
+  pipe.setup(dsmem);
+  if (!run_tiles<2, double>(pipe, e.csr, e.chunk_rows, scratch, gather, epi) &&
+      threadIdx.x == 0) {
+    raise_error(c);
   }
-  __syncthreads();
-  // part_rows1 holds [pviol0, pviol1, comp0, comp1] per block; maxima are written directly.
+  double mout[2], sums[2];
+  block_max<2>(cmax, scratch, mout);
+  block_sum<2>(acc, scratch, sums);
+  __shared__ int s_last;
   if (threadIdx.x == 0) {
-    e.part_rows1[blockIdx.x * 8 + 2] = mx[0];
-    e.part_rows1[blockIdx.x * 8 + 3] = mx[1];
-  }
-  double two[2] = {packed[0], packed[1]};
-  double sums[2];
-  block_sum<2>(two, smem, sums);
-  __shared__ bool is_last;
-  if (threadIdx.x == 0) {
-    e.part_rows1[blockIdx.x * 8 + 0] = sums[0];
-    e.part_rows1[blockIdx.x * 8 + 1] = sums[1];
+    double* p = e.part_rows1 + blockIdx.x * kEvalRowSlots;
+    p[0] = sums[0];
+    p[1] = sums[1];
+    p[2] = mout[0];
+    p[3] = mout[1];
     __threadfence();
-    const unsigned int t = atomicAdd(&c->ticket[1], 1u);
-    is_last = (t == gridDim.x - 1);
+    s_last = atomicAdd(&c->ticket[kTicketEvalRows], 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (!is_last) return;
+  if (!s_last) return;
   __threadfence();
 
-  // ---- Last block: combine the three passes in a fixed order. ----
+  // ---- Last block: long rows, then every partial in a fixed order. ----
+  acc[0] = acc[1] = 0.0;
+  cmax[0] = cmax[1] = 0.0;
+  run_long_rows<2>(e.csr, e.chunk_rows, epi);
   double s[15];
 #pragma unroll
   for (int q = 0; q < 15; ++q) s[q] = 0.0;
-  double m4[4] = {0.0, 0.0, 0.0, 0.0};
+  double m4[4] = {cmax[0], cmax[1], 0.0, 0.0};
+  s[5] = acc[0];
+  s[6] = acc[1];
   for (int b = threadIdx.x; b < e.grid_rows; b += blockDim.x) {
-    for (int q = 0; q < 5; ++q) s[q] += ldcg(e.part_rows0 + b * 8 + q);
-    s[5] += ldcg(e.part_rows1 + b * 8 + 0);
-    s[6] += ldcg(e.part_rows1 + b * 8 + 1);
-    m4[0] = dmax(m4[0], ldcg(e.part_rows1 + b * 8 + 2));
-    m4[1] = dmax(m4[1], ldcg(e.part_rows1 + b * 8 + 3));
+    for (int q = 0; q < 5; ++q) s[q] += __ldcg(e.part_rows0 + b * kEvalRowSlots + q);
+    s[5] += __ldcg(e.part_rows1 + b * kEvalRowSlots + 0);
+    s[6] += __ldcg(e.part_rows1 + b * kEvalRowSlots + 1);
+    m4[0] = dmax(m4[0], __ldcg(e.part_rows1 + b * kEvalRowSlots + 2));
+    m4[1] = dmax(m4[1], __ldcg(e.part_rows1 + b * kEvalRowSlots + 3));
   }
-  for (int b = threadIdx.x; b < e.grid_cols; b += blockDim.x) {
-    for (int q = 0; q < 8; ++q) s[7 + q] += ldcg(e.part_cols + b * 16 + q);
-    m4[2] = dmax(m4[2], ldcg(e.part_cols + b * 16 + 8));
-    m4[3] = dmax(m4[3], ldcg(e.part_cols + b * 16 + 9));
+  for (int b = threadIdx.x; b <= e.grid_cols; b += blockDim.x) {
+    for (int q = 0; q < 8; ++q) s[7 + q] += __ldcg(e.part_cols + b * kEvalColSlots + q);
+    m4[2] = dmax(m4[2], __ldcg(e.part_cols + b * kEvalColSlots + 8));
+    m4[3] = dmax(m4[3], __ldcg(e.part_cols + b * kEvalColSlots + 9));
   }
   double t15[15];
-  block_sum<15>(s, smem, t15);
+  block_sum<15>(s, scratch, t15);
   double t4[4];
-  block_max<4>(m4, smem, t4);
+  block_max<4>(m4, scratch, t4);
   if (threadIdx.x != 0) return;
-  c->ticket[1] = 0;
+  c->ticket[kTicketEvalRows] = 0;
   // t15: [0] support0 [1] rviol0 [2] support1 [3] rviol1 [4] dy^2 [5] pviol0 [6] pviol1
   //      [7] cviol0 [8] bc0 [9] pobj0 [10] cviol1 [11] bc1 [12] pobj1 [13] dx^2 [14] model obj
   const Residuals cur = assemble(t15[5], t15[7], t15[1], t15[8], t15[0], t15[9],
@@ -490,8 +459,11 @@ __global__ void __launch_bounds__(kTileThreads) k_eval_rows1(EvalBuffers e) {
     c->log[slot].gap = chosen.gap;
     c->log_count += 1;
   }
-  if (meets_request(chosen, c->tolerance) &&
-      (c->stop_at_request || meets_project_standard(chosen))) {
+  const bool stop_here =
+      c->stop_rule == 1 ? worst(chosen) <= c->tolerance
+                        : meets_request(chosen, c->tolerance) &&
+                              (c->stop_at_request || meets_project_standard(chosen));
+  if (stop_here) {
     c->best = chosen;
     c->copy_best = which;
     c->done = kConverged;
@@ -536,15 +508,15 @@ __global__ void k_eval_apply(EvalBuffers e) {
     if (k < e.n) {
       if (copy) e.best_x[k] = e.xu[copy - 1][k];
       if (restart) {
-        const_cast<double*>(e.x_rst)[k] = e.x[cur][k];
-        const_cast<double*>(e.x_sum)[k] = 0.0;
+        e.x_rst[k] = e.x[cur][k];
+        e.x_sum[k] = 0.0;
       }
     }
     if (k < e.m) {
       if (copy) e.best_y[k] = e.yu[copy - 1][k];
       if (restart) {
-        const_cast<double*>(e.y_rst)[k] = e.y[cur][k];
-        const_cast<double*>(e.y_sum)[k] = 0.0;
+        e.y_rst[k] = e.y[cur][k];
+        e.y_sum[k] = 0.0;
       }
     }
   }
@@ -592,27 +564,45 @@ __global__ void k_scale_vectors(int m, int n, const double* cost, const double* 
                                 double* us, double* rls, double* rus) {
   const int total = m > n ? m : n;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
+    // An absent bound is stored as an IEEE infinity (the reference keeps +-1e30 as is and
+    // tests it with is_finite_bound each time), so the step kernels project with min/max.
     if (k < n) {
       const double d = dc[k];
       cs[k] = cost[k] * d;
       const double inv = 1.0 / d;
-      ls[k] = finite_bound(l[k]) ? l[k] * inv : l[k];
-      us[k] = finite_bound(u[k]) ? u[k] * inv : u[k];
+      ls[k] = finite_bound(l[k]) ? l[k] * inv : -HUGE_VAL;
+      us[k] = finite_bound(u[k]) ? u[k] * inv : HUGE_VAL;
     }
     if (k < m) {
       const double d = dr[k];
-      rls[k] = finite_bound(rl[k]) ? rl[k] * d : rl[k];
-      rus[k] = finite_bound(ru[k]) ? ru[k] * d : ru[k];
+      rls[k] = finite_bound(rl[k]) ? rl[k] * d : -HUGE_VAL;
+      rus[k] = finite_bound(ru[k]) ? ru[k] * d : HUGE_VAL;
     }
   }
 }
 
-__global__ void __launch_bounds__(kTileThreads) k_spmv(Matrix<double> a, const double* x,
-                                                       double* y) {
-  __shared__ double smem[kTileCap];
-  tile_loop<1>(
-      a, smem, [&](int, int col, double v, double* p) { p[0] = v * __ldg(x + col); },
-      [&](int r, const double* s) { y[r] = 0.0 + s[0]; });
+// y = A x with products summed in ascending index order per row.
+__global__ void __launch_bounds__(kTileThreads) k_spmv(TileSet<double> a, const double* x,
+                                                       double* y, double* chunk,
+                                                       unsigned int* ticket) {
+  extern __shared__ __align__(16) unsigned char dsmem[];
+  __shared__ double scratch[kScratch];
+  auto gather = [&](int col, double v, double* acc) { acc[0] = fma(v, __ldg(x + col), acc[0]); };
+  auto epi = [&](int r, const double* s) { y[r] = 0.0 + s[0]; };
+  TilePipe<double> pipe;
+  pipe.setup(dsmem);
+  run_tiles<1, double>(pipe, a, chunk, scratch, gather, epi);
+  if (a.nlong == 0) return;
+  __shared__ int s_last;
+  if (threadIdx.x == 0) {
+    __threadfence();  // this block's chunk partials (written by thread 0) before the ticket
+    s_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  run_long_rows<1>(a, chunk, epi);
+  if (threadIdx.x == 0) *ticket = 0;
 }
 
 __global__ void k_sumsq(const double* v, int count, double* part, double* out,
@@ -620,7 +610,7 @@ __global__ void k_sumsq(const double* v, int count, double* part, double* out,
   __shared__ double scratch[kTileThreads / 32];
   double acc[1] = {0.0};
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
-    acc[0] += v[k] * v[k];
+    acc[0] = fma(v[k], v[k], acc[0]);
   }
   double o[1];
   block_sum<1>(acc, scratch, o);
@@ -685,7 +675,7 @@ __global__ void k_abs_minmax(const double* v, int count, double* part, double* o
 
 __global__ void k_project_start(int n, const double* l, const double* u, double* x) {
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
-    x[k] = project(0.0, l[k], u[k]);
+    x[k] = clamp_box(0.0, l[k], u[k]);
   }
 }
 
@@ -694,9 +684,6 @@ __global__ void k_fill(double* v, int count, double value) {
     v[k] = value;
   }
 }
-
-int g_tile_blocks_per_sm = 0;
-int g_num_sms = 0;
 
 int elementwise_grid(int count) {
   if (g_num_sms == 0) {
@@ -710,44 +697,61 @@ int elementwise_grid(int count) {
   return blocks < 1 ? 1 : blocks;
 }
 
-unsigned int* g_scratch_ticket = nullptr;
-
-unsigned int* scratch_ticket() {
-  if (g_scratch_ticket == nullptr) {
-    cudaMalloc(&g_scratch_ticket, sizeof(unsigned int));
-    cudaMemset(g_scratch_ticket, 0, sizeof(unsigned int));
-  }
-  return g_scratch_ticket;
-}
+constexpr int kTileSmem = tile_smem_bytes<double>();
 
 }  // namespace
 
+void configure_tile_kernels() {
+  static bool done = false;
+  if (done) return;
+  cudaFuncSetAttribute(k_primal, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
+  cudaFuncSetAttribute(k_dual, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
+  cudaFuncSetAttribute(k_eval_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
+  cudaFuncSetAttribute(k_eval_rows1, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
+  cudaFuncSetAttribute(k_spmv, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
+  done = true;
+}
+
 int tile_blocks_per_sm() {
   if (g_tile_blocks_per_sm == 0) {
+    configure_tile_kernels();
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dual, kTileThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dual, kTileThreads, kTileSmem);
     g_tile_blocks_per_sm = per_sm > 0 ? per_sm : 1;
   }
   return g_tile_blocks_per_sm;
 }
 
-void launch_pdhg_step(const StepBuffers& b, cudaStream_t s) {
-  k_primal<<<b.grid_primal, kTileThreads, 0, s>>>(b);
-  k_dual<<<b.grid_dual, kTileThreads, 0, s>>>(b);
+long long kernel_launch_count() { return g_launches; }
+
+void launch_primal_pass(const StepBuffers& b, cudaStream_t s) {
+  k_primal<<<b.grid_primal, kTileThreads, kTileSmem, s>>>(b);
+  ++g_launches;
 }
 
-void launch_evaluation(const EvalBuffers& e, const StepBuffers& b, cudaStream_t s) {
-  (void)b;
+void launch_dual_pass(const StepBuffers& b, cudaStream_t s) {
+  k_dual<<<b.grid_dual, kTileThreads, kTileSmem, s>>>(b);
+  ++g_launches;
+}
+
+void launch_pdhg_step(const StepBuffers& b, cudaStream_t s) {
+  launch_primal_pass(b, s);
+  launch_dual_pass(b, s);
+}
+
+void launch_evaluation(const EvalBuffers& e, cudaStream_t s) {
+  g_launches += 4;
   k_eval_rows0<<<e.grid_rows, kTileThreads, 0, s>>>(e);
-  k_eval_cols<<<e.grid_cols, kTileThreads, 0, s>>>(e);
-  k_eval_rows1<<<e.grid_rows, kTileThreads, 0, s>>>(e);
+  k_eval_cols<<<e.grid_cols, kTileThreads, kTileSmem, s>>>(e);
+  k_eval_rows1<<<e.grid_rows, kTileThreads, kTileSmem, s>>>(e);
   const int total = e.m > e.n ? e.m : e.n;
   k_eval_apply<<<elementwise_grid(total), 256, 0, s>>>(e);
 }
 
-void launch_scaling_round(int m, int n, Matrix<double> csr, Matrix<double> csc, double* csr_val,
+void launch_scaling_round(int m, int n, TileSet<double> csr, TileSet<double> csc, double* csr_val,
                           double* csc_val, double* row_acc, double* col_acc, double* dr,
                           double* dc, int sum_mode, cudaStream_t s) {
+  g_launches += 6;
   k_line_factor<<<elementwise_grid(m), 256, 0, s>>>(csr.ptr, csr_val, m, sum_mode, row_acc);
   k_line_factor<<<elementwise_grid(n), 256, 0, s>>>(csc.ptr, csc_val, n, sum_mode, col_acc);
   k_apply_pass<<<elementwise_grid(m), 256, 0, s>>>(csr.ptr, csr.idx, csr_val, m, row_acc, col_acc,
@@ -762,35 +766,43 @@ void launch_scale_vectors(int m, int n, const double* cost, const double* l, con
                           const double* rl, const double* ru, const double* dr, const double* dc,
                           double* cs, double* ls, double* us, double* rls, double* rus,
                           cudaStream_t s) {
+  ++g_launches;
   k_scale_vectors<<<elementwise_grid(m > n ? m : n), 256, 0, s>>>(m, n, cost, l, u, rl, ru, dr, dc,
                                                                   cs, ls, us, rls, rus);
 }
 
-void launch_spmv(Matrix<double> a, const double* x, double* y, cudaStream_t s, int grid) {
+void launch_spmv(TileSet<double> a, const double* x, double* y, double* chunk,
+                 unsigned int* ticket, cudaStream_t s, int grid) {
   if (a.nrows == 0) return;
-  k_spmv<<<grid, kTileThreads, 0, s>>>(a, x, y);
+  ++g_launches;
+  k_spmv<<<grid, kTileThreads, kTileSmem, s>>>(a, x, y, chunk, ticket);
 }
 
-void launch_sumsq(const double* v, int count, double* part, double* out, cudaStream_t s,
-                  int grid) {
-  k_sumsq<<<grid, kTileThreads, 0, s>>>(v, count, part, out, scratch_ticket());
+void launch_sumsq(const double* v, int count, double* part, double* out, unsigned int* ticket,
+                  cudaStream_t s, int grid) {
+  ++g_launches;
+  k_sumsq<<<grid, kTileThreads, 0, s>>>(v, count, part, out, ticket);
 }
 
 void launch_scale_div(double* v, int count, const double* by_sqrt_of, cudaStream_t s) {
+  ++g_launches;
   k_div_by_sqrt<<<elementwise_grid(count), 256, 0, s>>>(v, count, by_sqrt_of);
 }
 
-void launch_abs_minmax(const double* v, int count, double* part, double* out, cudaStream_t s,
-                       int grid) {
-  k_abs_minmax<<<grid, kTileThreads, 0, s>>>(v, count, part, out, scratch_ticket());
+void launch_abs_minmax(const double* v, int count, double* part, double* out,
+                       unsigned int* ticket, cudaStream_t s, int grid) {
+  ++g_launches;
+  k_abs_minmax<<<grid, kTileThreads, 0, s>>>(v, count, part, out, ticket);
 }
 
 void launch_project_start(int n, const double* l, const double* u, double* x, cudaStream_t s) {
+  ++g_launches;
   k_project_start<<<elementwise_grid(n), 256, 0, s>>>(n, l, u, x);
 }
 
 void launch_fill(double* v, int count, double value, cudaStream_t s) {
   if (count <= 0) return;
+  ++g_launches;
   k_fill<<<elementwise_grid(count), 256, 0, s>>>(v, count, value);
 }
 

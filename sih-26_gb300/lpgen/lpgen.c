@@ -280,7 +280,12 @@ int64_t lpgen_planted_general_nnz(int32_t m, int32_t n, int32_t k) {
   return (int64_t)n * k;
 }
 
-int32_t lpgen_planted_general(int32_t m, int32_t n, int32_t k, uint64_t seed, lpgen_lp* lp) {
+/* flags: bit 0 leaves out free columns, bit 1 leaves out free rows (they become one-sided).
+ * SANKHYA's optimality standard multiplies a free column's reduced cost (a free row's
+ * multiplier) by an infinite slack, so an LP with either is `optimal` only when that value is
+ * exactly zero -- a matter of rounding luck, unfit for comparing two implementations. */
+int32_t lpgen_planted_general(int32_t m, int32_t n, int32_t k, int32_t flags, uint64_t seed,
+                              lpgen_lp* lp) {
   if (m <= 0 || n <= 0 || k <= 0 || k > m) return 1;
   mt64* g = (mt64*)malloc(sizeof(mt64));
   mt64_seed(g, seed);
@@ -297,7 +302,8 @@ int32_t lpgen_planted_general(int32_t m, int32_t n, int32_t k, uint64_t seed, lp
     for (int32_t t = 0; t < k; ++t) lp->values[at + t] = normal(g);
     at += k;
     double l, u, x, zz = 0.0;
-    const int kind = unif_int(g, 6);
+    int kind = unif_int(g, 6);
+    if (kind == 3 && (flags & 1)) kind = 1;
     const double state = unif(g);
     switch (kind) {
       case 0: /* boxed, arbitrary interval */
@@ -350,7 +356,9 @@ int32_t lpgen_planted_general(int32_t m, int32_t n, int32_t k, uint64_t seed, lp
   for (int32_t i = 0; i < m; ++i) {
     const double a = act[i];
     double rl, ru, lam = 0.0;
-    switch (unif_int(g, 8)) {
+    int row_kind = unif_int(g, 8);
+    if (row_kind == 7 && (flags & 2)) row_kind = 2;
+    switch (row_kind) {
       case 0: rl = a; ru = a; lam = normal(g); break;
       case 1: rl = a; ru = inf; lam = unif_ab(g, 0.1, 1.0); break;
       case 2: rl = a - unif_ab(g, 0.5, 2.0); ru = inf; break;

@@ -5,7 +5,8 @@ There is no CPU fallback: if the library is missing or no GPU is usable, every c
 ``sankhya::gpu::solve_pdhg_gpu(model, options, logger, control)`` (src/gpu/pdhg_gpu.hpp:19)
 and takes the reference's option names (src/util/options.cpp): ``pdhg_tolerance``,
 ``iteration_limit``, ``time_limit``, ``pdhg_restart``, ``pdhg_stop_at_request``,
-``random_seed``, plus the engine's ``pdhg_precision`` ("fp64" | "mixed").
+``random_seed``, plus the engine's ``pdhg_precision`` ("fp64" | "mixed") and
+``pdhg_stop_rule`` ("standard" | "relative").
 """
 from __future__ import annotations
 
@@ -25,6 +26,7 @@ STATUS_NAMES = {0: "not_solved", 1: "optimal", 2: "feasible", 3: "infeasible",
                 5: "iteration_limit", 6: "time_limit", 8: "numerical_error", 9: "model_error",
                 11: "interrupted"}
 PRECISIONS = {"fp64": 0, "mixed": 1}
+STOP_RULES = {"standard": 0, "relative": 1}
 
 _D = ctypes.POINTER(ctypes.c_double)
 _I = ctypes.POINTER(ctypes.c_int32)
@@ -50,6 +52,7 @@ class CParams(ctypes.Structure):
                 ("time_limit", ctypes.c_double), ("restart", ctypes.c_int32),
                 ("stop_at_request", ctypes.c_int32), ("random_seed", ctypes.c_int64),
                 ("precision", ctypes.c_int32), ("steps_per_poll", ctypes.c_int32),
+                ("stop_rule", ctypes.c_int32), ("reserved", ctypes.c_int32),
                 ("interrupt", ctypes.POINTER(ctypes.c_int32)), ("log", LOG_FN),
                 ("log_user", ctypes.c_void_p)]
 
@@ -72,6 +75,7 @@ class CResult(ctypes.Structure):
                 ("spectral_norm", ctypes.c_double), ("scaled_min_abs", ctypes.c_double),
                 ("scaled_max_abs", ctypes.c_double), ("setup_seconds", ctypes.c_double),
                 ("loop_seconds", ctypes.c_double), ("solve_seconds", ctypes.c_double),
+                ("device_seconds", ctypes.c_double), ("kernel_launches", ctypes.c_int64),
                 ("message", ctypes.c_char * 512)]
 
 
@@ -80,7 +84,7 @@ EXPORTS = [
     "sankhya_gb300_device_free_memory", "sankhya_gb300_device_compute_capability",
     "sankhya_gb300_estimate_memory", "sankhya_gb300_pdhg_create", "sankhya_gb300_pdhg_destroy",
     "sankhya_gb300_pdhg_load", "sankhya_gb300_pdhg_solve", "sankhya_gb300_pdhg_solution",
-    "sankhya_gb300_pdhg_scaling", "sankhya_gb300_pdhg_spmv",
+    "sankhya_gb300_pdhg_scaling", "sankhya_gb300_pdhg_spmv", "sankhya_gb300_pdhg_time_kernels",
 ]
 
 _lib = None
@@ -117,6 +121,7 @@ def load_library():
         lib.sankhya_gb300_pdhg_scaling.argtypes = [ctypes.c_void_p, ctypes.c_int64, _D, _D, _D, _D]
         lib.sankhya_gb300_pdhg_spmv.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                                 _D, _D]
+        lib.sankhya_gb300_pdhg_time_kernels.argtypes = [ctypes.c_void_p, ctypes.c_int32, _D]
         for name in EXPORTS:
             if name not in ("sankhya_gb300_last_error", "sankhya_gb300_estimate_memory"):
                 getattr(lib, name).restype = ctypes.c_int
@@ -165,6 +170,8 @@ class Result:
     setup_seconds: float
     loop_seconds: float
     solve_seconds: float
+    device_seconds: float
+    kernel_launches: int
     message: str
 
 
@@ -208,21 +215,29 @@ class PdhgEngine:
               time_limit: Optional[float] = None, restart: bool = True,
               stop_at_request: bool = False, random_seed: int = 0, precision: str = "fp64",
               steps_per_poll: int = 0, interrupt: Optional[np.ndarray] = None,
-              log: Optional[Callable] = None) -> Result:
+              log: Optional[Callable] = None, stop_rule: str = "standard") -> Result:
         cb = LOG_FN(lambda user, it, obj, p, d, s: log(it, obj, p, d, s)) if log else LOG_FN()
         intr = (interrupt.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
                 if interrupt is not None else ctypes.POINTER(ctypes.c_int32)())
         params = CParams(tolerance, iteration_limit,
                          1e308 if time_limit is None else float(time_limit), int(restart),
                          int(stop_at_request), random_seed, PRECISIONS[precision],
-                         steps_per_poll, intr, cb, None)
+                         steps_per_poll, STOP_RULES[stop_rule], 0, intr, cb, None)
         r = CResult()
         _check(self._lib.sankhya_gb300_pdhg_solve(self._h, ctypes.byref(params), ctypes.byref(r)))
         return Result(r.status, STATUS_NAMES.get(r.status, str(r.status)), bool(r.converged),
                       r.iterations, r.attempts, r.restarts, r.evaluations, r.refinements,
                       r.objective, r.dual_bound, r.final_residuals.as_dict(), r.spectral_norm,
                       r.scaled_min_abs, r.scaled_max_abs, r.setup_seconds, r.loop_seconds,
-                      r.solve_seconds, r.message.decode(errors="replace"))
+                      r.solve_seconds, r.device_seconds, r.kernel_launches,
+                      r.message.decode(errors="replace"))
+
+    def time_kernels(self, reps: int = 20):
+        """Mean device milliseconds of the primal and the dual pass (CUDA events on the
+        engine's stream), measured on the state of the last solve."""
+        ms = np.zeros(2)
+        _check(self._lib.sankhya_gb300_pdhg_time_kernels(self._h, reps, _ptr(ms)))
+        return float(ms[0]), float(ms[1])
 
     def solution(self):
         lp = self._lp
@@ -273,7 +288,7 @@ def solve_pdhg_gpu(lp: LP, options: Optional[dict] = None, device: int = 0,
     model defect is status "model_error", a device failure raises EngineError."""
     o = {"pdhg_tolerance": 1e-4, "iteration_limit": -1, "time_limit": None,
          "pdhg_restart": True, "pdhg_stop_at_request": False, "random_seed": 0,
-         "pdhg_precision": "fp64", "steps_per_poll": 0}
+         "pdhg_precision": "fp64", "pdhg_stop_rule": "standard", "steps_per_poll": 0}
     o.update(options or {})
     own = engine is None
     eng = engine or PdhgEngine(device)
@@ -290,7 +305,7 @@ def solve_pdhg_gpu(lp: LP, options: Optional[dict] = None, device: int = 0,
                       time_limit=o["time_limit"], restart=o["pdhg_restart"],
                       stop_at_request=o["pdhg_stop_at_request"], random_seed=o["random_seed"],
                       precision=o["pdhg_precision"], steps_per_poll=o["steps_per_poll"],
-                      interrupt=interrupt, log=log)
+                      interrupt=interrupt, log=log, stop_rule=o["pdhg_stop_rule"])
         x, d, y = eng.solution()
         return Solution(r.status_name, r.objective, r.dual_bound, x, d, y, r.iterations,
                         r.message, "pdhg-gpu", r)

@@ -41,11 +41,13 @@ def _load():
             raise RuntimeError(f"{_paths.LPGEN_LIB} is not built; run __graft_entry__.build()")
         lib = ctypes.CDLL(_paths.LPGEN_LIB)
         for name in ("lpgen_planted_uniform", "lpgen_planted_general"):
-            getattr(lib, name).argtypes = [ctypes.c_int32] * 3 + [ctypes.c_uint64,
-                                                                  ctypes.POINTER(_CLp)]
-            getattr(lib, name).restype = ctypes.c_int32
             getattr(lib, name + "_nnz").argtypes = [ctypes.c_int32] * 3
             getattr(lib, name + "_nnz").restype = ctypes.c_int64
+            getattr(lib, name).restype = ctypes.c_int32
+        lib.lpgen_planted_uniform.argtypes = [ctypes.c_int32] * 3 + [ctypes.c_uint64,
+                                                                     ctypes.POINTER(_CLp)]
+        lib.lpgen_planted_general.argtypes = [ctypes.c_int32] * 4 + [ctypes.c_uint64,
+                                                                     ctypes.POINTER(_CLp)]
         lib.lpgen_planted_blocks.argtypes = [ctypes.c_int32] * 4 + [ctypes.c_uint64,
                                                                     ctypes.POINTER(_CLp)]
         lib.lpgen_planted_blocks.restype = ctypes.c_int32
@@ -95,13 +97,15 @@ def planted_blocks(blocks: int, rows_per_block: int, cols_per_block: int, k: int
     return _finish(arrays, c, f"planted_blocks_{blocks}x{rows_per_block}x{cols_per_block}")
 
 
-def planted_general(m: int, n: int, k: int = 4, seed: int = 1, maximize: bool = False) -> LP:
+def planted_general(m: int, n: int, k: int = 4, seed: int = 1, maximize: bool = False,
+                    free: bool = True) -> LP:
     """Mixed row and column kinds. With ``maximize`` the cost is negated and the sense set
-    to maximise, so the optimum point is unchanged and the objective is ``-fstar``."""
+    to maximise, so the optimum point is unchanged and the objective is ``-fstar``. With
+    ``free=False`` there are no free rows or columns."""
     lib = _load()
     nnz = lib.lpgen_planted_general_nnz(m, n, k)
     arrays, c = _alloc(m, n, nnz)
-    if lib.lpgen_planted_general(m, n, k, seed, ctypes.byref(c)) != 0:
+    if lib.lpgen_planted_general(m, n, k, 0 if free else 3, seed, ctypes.byref(c)) != 0:
         raise ValueError("planted_general: bad shape")
     lp = _finish(arrays, c, f"planted_general_{m}x{n}_s{seed}")
     if maximize:

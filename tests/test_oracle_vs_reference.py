@@ -13,7 +13,8 @@ INF = np.inf
 def _cases():
     yield "uniform_200x500", lpgen.planted_uniform(200, 500, 5, seed=3), dict(tolerance=1e-8)
     for s in range(3):
-        yield (f"general_{s}", lpgen.planted_general(40, 60, 3, seed=s, maximize=s == 1),
+        yield (f"general_{s}", lpgen.planted_general(40, 60, 3, seed=s, maximize=s == 1,
+                                                     free=s != 2),
                dict(tolerance=1e-8, iteration_limit=20000))
     yield "sum", from_dense([[1, 1]], [2], [INF], [1, 1]), dict(tolerance=1e-8)
     yield ("max_3x2", from_dense([[1, 0], [0, 2], [3, 2]], [-INF] * 3, [4, 12, 18], [3, 5],
