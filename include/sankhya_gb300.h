@@ -94,6 +94,11 @@ typedef struct sankhya_gb300_lp {
 typedef void (*sankhya_gb300_log_fn)(void* user, long long iteration, double objective,
                                      double primal, double dual, double seconds);
 
+/* Polled at every status snapshot; a nonzero return interrupts the solve (the reference's
+ * StopController::should_stop, src/core/stop_controller.hpp:36-75: SolveControl::interrupt()
+ * or a progress callback asking to stop). */
+typedef int (*sankhya_gb300_poll_fn)(void* user, long long iteration, double objective);
+
 /* The PDHG option rows (src/util/options.cpp) plus the engine's own. */
 typedef struct sankhya_gb300_params {
   double tolerance;          /* pdhg_tolerance */
@@ -106,9 +111,11 @@ typedef struct sankhya_gb300_params {
   int32_t steps_per_poll;    /* attempted steps per CUDA-graph launch; 0 = default */
   int32_t stop_rule;         /* SANKHYA_GB300_STOP_STANDARD or SANKHYA_GB300_STOP_RELATIVE */
   int32_t reserved;
-  const volatile int32_t* interrupt; /* SolveControl::interrupt flag, polled; may be NULL */
+  const volatile int32_t* interrupt; /* an interrupt flag, polled; may be NULL */
   sankhya_gb300_log_fn log;  /* may be NULL */
   void* log_user;
+  sankhya_gb300_poll_fn poll; /* may be NULL */
+  void* poll_user;
 } sankhya_gb300_params;
 
 /* sankhya::pdhg::Residuals (src/pdhg/pdhg_evaluate.hpp:19-70). */

@@ -1,0 +1,108 @@
+// decisions.cuh -- the scalar decisions of the restarted PDHG, shared by the FP64 loop and
+// the FP32 inner loop of the mixed method. All of it runs on ONE device thread, in FP64.
+#pragma once
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace sgb {
+
+// Adaptive step, src/pdhg/pdhg.cpp:252-335: accept iff eta <= movement / interaction, then
+// eta <- clamp(min(shrink * limit, grow * eta), 1e-12, ceiling) unless the step carried no
+// information; an accepted step flips the current buffer and counts an iteration.
+__device__ inline void step_decision(Ctl* c, double movement, double interaction) {
+  c->movement = movement;
+  c->interaction = interaction;
+  const bool no_information = interaction <= 0.0;
+  const double limit = no_information ? __longlong_as_double(0x7ff0000000000000LL)
+                                      : movement / interaction;
+  const long long e = c->iteration + 1 > 2 ? c->iteration + 1 : 2;
+  const double exponent = static_cast<double>(e);
+  const double shrink = 1.0 - pow(exponent, -0.3);
+  const double grow = 1.0 + pow(exponent, -0.6);
+  const double proposed = dmin(shrink * limit, grow * c->eta);
+  const bool accept = c->eta <= limit;
+  if (accept) {
+    c->cur ^= 1;
+    c->iteration += 1;
+    c->averaged += 1;
+    c->pending_add = 1;
+  } else {
+    c->pending_add = 0;
+  }
+  if (!no_information) {
+    double eta = proposed;
+    eta = eta < 1e-12 ? 1e-12 : (c->eta_ceiling < eta ? c->eta_ceiling : eta);
+    c->eta = eta;
+  }
+  c->attempts += 1;
+  c->accepted = accept;
+  c->no_information = no_information;
+  c->eval_now = (c->iteration > 0) && ((c->iteration % 40) == 0 || no_information);
+}
+
+// The evaluation-tick decisions of src/pdhg/pdhg.cpp:349-483 given the assembled residuals
+// of the current candidate and (if averaged > 0) of the average: the better one, the best
+// so far, the stop test, the restart and the primal-weight update. `stop_here` is the
+// caller's stopping test applied to the chosen candidate. dx2 / dy2 are the squared
+// distances of the current iterate from the restart anchor. omega_lo / omega_hi clamp the
+// primal weight (the reference uses 1e-6 and 1e6).
+__device__ inline void tick_decisions(Ctl* c, const Residuals& cur, const Residuals* avg,
+                                      bool (*stop_test)(const Ctl*, const Residuals&),
+                                      double dx2, double dy2, double omega_lo,
+                                      double omega_hi) {
+  c->evaluations += 1;
+  Residuals chosen = cur;
+  int which = 1;
+  if (avg != nullptr && worst(*avg) < worst(cur)) {
+    chosen = *avg;
+    which = 2;
+  }
+  int copy = 0;
+  if (worst(chosen) < worst(c->best)) {
+    c->best = chosen;
+    copy = which;
+  }
+  {
+    const long long slot = c->log_count % kLogRing;
+    c->log[slot].iteration = c->iteration;
+    c->log[slot].primal_objective = chosen.primal_objective;
+    c->log[slot].primal = chosen.primal;
+    c->log[slot].dual = chosen.dual;
+    c->log[slot].gap = chosen.gap;
+    c->log_count += 1;
+  }
+  if (stop_test(c, chosen)) {
+    c->best = chosen;
+    c->copy_best = which;
+    c->done = kConverged;
+    return;
+  }
+  c->copy_best = copy;
+  if (c->use_restarts) {
+    const double kkt = worst(chosen);
+    const long long since = c->iteration - c->last_restart;
+    const bool sufficient = kkt <= 0.2 * c->restart_kkt;
+    const long long f36 = static_cast<long long>(0.36 * static_cast<double>(c->iteration));
+    const bool artificial = since >= (f36 > 40 ? f36 : 40);
+    if (sufficient || artificial) {
+      const double dx_norm = sqrt(dx2);
+      const double dy_norm = sqrt(dy2);
+      if (dx_norm > 1e-12 && dy_norm > 1e-12) {
+        const double theta = 0.5;
+        double omega = exp(theta * log(dy_norm / dx_norm) + (1.0 - theta) * log(c->omega));
+        omega = omega < omega_lo ? omega_lo : (omega_hi < omega ? omega_hi : omega);
+        c->omega = omega;
+      }
+      c->do_restart = 1;
+      c->averaged = 0;
+      c->pending_add = 0;
+      c->restart_kkt = kkt;
+      c->last_restart = c->iteration;
+      c->restarts += 1;
+      if (c->inner_mode) c->done = kRestartRound;
+    }
+  }
+}
+
+}  // namespace sgb

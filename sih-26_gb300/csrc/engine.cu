@@ -66,10 +66,13 @@ void DeviceArray<T>::release() {
 }
 template struct DeviceArray<int>;
 template struct DeviceArray<int2>;
+template struct DeviceArray<double2>;
+template struct DeviceArray<float2>;
 template struct DeviceArray<Tile>;
 template struct DeviceArray<LongRow>;
 template struct DeviceArray<unsigned int>;
 template struct DeviceArray<double>;
+template struct DeviceArray<float>;
 template struct DeviceArray<Ctl>;
 
 namespace {
@@ -163,10 +166,16 @@ Engine::Engine(int device) : device_(device) {
   SGB_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device));
   SGB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&snapshot_), 2 * sizeof(Ctl),
                          cudaHostAllocDefault));
+  SGB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&snapshot_mixed_), 2 * sizeof(Ctl),
+                         cudaHostAllocDefault));
   for (auto& ev : done_event_) SGB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   for (auto& ev : timing_) SGB_CUDA(cudaEventCreate(&ev));
   ctl_.allocate(1);
   SGB_CUDA(cudaMemset(ctl_.ptr, 0, sizeof(Ctl)));
+  ctl_mixed_.allocate(1);
+  SGB_CUDA(cudaMemset(ctl_mixed_.ptr, 0, sizeof(Ctl)));
+  configure_tile_kernels();
+  configure_mixed_kernels();
 }
 
 Engine::~Engine() {
@@ -179,6 +188,7 @@ Engine::~Engine() {
     if (ev != nullptr) cudaEventDestroy(ev);
   }
   if (snapshot_ != nullptr) cudaFreeHost(snapshot_);
+  if (snapshot_mixed_ != nullptr) cudaFreeHost(snapshot_mixed_);
   if (stream_ != nullptr) cudaStreamDestroy(stream_);
 }
 
@@ -187,7 +197,105 @@ void Engine::destroy_graphs() {
     if (g != nullptr) cudaGraphExecDestroy(g);
     g = nullptr;
   }
+  for (auto& g : mgraph_exec_) {
+    if (g != nullptr) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
   graph_steps_ = 0;
+  mgraph_steps_ = 0;
+}
+
+// The FP32 copies, the correction problem and the FP64 anchor of the mixed method.
+void Engine::allocate_mixed() {
+  if (mixed_ready_) return;
+  cudaStream_t s = stream_;
+  const size_t z = static_cast<size_t>(nnz_), n = static_cast<size_t>(n_);
+  const size_t m = static_cast<size_t>(m_);
+  csc_f_.allocate_padded(z, kPad, s);
+  csr_f_.allocate_padded(z, kPad, s);
+  for (DeviceArray<float>* a : {&u0f_, &u1f_, &usumf_, &urstf_, &cf_, &lf_, &uf_, &uc0_, &uc1_,
+                                &ubest_, &csf_}) {
+    a->allocate(n);
+  }
+  for (DeviceArray<float>* a : {&v0f_, &v1f_, &vsumf_, &vrstf_, &gu_, &gl_, &yhat_, &vc0_, &vc1_,
+                                &vbest_}) {
+    a->allocate(m);
+  }
+  udf_.allocate(n);
+  for (DeviceArray<double>* a : {&anchor_x_, &aty64_}) a->allocate(n);
+  for (DeviceArray<double>* a : {&anchor_y_, &ax64_}) a->allocate(m);
+  fill_mixed_buffers();
+  mixed_ready_ = true;
+}
+
+void Engine::fill_mixed_buffers() {
+  MixedBuffers& b = mixed_;
+  b.ctl = ctl_mixed_.ptr;
+  b.csc = TileSet<float>{csc_ptr_.ptr,   csc_idx_.ptr,  csc_f_.ptr,   csc_tiles_f_.ptr,
+                         csc_longs_.ptr, ntiles_csc_f_, nlong_csc_,   nchunks_csc_,
+                         n_,             lanes_csc_f_};
+  b.csr = TileSet<float>{csr_ptr_.ptr,   csr_idx_.ptr,  csr_f_.ptr,   csr_tiles_f_.ptr,
+                         csr_longs_.ptr, ntiles_csr_f_, nlong_csr_,   nchunks_csr_,
+                         m_,             lanes_csr_f_};
+  b.u[0] = u0f_.ptr;
+  b.u[1] = u1f_.ptr;
+  b.v[0] = v0f_.ptr;
+  b.v[1] = v1f_.ptr;
+  b.u_sum = usumf_.ptr;
+  b.v_sum = vsumf_.ptr;
+  b.u_rst = urstf_.ptr;
+  b.v_rst = vrstf_.ptr;
+  b.ud = udf_.ptr;
+  b.cf = cf_.ptr;
+  b.lf = lf_.ptr;
+  b.uf = uf_.ptr;
+  b.cs = csf_.ptr;
+  b.gu = gu_.ptr;
+  b.gl = gl_.ptr;
+  b.yhat = yhat_.ptr;
+  b.uc[0] = uc0_.ptr;
+  b.uc[1] = uc1_.ptr;
+  b.vc[0] = vc0_.ptr;
+  b.vc[1] = vc1_.ptr;
+  b.u_best = ubest_.ptr;
+  b.v_best = vbest_.ptr;
+  b.part_primal = part_primal_.ptr;
+  b.part_dual = part_dual_.ptr;
+  b.chunk_primal = chunk_primal_.ptr;
+  b.chunk_dual = chunk_dual_.ptr;
+  b.part_rows0 = part_rows0_.ptr;
+  b.part_cols = part_cols_.ptr;
+  b.part_rows1 = part_rows1_.ptr;
+  b.chunk_cols = chunk_cols_.ptr;
+  b.chunk_rows = chunk_rows_.ptr;
+  b.grid_primal = grid_csc_f_;
+  b.grid_dual = grid_csr_f_;
+  b.m = m_;
+  b.n = n_;
+}
+
+void Engine::build_mixed_graphs(int steps) {
+  if (mgraph_steps_ == steps && mgraph_exec_[0] != nullptr) return;
+  for (auto& g : mgraph_exec_) {
+    if (g != nullptr) cudaGraphExecDestroy(g);
+    g = nullptr;
+  }
+  for (int slot = 0; slot < 2; ++slot) {
+    cudaGraph_t graph = nullptr;
+    SGB_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    for (int k = 0; k < steps; ++k) {
+      launch_mixed_step(mixed_, stream_);
+      launch_mixed_evaluation(mixed_, stream_);
+    }
+    cudaMemcpyAsync(snapshot_mixed_ + slot, ctl_mixed_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost,
+                    stream_);
+    const cudaError_t end = cudaStreamEndCapture(stream_, &graph);
+    SGB_CUDA(end);
+    const cudaError_t inst = cudaGraphInstantiate(&mgraph_exec_[slot], graph, 0);
+    cudaGraphDestroy(graph);
+    SGB_CUDA(inst);
+  }
+  mgraph_steps_ = steps;
 }
 
 void Engine::require_loaded() const {
@@ -243,7 +351,7 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   }
   SGB_CUDA(cudaSetDevice(device_));
   destroy_graphs();
-  loaded_ = solved_ = scaled_ = false;
+  loaded_ = solved_ = scaled_ = mixed_ready_ = false;
   m_ = m;
   n_ = n;
   nnz_ = nnz;
@@ -266,19 +374,38 @@ void Engine::load(const sankhya_gb300_lp& lp) {
       rval[slot] = lp.values[k];
     }
   }
-  std::vector<Tile> ctiles, rtiles;
+  // Two tile layouts per pattern. FP64 kernels run one row per thread: GB300's FP64 pipe
+  // charges per warp instruction, so lanes that sit out an epilogue or add up a row that is
+  // split across lanes cost as much as working ones. The FP32 kernels are bound by memory
+  // latency instead and split rows over `lanes` threads so every thread issues gathers.
+  // The chunking of long rows does not depend on the lanes, so both layouts share it.
+  std::vector<Tile> ctiles, rtiles, ctiles_f, rtiles_f;
   std::vector<LongRow> clongs, rlongs;
-  lanes_csc_ = choose_lanes(n > 0 ? static_cast<double>(nnz) / n : 1.0);
-  lanes_csr_ = choose_lanes(m > 0 ? static_cast<double>(nnz) / m : 1.0);
+  int unused_chunks = 0;
+  lanes_csc_ = 1;
+  lanes_csr_ = 1;
+  lanes_csc_f_ = choose_lanes(n > 0 ? static_cast<double>(nnz) / n : 1.0);
+  lanes_csr_f_ = choose_lanes(m > 0 ? static_cast<double>(nnz) / m : 1.0);
   build_tiles(cptr, n, lanes_csc_, &ctiles, &clongs, &nchunks_csc_);
   build_tiles(rptr, m, lanes_csr_, &rtiles, &rlongs, &nchunks_csr_);
+  {
+    std::vector<LongRow> same;
+    build_tiles(cptr, n, lanes_csc_f_, &ctiles_f, &same, &unused_chunks);
+    build_tiles(rptr, m, lanes_csr_f_, &rtiles_f, &same, &unused_chunks);
+  }
   ntiles_csc_ = static_cast<int>(ctiles.size());
   ntiles_csr_ = static_cast<int>(rtiles.size());
+  ntiles_csc_f_ = static_cast<int>(ctiles_f.size());
+  ntiles_csr_f_ = static_cast<int>(rtiles_f.size());
   nlong_csc_ = static_cast<int>(clongs.size());
   nlong_csr_ = static_cast<int>(rlongs.size());
   const int resident = tile_blocks_per_sm() * num_sms_;
   grid_csc_ = std::max(1, std::min(ntiles_csc_, resident));
   grid_csr_ = std::max(1, std::min(ntiles_csr_, resident));
+  const int resident_f = mixed_blocks_per_sm() * num_sms_;
+  grid_csc_f_ = std::max(1, std::min(ntiles_csc_f_, resident_f));
+  grid_csr_f_ = std::max(1, std::min(ntiles_csr_f_, resident_f));
+  const int grid_c = std::max(grid_csc_, grid_csc_f_), grid_r = std::max(grid_csr_, grid_csr_f_);
 
   // Minimise-space cost and the norms of src/pdhg/pdhg.cpp:95-111, summed in the
   // reference's order on the host (they are computed once).
@@ -312,6 +439,8 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   csr_s_.allocate_padded(z, kPad, s);
   csc_tiles_.upload(ctiles.data(), ctiles.size(), s);
   csr_tiles_.upload(rtiles.data(), rtiles.size(), s);
+  csc_tiles_f_.upload(ctiles_f.data(), ctiles_f.size(), s);
+  csr_tiles_f_.upload(rtiles_f.data(), rtiles_f.size(), s);
   csc_longs_.upload(clongs.data(), clongs.size(), s);
   csr_longs_.upload(rlongs.data(), rlongs.size(), s);
   cost_.upload(cost.data(), cost.size(), s);
@@ -321,19 +450,20 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   rl_.upload(lp.row_lower, static_cast<size_t>(m), s);
   ru_.upload(lp.row_upper, static_cast<size_t>(m), s);
   for (DeviceArray<double>* a : {&cs_, &ls_, &us_, &dc_, &col_acc_, &x0_, &x1_, &x_sum_, &x_rst_,
-                                 &xu0_, &xu1_, &reduced_, &best_x_, &power_v_, &xbar_, &dx_}) {
+                                 &xu0_, &xu1_, &reduced_, &best_x_, &power_v_}) {
     a->allocate(static_cast<size_t>(n));
   }
+  xd_.allocate(static_cast<size_t>(n));
   for (DeviceArray<double>* a : {&rls_, &rus_, &dr_, &row_acc_, &y0_, &y1_, &y_sum_, &y_rst_,
                                  &yu0_, &yu1_, &best_y_, &power_av_}) {
     a->allocate(static_cast<size_t>(m));
   }
-  const int pgrid = std::max(grid_csc_, grid_csr_) + num_sms_ * 8;
-  part_primal_.allocate(static_cast<size_t>(grid_csc_));
-  part_dual_.allocate(static_cast<size_t>(grid_csr_) * 2);
-  part_rows0_.allocate(static_cast<size_t>(grid_csr_) * kEvalRowSlots);
-  part_cols_.allocate(static_cast<size_t>(grid_csc_ + 1) * kEvalColSlots);
-  part_rows1_.allocate(static_cast<size_t>(grid_csr_) * kEvalRowSlots);
+  const int pgrid = std::max(grid_c, grid_r) + num_sms_ * 8;
+  part_primal_.allocate(static_cast<size_t>(grid_c));
+  part_dual_.allocate(static_cast<size_t>(grid_r) * 2);
+  part_rows0_.allocate(static_cast<size_t>(grid_r) * kEvalRowSlots);
+  part_cols_.allocate(static_cast<size_t>(grid_c + 1) * kEvalColSlots);
+  part_rows1_.allocate(static_cast<size_t>(grid_r) * kEvalRowSlots);
   chunk_primal_.allocate(static_cast<size_t>(nchunks_csc_) + 1);
   chunk_cols_.allocate(2 * static_cast<size_t>(nchunks_csc_) + 2);
   chunk_dual_.allocate(2 * static_cast<size_t>(nchunks_csr_) + 2);
@@ -365,8 +495,7 @@ void Engine::fill_buffers() {
   b.y[1] = y1_.ptr;
   b.x_sum = x_sum_.ptr;
   b.y_sum = y_sum_.ptr;
-  b.xbar = xbar_.ptr;
-  b.dx = dx_.ptr;
+  b.xd = xd_.ptr;
   b.c = cs_.ptr;
   b.l = ls_.ptr;
   b.u = us_.ptr;
@@ -554,18 +683,17 @@ void Engine::build_graphs(int steps) {
   graph_steps_ = steps;
 }
 
-void Engine::run_loop(const sankhya_gb300_params& p, double t0, int* stop_status) {
-  const int steps = p.steps_per_poll > 0 ? p.steps_per_poll : 32;
-  build_graphs(steps);
+void Engine::run_graphs(const sankhya_gb300_params& p, double t0, cudaGraphExec_t* graphs,
+                        Ctl* snapshot, bool forward_log, long long iteration_offset,
+                        int* stop_status) {
   const bool has_time_limit = p.time_limit < 1e300;
   long long logged = 0;
   auto launch = [&](int slot) {
     ++graphs_launched_;
-    SGB_CUDA(cudaGraphLaunch(graph_exec_[slot], stream_));
+    SGB_CUDA(cudaGraphLaunch(graphs[slot], stream_));
     SGB_CUDA(cudaEventRecord(done_event_[slot], stream_));
   };
-  *stop_status = SANKHYA_GB300_ITERATION_LIMIT;
-  // The time limit is checked once before any step, as the reference's loop does.
+  // The time limit is checked before any step, as the reference's loop does.
   if (has_time_limit && (p.time_limit <= 0.0 || now_seconds() - t0 > p.time_limit)) {
     *stop_status = SANKHYA_GB300_TIME_LIMIT;
     return;
@@ -575,14 +703,14 @@ void Engine::run_loop(const sankhya_gb300_params& p, double t0, int* stop_status
   for (long long k = 0;; ++k) {
     const int slot = static_cast<int>(k & 1);
     SGB_CUDA(cudaEventSynchronize(done_event_[slot]));
-    const Ctl& snap = snapshot_[slot];
-    if (p.log != nullptr && snap.log_count > logged) {
+    const Ctl& snap = snapshot[slot];
+    if (forward_log && p.log != nullptr && snap.log_count > logged) {
       const double elapsed = now_seconds() - t0;
-      long long first = std::max(logged, snap.log_count - kLogRing);
+      const long long first = std::max(logged, snap.log_count - kLogRing);
       for (long long r = first; r < snap.log_count; ++r) {
         const EvalRecord& rec = snap.log[r % kLogRing];
-        p.log(p.log_user, rec.iteration, sense_ * rec.primal_objective + offset_, rec.primal,
-              rec.dual, elapsed);
+        p.log(p.log_user, iteration_offset + rec.iteration,
+              sense_ * rec.primal_objective + offset_, rec.primal, rec.dual, elapsed);
       }
       logged = snap.log_count;
     }
@@ -591,7 +719,10 @@ void Engine::run_loop(const sankhya_gb300_params& p, double t0, int* stop_status
       *stop_status = SANKHYA_GB300_TIME_LIMIT;
       break;
     }
-    if (p.interrupt != nullptr && *p.interrupt != 0) {
+    if ((p.interrupt != nullptr && *p.interrupt != 0) ||
+        (p.poll != nullptr &&
+         p.poll(p.poll_user, iteration_offset + snap.iteration,
+                sense_ * snap.best.primal_objective + offset_) != 0)) {
       *stop_status = SANKHYA_GB300_INTERRUPTED;
       break;
     }
@@ -609,34 +740,94 @@ void Engine::final_evaluation() {
   SGB_CUDA(cudaGetLastError());
 }
 
+// Device preconditioning, the spectral-norm estimate and the scaled entry range (the log
+// line of src/pdhg/pdhg.cpp:132-133); the same for both precisions.
+void Engine::setup(const sankhya_gb300_params& p, sankhya_gb300_result* r, double* norm) {
+  cudaStream_t s = stream_;
+  precondition(p.random_seed);
+  *norm = power_iteration(p.random_seed);
+  const int grid = std::min(num_sms_ * 4, std::max(1, static_cast<int>((nnz_ + 255) / 256)));
+  launch_abs_minmax(csc_s_.ptr, static_cast<int>(nnz_), scalars_.ptr,
+                    scalars_.ptr + 2 * grid + 2, tickets_.ptr, s, grid);
+  double mm[2] = {0.0, 0.0};
+  SGB_CUDA(cudaMemcpyAsync(mm, scalars_.ptr + 2 * grid + 2, 2 * sizeof(double),
+                           cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaStreamSynchronize(s));
+  r->scaled_max_abs = mm[0];
+  r->scaled_min_abs = mm[1];
+  r->spectral_norm = *norm;
+}
+
 void Engine::solve(const sankhya_gb300_params& p, sankhya_gb300_result* r) {
   require_loaded();
   const double t0 = now_seconds();
   std::memset(r, 0, sizeof(*r));
-  if (p.precision != SANKHYA_GB300_FP64) {
-    throw EngineError{SANKHYA_GB300_ERROR_OPTION, "this build solves pdhg_precision=fp64 only"};
+  if (p.precision != SANKHYA_GB300_FP64 && p.precision != SANKHYA_GB300_MIXED) {
+    throw EngineError{SANKHYA_GB300_ERROR_OPTION, "pdhg_precision must be fp64 or mixed"};
   }
   SGB_CUDA(cudaSetDevice(device_));
-  cudaStream_t s = stream_;
-  SGB_CUDA(cudaEventRecord(timing_[0], s));
-  const long long launches_before = kernel_launch_count();
+  SGB_CUDA(cudaEventRecord(timing_[0], stream_));
   graphs_launched_ = 0;
-
-  precondition(p.random_seed);
-  const double norm = power_iteration(p.random_seed);
-  {
-    // Scaled entry magnitudes, for the log line of src/pdhg/pdhg.cpp:132-133.
-    const int grid = std::min(num_sms_ * 4, std::max(1, static_cast<int>((nnz_ + 255) / 256)));
-    launch_abs_minmax(csc_s_.ptr, static_cast<int>(nnz_), scalars_.ptr, scalars_.ptr + 2 * grid + 2,
-                      tickets_.ptr, s, grid);
-    double mm[2] = {0.0, 0.0};
-    SGB_CUDA(cudaMemcpyAsync(mm, scalars_.ptr + 2 * grid + 2, 2 * sizeof(double),
-                             cudaMemcpyDeviceToHost, s));
-    SGB_CUDA(cudaStreamSynchronize(s));
-    r->scaled_max_abs = mm[0];
-    r->scaled_min_abs = mm[1];
+  extra_launches_ = 0;
+  if (p.precision == SANKHYA_GB300_MIXED) {
+    solve_mixed(p, r, t0);
+  } else {
+    solve_fp64(p, r, t0);
   }
-  r->spectral_norm = norm;
+  last_precision_ = p.precision;
+  solved_ = true;
+  r->solve_seconds = now_seconds() - t0;
+}
+
+void Engine::report(const sankhya_gb300_params& p, const Ctl& c, bool converged,
+                    long long iterations, long long restarts, int stop_status,
+                    sankhya_gb300_result* r) {
+  const Residuals& f = c.final_residuals;
+  r->final_residuals = sankhya_gb300_residuals{f.primal,          f.dual,           f.gap,
+                                              f.primal_objective, f.dual_objective,
+                                              f.absolute_primal,  f.absolute_dual,
+                                              f.gap_as_verified,  f.complementarity};
+  r->converged = converged;
+  // src/pdhg/pdhg.cpp:506-557: `optimal` only for a point that meets the project standard.
+  const bool verifiable = converged && meets_project_standard(f);
+  std::string message;
+  if (verifiable) {
+    r->status = SANKHYA_GB300_OPTIMAL;
+    message = format(
+        "converged after %lld iterations and %lld restarts; absolute primal %.3e, dual %.3e, "
+        "relative gap %.3e",
+        iterations, restarts, f.absolute_primal, f.absolute_dual, f.gap_as_verified);
+  } else if (converged) {
+    r->status = SANKHYA_GB300_FEASIBLE;
+    message = format(
+        "met the requested relative tolerance %.1e after %lld iterations, but NOT the absolute "
+        "standard this project verifies against (primal %.3e vs 1.0e-07, dual %.3e vs 1.0e-07, "
+        "relative gap %.3e vs 1.0e-09). Reported as feasible, not optimal. %s",
+        p.tolerance, iterations, f.absolute_primal, f.absolute_dual, f.gap_as_verified,
+        p.stop_at_request ? "pdhg_stop_at_request is on, so this is the cheap answer that was "
+                            "asked for; turn it off to run on to the standard"
+                          : "Tighten --option pdhg_tolerance to close it");
+  } else {
+    r->status = stop_status == SANKHYA_GB300_TIME_LIMIT || stop_status == SANKHYA_GB300_INTERRUPTED
+                    ? stop_status
+                    : SANKHYA_GB300_ITERATION_LIMIT;
+    message = format(
+        "stopped at relative primal %.3e, dual %.3e, gap %.3e after %lld iterations and %lld "
+        "restarts (target %.1e)",
+        f.primal, f.dual, f.gap, iterations, restarts, p.tolerance);
+  }
+  r->dual_bound = verifiable ? sense_ * f.dual_objective + offset_
+                             : (sense_ < 0.0 ? std::numeric_limits<double>::infinity()
+                                             : -std::numeric_limits<double>::infinity());
+  r->objective = offset_ + c.model_objective;
+  std::snprintf(r->message, sizeof(r->message), "%s", message.c_str());
+}
+
+void Engine::solve_fp64(const sankhya_gb300_params& p, sankhya_gb300_result* r, double t0) {
+  cudaStream_t s = stream_;
+  const long long launches_before = kernel_launch_count();
+  double norm = 1.0;
+  setup(p, r, &norm);
   init_iterates(p);
 
   Ctl c;
@@ -659,15 +850,9 @@ void Engine::solve(const sankhya_gb300_params& p, sankhya_gb300_result* r) {
 
   int stop_status = SANKHYA_GB300_ITERATION_LIMIT;
   const long long launches_setup = kernel_launch_count() - launches_before;
-  {
-    // Capturing a graph issues no launch; keep the capture out of the count.
-    const int steps = p.steps_per_poll > 0 ? p.steps_per_poll : 32;
-    const long long before_capture = kernel_launch_count();
-    build_graphs(steps);
-    (void)before_capture;
-  }
+  build_graphs(p.steps_per_poll > 0 ? p.steps_per_poll : 32);  // capture launches nothing
   const long long count_after_capture = kernel_launch_count();
-  run_loop(p, t0, &stop_status);
+  run_graphs(p, t0, graph_exec_, snapshot_, true, 0, &stop_status);
   const double t_end_loop = now_seconds();
   final_evaluation();
   SGB_CUDA(cudaEventRecord(timing_[1], s));
@@ -680,55 +865,227 @@ void Engine::solve(const sankhya_gb300_params& p, sankhya_gb300_result* r) {
   launches_ = launches_setup + (kernel_launch_count() - count_after_capture) +
               graphs_launched_ * static_cast<long long>(graph_steps_) * kKernelsPerStep;
   r->kernel_launches = launches_;
-
-  const Residuals& f = c.final_residuals;
-  r->final_residuals = sankhya_gb300_residuals{f.primal,          f.dual,           f.gap,
-                                              f.primal_objective, f.dual_objective,
-                                              f.absolute_primal,  f.absolute_dual,
-                                              f.gap_as_verified,  f.complementarity};
+  if (c.error) {
+    throw EngineError{SANKHYA_GB300_ERROR_DEVICE, "a tile copy did not complete in time"};
+  }
   r->iterations = c.iteration;
   r->attempts = c.attempts;
   r->restarts = c.restarts;
   r->evaluations = c.evaluations;
-  r->converged = c.done == kConverged;
-  const bool converged = c.done == kConverged;
-  const bool verifiable = converged && meets_project_standard(f);
-  std::string message;
-  if (verifiable) {
-    r->status = SANKHYA_GB300_OPTIMAL;
-    message = format(
-        "converged after %lld iterations and %lld restarts; absolute primal %.3e, dual %.3e, "
-        "relative gap %.3e",
-        c.iteration, c.restarts, f.absolute_primal, f.absolute_dual, f.gap_as_verified);
-  } else if (converged) {
-    r->status = SANKHYA_GB300_FEASIBLE;
-    message = format(
-        "met the requested relative tolerance %.1e after %lld iterations, but NOT the absolute "
-        "standard this project verifies against (primal %.3e vs 1.0e-07, dual %.3e vs 1.0e-07, "
-        "relative gap %.3e vs 1.0e-09). Reported as feasible, not optimal. %s",
-        p.tolerance, c.iteration, f.absolute_primal, f.absolute_dual, f.gap_as_verified,
-        p.stop_at_request ? "pdhg_stop_at_request is on, so this is the cheap answer that was "
-                            "asked for; turn it off to run on to the standard"
-                          : "Tighten --option pdhg_tolerance to close it");
-  } else {
-    r->status = stop_status == SANKHYA_GB300_TIME_LIMIT || stop_status == SANKHYA_GB300_INTERRUPTED
-                    ? stop_status
-                    : SANKHYA_GB300_ITERATION_LIMIT;
-    message = format(
-        "stopped at relative primal %.3e, dual %.3e, gap %.3e after %lld iterations and %lld "
-        "restarts (target %.1e)",
-        f.primal, f.dual, f.gap, c.iteration, c.restarts, p.tolerance);
+  report(p, c, c.done == kConverged, c.iteration, c.restarts, stop_status, r);
+}
+
+// The mixed method (mixed.cuh): FP32 inner PDHG on correction problems, FP64 anchor updates,
+// and the reference's exact FP64 evaluation after every round.
+void Engine::solve_mixed(const sankhya_gb300_params& p, sankhya_gb300_result* r, double t0) {
+  cudaStream_t s = stream_;
+  allocate_mixed();
+  const long long launches_before = kernel_launch_count();
+  double norm = 1.0;
+  setup(p, r, &norm);
+  // FP32 copies of the scaled values; the FP64 anchor starts at proj(0), y = 0.
+  launch_to_float(csc_s_.ptr, csc_f_.ptr, nnz_, s);
+  launch_to_float(csr_s_.ptr, csr_f_.ptr, nnz_, s);
+  launch_to_float(cs_.ptr, csf_.ptr, n_, s);
+  extra_launches_ += 3;
+  launch_project_start(n_, ls_.ptr, us_.ptr, anchor_x_.ptr, s);
+  launch_fill(anchor_y_.ptr, m_, 0.0, s);
+  extra_launches_ += 2;
+  {
+    // The scaled problem's norms, for the inner loop's relative residuals.
+    std::vector<double> h(static_cast<size_t>(std::max(m_, n_)));
+    double bs = 0.0, cs2 = 0.0;
+    std::vector<double> rl(static_cast<size_t>(m_)), ru(static_cast<size_t>(m_));
+    if (m_ > 0) {
+      SGB_CUDA(cudaMemcpyAsync(rl.data(), rls_.ptr, m_ * sizeof(double), cudaMemcpyDeviceToHost, s));
+      SGB_CUDA(cudaMemcpyAsync(ru.data(), rus_.ptr, m_ * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    if (n_ > 0) {
+      SGB_CUDA(cudaMemcpyAsync(h.data(), cs_.ptr, n_ * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    SGB_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < m_; ++i) {
+      const double b = !std::isinf(rl[i]) ? rl[i] : (!std::isinf(ru[i]) ? ru[i] : 0.0);
+      bs += b * b;
+    }
+    for (int j = 0; j < n_; ++j) cs2 += h[j] * h[j];
+    bound_norm_s_ = std::sqrt(bs);
+    cost_norm_s_ = std::sqrt(cs2);
   }
-  if (verifiable) {
-    r->dual_bound = sense_ * f.dual_objective + offset_;
-  } else {
-    r->dual_bound = sense_ < 0.0 ? std::numeric_limits<double>::infinity()
-                                 : -std::numeric_limits<double>::infinity();
+  const double t_loop = now_seconds();
+  r->setup_seconds = t_loop - t0;
+  const long long launches_setup = kernel_launch_count() - launches_before;
+
+  const int steps = p.steps_per_poll > 0 ? p.steps_per_poll : 32;
+  build_mixed_graphs(steps);
+  const long long limit = p.iteration_limit < 0 ? 1000000 : p.iteration_limit;
+  const double inf = std::numeric_limits<double>::infinity();
+  const int rgrid = std::min(num_sms_ * 4, std::max(1, (std::max(m_, n_) + 255) / 256));
+  RoundBuffers rb{};
+  rb.ctl = ctl_mixed_.ptr;
+  rb.m = m_;
+  rb.n = n_;
+  rb.cs = cs_.ptr;
+  rb.ls = ls_.ptr;
+  rb.us = us_.ptr;
+  rb.rls = rls_.ptr;
+  rb.rus = rus_.ptr;
+  rb.dr = dr_.ptr;
+  rb.dc = dc_.ptr;
+  rb.xbar = anchor_x_.ptr;
+  rb.ybar = anchor_y_.ptr;
+  rb.ax = ax64_.ptr;
+  rb.aty = aty64_.ptr;
+  rb.cf = cf_.ptr;
+  rb.lf = lf_.ptr;
+  rb.uf = uf_.ptr;
+  rb.gu = gu_.ptr;
+  rb.gl = gl_.ptr;
+  rb.yhat = yhat_.ptr;
+  rb.u_src = ubest_.ptr;
+  rb.v_src = vbest_.ptr;
+  rb.best_x = best_x_.ptr;
+  rb.best_y = best_y_.ptr;
+  rb.part = scalars_.ptr;
+  rb.out = power_norms_.ptr;
+  rb.ticket = tickets_.ptr + 2;
+  rb.grid = rgrid;
+
+  // FP64 control block for the exact evaluations.
+  Ctl fc;
+  std::memset(&fc, 0, sizeof(fc));
+  fc.final_mode = 1;
+  SGB_CUDA(cudaMemcpyAsync(ctl_.ptr, &fc, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+
+  // The inner loop's state carries across rounds: a round is only a change of variables, so
+  // the step size, primal weight, restart bookkeeping and the GLOBAL iteration count go on
+  // as one PDHG run. A round ends at each restart the inner loop decides (the anchor moves to
+  // the current iterate -- the restart point -- and the correction is rescaled to the new
+  // residuals), or when the inner KKT estimate meets the round's target (the anchor moves to
+  // the better candidate and is checked exactly), or at a limit.
+  Ctl c;
+  std::memset(&c, 0, sizeof(c));
+  c.eta = norm > 0.0 ? 1.0 / norm : 1.0;
+  c.omega = 1.0;
+  c.spectral_norm = norm;
+  c.eta_ceiling = 1.0e3 / std::max(norm, 1e-12);
+  c.restart_kkt = inf;
+  c.tolerance = p.tolerance;
+  c.iteration_limit = limit;
+  c.use_restarts = p.restart != 0;
+  c.inner_mode = 1;
+  c.bound_norm_s = bound_norm_s_;
+  c.cost_norm_s = cost_norm_s_;
+  double dp = 1.0, dd = 1.0;
+  double target = 0.5 * p.tolerance;
+  long long rounds = 0;
+  int stop_status = SANKHYA_GB300_ITERATION_LIMIT;
+  bool converged = false;
+  Ctl exact_ctl;
+  std::memset(&exact_ctl, 0, sizeof(exact_ctl));
+  const auto stop_test = [&](const Residuals& f) {
+    return p.stop_rule == SANKHYA_GB300_STOP_RELATIVE
+               ? worst(f) <= p.tolerance
+               : meets_request(f, p.tolerance) &&
+                     (p.stop_at_request != 0 || meets_project_standard(f));
+  };
+  for (;; ++rounds) {
+    // Anchor residuals in FP64, then the scales of this round's correction problem.
+    launch_spmv(step_.csr, anchor_x_.ptr, ax64_.ptr, chunk_spmv_.ptr, tickets_.ptr + 1, s, grid_csr_);
+    launch_spmv(step_.csc, anchor_y_.ptr, aty64_.ptr, chunk_spmv_.ptr, tickets_.ptr + 1, s, grid_csc_);
+    launch_round_measure(rb, s);
+    extra_launches_ += 3;
+    double out[3];
+    SGB_CUDA(cudaMemcpyAsync(out, rb.out, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    SGB_CUDA(cudaStreamSynchronize(s));
+    // 1 / residual, never below 1, at most 1e3 times the previous scale and 1e15 overall: an
+    // anchor whose residual is exactly zero must not push the FP32 data out of range.
+    const auto scale = [&](double residual, double prev) {
+      if (rounds == 0) return 1.0;
+      const double want = 1.0 / std::max(residual, 1e-300);
+      return std::max(1.0, std::min({want, prev * 1e3, 1e15}));
+    };
+    const double dp_new = scale(out[0], dp);
+    const double dd_new = scale(out[1], dd);
+    // The primal weight lives in correction units: omega_c = omega (Dd / Dp).
+    c.omega = std::min(std::max(c.omega * (dd_new / dd) / (dp_new / dp), 1e-10), 1e10);
+    dp = dp_new;
+    dd = dd_new;
+    c.dp = dp;
+    c.dd = dd;
+    c.pobj0 = out[2];
+    c.round_target = target;
+    c.cur = 0;
+    c.averaged = 0;
+    c.pending_add = 0;
+    c.done = kRunning;
+    c.eval_now = c.copy_best = c.do_restart = 0;
+    c.best.primal = c.best.dual = c.best.gap = inf;
+    std::memset(c.ticket, 0, sizeof(c.ticket));
+    SGB_CUDA(cudaMemcpyAsync(ctl_mixed_.ptr, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+    launch_round_build(rb, s);
+    for (DeviceArray<float>* a : {&u0f_, &usumf_, &urstf_, &ubest_}) launch_fill_float(a->ptr, n_, 0.0f, s);
+    for (DeviceArray<float>* a : {&v0f_, &vsumf_, &vrstf_, &vbest_}) launch_fill_float(a->ptr, m_, 0.0f, s);
+    extra_launches_ += 9;
+    SGB_CUDA(cudaGetLastError());
+    int round_stop = SANKHYA_GB300_ITERATION_LIMIT;
+    run_graphs(p, t0, mgraph_exec_, snapshot_mixed_, false, 0, &round_stop);
+    SGB_CUDA(cudaMemcpyAsync(&c, ctl_mixed_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    SGB_CUDA(cudaStreamSynchronize(s));
+    if (c.error) {
+      throw EngineError{SANKHYA_GB300_ERROR_DEVICE, "a tile copy did not complete in time"};
+    }
+    // A restart moves the anchor to the current iterate (the restart point); otherwise to
+    // the better of the last evaluated candidates.
+    if (c.done == kRestartRound) {
+      rb.u_src = c.cur ? u1f_.ptr : u0f_.ptr;
+      rb.v_src = c.cur ? v1f_.ptr : v0f_.ptr;
+    } else {
+      rb.u_src = ubest_.ptr;
+      rb.v_src = vbest_.ptr;
+    }
+    launch_round_update(rb, s);
+    final_evaluation();
+    extra_launches_ += 5;
+    SGB_CUDA(cudaMemcpyAsync(&exact_ctl, ctl_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+    SGB_CUDA(cudaStreamSynchronize(s));
+    const Residuals& f = exact_ctl.final_residuals;
+    if (p.log != nullptr) {
+      p.log(p.log_user, c.iteration, sense_ * f.primal_objective + offset_, f.primal, f.dual,
+            now_seconds() - t0);
+    }
+    if (stop_test(f)) {
+      converged = true;
+      break;
+    }
+    if (round_stop != SANKHYA_GB300_ITERATION_LIMIT) {
+      stop_status = round_stop;
+      break;
+    }
+    if (c.done == kIterationLimit || c.iteration >= limit) break;
+    if (c.done == kConverged) {
+      // The estimate met the target but the exact check did not: tighten the estimate's bar.
+      target *= 0.3;
+    }
   }
-  r->objective = offset_ + c.model_objective;
-  std::snprintf(r->message, sizeof(r->message), "%s", message.c_str());
-  solved_ = true;
-  r->solve_seconds = now_seconds() - t0;
+  const long long total_it = c.iteration, total_att = c.attempts, restarts = c.restarts;
+  const long long evals = c.evaluations;
+  SGB_CUDA(cudaEventRecord(timing_[1], s));
+  SGB_CUDA(cudaStreamSynchronize(s));
+  const double t_end_loop = now_seconds();
+  r->loop_seconds = t_end_loop - t_loop;
+  float device_ms = 0.0f;
+  SGB_CUDA(cudaEventElapsedTime(&device_ms, timing_[0], timing_[1]));
+  r->device_seconds = 1e-3 * device_ms;
+  launches_ = launches_setup + extra_launches_ +
+              graphs_launched_ * static_cast<long long>(mgraph_steps_) * kKernelsPerStep;
+  r->kernel_launches = launches_;
+  r->iterations = total_it;
+  r->attempts = total_att;
+  r->restarts = restarts;
+  r->evaluations = evals;
+  r->refinements = rounds + 1;
+  report(p, exact_ctl, converged, total_it, restarts, stop_status, r);
 }
 
 void Engine::time_kernels(int reps, double* ms) {
@@ -736,21 +1093,25 @@ void Engine::time_kernels(int reps, double* ms) {
   if (!solved_) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no solve has run"};
   SGB_CUDA(cudaSetDevice(device_));
   cudaStream_t s = stream_;
+  // The kernels of the last solve's method, on its own control block (the FP32 pair for a
+  // mixed solve, the FP64 pair otherwise).
+  const bool mixed = last_precision_ == SANKHYA_GB300_MIXED;
+  Ctl* ctl = mixed ? ctl_mixed_.ptr : ctl_.ptr;
   Ctl saved;
-  SGB_CUDA(cudaMemcpyAsync(&saved, ctl_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaMemcpyAsync(&saved, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, s));
   SGB_CUDA(cudaStreamSynchronize(s));
   Ctl run = saved;
   run.done = kRunning;
   run.final_mode = 0;
   run.iteration_limit = std::numeric_limits<long long>::max();
-  SGB_CUDA(cudaMemcpyAsync(ctl_.ptr, &run, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+  SGB_CUDA(cudaMemcpyAsync(ctl, &run, sizeof(Ctl), cudaMemcpyHostToDevice, s));
   std::vector<cudaEvent_t> ev(3 * static_cast<size_t>(reps));
   for (auto& e : ev) SGB_CUDA(cudaEventCreate(&e));
   for (int r = 0; r < reps; ++r) {
     SGB_CUDA(cudaEventRecord(ev[3 * r], s));
-    launch_primal_pass(step_, s);
+    if (mixed) launch_mixed_primal(mixed_, s); else launch_primal_pass(step_, s);
     SGB_CUDA(cudaEventRecord(ev[3 * r + 1], s));
-    launch_dual_pass(step_, s);
+    if (mixed) launch_mixed_dual(mixed_, s); else launch_dual_pass(step_, s);
     SGB_CUDA(cudaEventRecord(ev[3 * r + 2], s));
   }
   SGB_CUDA(cudaGetLastError());
@@ -764,7 +1125,7 @@ void Engine::time_kernels(int reps, double* ms) {
     dual += b;
   }
   for (auto& e : ev) cudaEventDestroy(e);
-  SGB_CUDA(cudaMemcpyAsync(ctl_.ptr, &saved, sizeof(Ctl), cudaMemcpyHostToDevice, s));
+  SGB_CUDA(cudaMemcpyAsync(ctl, &saved, sizeof(Ctl), cudaMemcpyHostToDevice, s));
   SGB_CUDA(cudaStreamSynchronize(s));
   ms[0] = primal / reps;
   ms[1] = dual / reps;

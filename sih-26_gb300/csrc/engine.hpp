@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "kernels.cuh"
+#include "mixed.cuh"
 #include "sankhya_gb300.h"
 
 namespace sgb {
@@ -58,10 +59,21 @@ class Engine {
   double power_iteration(long long seed);
   void init_iterates(const sankhya_gb300_params& p);
   void build_graphs(int steps);
+  void build_mixed_graphs(int steps);
   void destroy_graphs();
   void fill_buffers();
-  void run_loop(const sankhya_gb300_params& p, double t0, int* stop_status);
+  void fill_mixed_buffers();
+  void allocate_mixed();
+  // Runs CUDA graphs of `graph_steps_` steps until the control block behind `snapshot` says
+  // done, the time limit passes or the interrupt flag is raised.
+  void run_graphs(const sankhya_gb300_params& p, double t0, cudaGraphExec_t* graphs,
+                  Ctl* snapshot, bool forward_log, long long iteration_offset, int* stop_status);
   void final_evaluation();
+  void setup(const sankhya_gb300_params& p, sankhya_gb300_result* r, double* norm);
+  void solve_fp64(const sankhya_gb300_params& p, sankhya_gb300_result* r, double t0);
+  void solve_mixed(const sankhya_gb300_params& p, sankhya_gb300_result* r, double t0);
+  void report(const sankhya_gb300_params& p, const Ctl& c, bool converged, long long iterations,
+              long long restarts, int stop_status, sankhya_gb300_result* r);
 
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
@@ -80,6 +92,11 @@ class Engine {
   int nchunks_csr_ = 0, nchunks_csc_ = 0;
   int lanes_csr_ = 1, lanes_csc_ = 1;
   int grid_csr_ = 1, grid_csc_ = 1;
+  // The FP32 kernels' tile layout (same chunks of long rows, `lanes` threads per row).
+  int ntiles_csr_f_ = 0, ntiles_csc_f_ = 0;
+  int lanes_csr_f_ = 1, lanes_csc_f_ = 1;
+  int grid_csr_f_ = 1, grid_csc_f_ = 1;
+  DeviceArray<Tile> csc_tiles_f_, csr_tiles_f_;
 
   // Pattern (shared by scaled and unscaled values).
   DeviceArray<int> csc_ptr_, csc_idx_, csr_ptr_, csr_idx_;
@@ -93,7 +110,8 @@ class Engine {
   DeviceArray<double> cs_, ls_, us_, rls_, rus_, dr_, dc_, row_acc_, col_acc_;
   // Iterates.
   DeviceArray<double> x0_, x1_, y0_, y1_, x_sum_, y_sum_, x_rst_, y_rst_;
-  DeviceArray<double> xu0_, xu1_, yu0_, yu1_, reduced_, best_x_, best_y_, xbar_, dx_;
+  DeviceArray<double> xu0_, xu1_, yu0_, yu1_, reduced_, best_x_, best_y_;
+  DeviceArray<double2> xd_;  // (2x' - x, x' - x) per column
   // Reductions.
   DeviceArray<double> part_primal_, part_dual_, part_rows0_, part_cols_, part_rows1_;
   DeviceArray<double> chunk_primal_, chunk_dual_, chunk_cols_, chunk_rows_, chunk_spmv_;
@@ -111,6 +129,23 @@ class Engine {
 
   StepBuffers step_{};
   EvalBuffers eval_{};
+
+  // Mixed method (allocated on its first solve).
+  int last_precision_ = SANKHYA_GB300_FP64;
+  bool mixed_ready_ = false;
+  MixedBuffers mixed_{};
+  DeviceArray<float> csc_f_, csr_f_;
+  DeviceArray<float> u0f_, u1f_, v0f_, v1f_, usumf_, vsumf_, urstf_, vrstf_;
+  DeviceArray<float> cf_, lf_, uf_, gu_, gl_, yhat_, uc0_, uc1_, vc0_, vc1_, ubest_, vbest_;
+  DeviceArray<float> csf_;   // scaled cost in FP32
+  DeviceArray<float2> udf_;  // (2u' - u, u' - u) per column
+  DeviceArray<double> anchor_x_, anchor_y_, ax64_, aty64_;
+  DeviceArray<Ctl> ctl_mixed_;
+  Ctl* snapshot_mixed_ = nullptr;  // pinned host, two slots
+  cudaGraphExec_t mgraph_exec_[2] = {nullptr, nullptr};
+  int mgraph_steps_ = 0;
+  double bound_norm_s_ = 0.0, cost_norm_s_ = 0.0;  // scaled problem norms
+  long long extra_launches_ = 0;
 };
 
 size_t estimate_memory(long long rows, long long cols, long long nnz, int precision);

@@ -39,7 +39,11 @@ __host__ __device__ inline bool meets_project_standard(const Residuals& r) {
          r.complementarity <= 1e-6;
 }
 
-enum DoneCode : int { kRunning = 0, kConverged = 1, kIterationLimit = 2, kFault = 3 };
+// kRestartRound: the mixed method's inner loop decided a restart, which ends a refinement
+// round (the anchor moves to the current iterate and the correction is rescaled).
+enum DoneCode : int {
+  kRunning = 0, kConverged = 1, kIterationLimit = 2, kFault = 3, kRestartRound = 4
+};
 
 constexpr int kLogRing = 64;
 
@@ -69,9 +73,13 @@ struct Ctl {
   int final_mode;   // the evaluation kernels evaluate (best_x, best_y) only
   int stop_rule;    // 0: the reference's stopping test; 1: relative KKT only
   int error;        // a bounded wait gave up (nonzero: the host stops with an error)
-  int pad0;
+  int inner_mode;   // the mixed method's inner loop: a restart ends the round
   double movement, interaction;  // of the last attempted step
   double mv_primal;              // primal half of the movement, from k_primal's last block
+  // Mixed method, one refinement round (the FP32 inner loop reads these): the primal and
+  // dual scale factors of the correction problem, the scaled problem's bound and cost
+  // norms, the scaled objective at the round's anchor, and the round's KKT target.
+  double dp, dd, bound_norm_s, cost_norm_s, pobj0, round_target;
   Residuals best;
   Residuals final_residuals;
   double model_objective;  // sum of the original-sense costs times best_x (final mode)
@@ -90,8 +98,9 @@ struct StepBuffers {
   double* y[2];
   double* x_sum;
   double* y_sum;
-  double* xbar;  // 2 x' - x of the step, written by k_primal, gathered by k_dual
-  double* dx;    // x' - x
+  // (2 x' - x, x' - x) of the step, written by k_primal and gathered by k_dual as ONE
+  // 16-byte element per entry: a scattered gather costs a cache sector whatever it reads.
+  double2* xd;
   const double *c, *l, *u, *rl, *ru;  // scaled problem
   double* part_primal;   // [grid_primal]
   double* part_dual;     // [grid_dual * 2]

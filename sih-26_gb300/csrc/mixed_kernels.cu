@@ -1,0 +1,562 @@
+// mixed_kernels.cu -- the FP32 inner loop and the FP64 refinement rounds (see mixed.cuh).
+//
+// The step kernels mirror k_primal / k_dual with FP32 values, iterates and FP32-accumulated
+// products; the movement and interaction partials are promoted to FP64 at the block level,
+// and the step-size decision, restarts and primal weight (decisions.cuh) are FP64. In FP32
+// the row pass gathers u and u' and forms 2u' - u and u' - u per entry itself: the ALU cost
+// is negligible and no extra vector has to be written, which keeps the pass HBM-bound.
+#include "common.cuh"
+#include "decisions.cuh"
+#include "kernels.cuh"
+#include "mixed.cuh"
+#include "tiles.cuh"
+
+namespace sgb {
+
+namespace {
+
+constexpr int kScratch = 16 * (kTileThreads / 32);
+constexpr int kSmemF = tile_smem_bytes<float>();
+
+__device__ __forceinline__ void raise_error(Ctl* c) {
+  c->error = 1;
+  c->done = kFault;
+}
+
+__device__ __forceinline__ int grid_stride_begin() {
+  return blockIdx.x * blockDim.x + threadIdx.x;
+}
+
+// ---- Inner step ----------------------------------------------------------------------------
+__global__ void __launch_bounds__(kTileThreads) k_primal_f(MixedBuffers b) {
+  extern __shared__ __align__(16) unsigned char dsmem[];
+  __shared__ double scratch[kScratch];
+  Ctl* ctl = b.ctl;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl->eval_now = 0;
+    ctl->copy_best = 0;
+    ctl->do_restart = 0;
+  }
+  if (ctl->done != kRunning) return;
+  if (ctl->iteration >= ctl->iteration_limit) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->done = kIterationLimit;
+    return;
+  }
+  const int cur = ctl->cur;
+  const float* __restrict__ u = b.u[cur];
+  float* __restrict__ un = b.u[cur ^ 1];
+  const float* __restrict__ v = b.v[cur];
+  const double omega = ctl->omega;
+  const float tau = static_cast<float>(ctl->eta / omega);
+  const bool add = ctl->pending_add != 0;
+  float mvf = 0.0f;
+  auto gather = [&](int row, float a, float* acc) { acc[0] = fmaf(a, __ldg(v + row), acc[0]); };
+  auto epi = [&](int j, const float* s) {
+    const float uj = u[j];
+    if (add) b.u_sum[j] += uj;
+    const float g = b.cf[j] + s[0];
+    const float unj = clamp_box(fmaf(-tau, g, uj), b.lf[j], b.uf[j]);
+    un[j] = unj;
+    const float d = unj - uj;
+    b.ud[j] = make_float2(fmaf(2.0f, unj, -uj), d);
+    mvf = fmaf(d, d, mvf);
+  };
+  TilePipe<float> pipe;
+  pipe.setup(dsmem);
+  if (!run_tiles<1, float>(pipe, b.csc, b.chunk_primal, scratch, gather, epi) &&
+      threadIdx.x == 0) {
+    raise_error(ctl);
+  }
+  double mv[1] = {static_cast<double>(mvf)};
+  if (!arrive_last<1>(mv, scratch, b.part_primal, &ctl->ticket[kTicketPrimal])) return;
+  mvf = 0.0f;
+  run_long_rows<1, float>(b.csc, b.chunk_primal, epi);
+  mv[0] = static_cast<double>(mvf);
+  double longs[1], total[1];
+  block_sum<1>(mv, scratch, longs);
+  sum_partials<1>(b.part_primal, gridDim.x, scratch, total);
+  if (threadIdx.x == 0) {
+    ctl->mv_primal = 0.5 * omega * (total[0] + longs[0]);
+    ctl->ticket[kTicketPrimal] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_dual_f(MixedBuffers b) {
+  extern __shared__ __align__(16) unsigned char dsmem[];
+  __shared__ double scratch[kScratch];
+  Ctl* ctl = b.ctl;
+  if (ctl->done != kRunning) return;
+  const int cur = ctl->cur;
+  const float2* __restrict__ ud = b.ud;
+  const float* __restrict__ v = b.v[cur];
+  float* __restrict__ vn = b.v[cur ^ 1];
+  const double omega = ctl->omega;
+  const float sigma = static_cast<float>(ctl->eta * omega);
+  const float inv_sigma = 1.0f / sigma;
+  const bool add = ctl->pending_add != 0;
+  float a0 = 0.0f, a1 = 0.0f;  // sum dv^2, sum dv (A du)
+  auto gather = [&](int col, float a, float* acc) {
+    const float2 p = __ldg(ud + col);
+    acc[0] = fmaf(a, p.x, acc[0]);
+    acc[1] = fmaf(a, p.y, acc[1]);
+  };
+  auto epi = [&](int i, const float* s) {
+    const float vi = v[i];
+    if (add) b.v_sum[i] += vi;
+    const float gu = b.gu[i], gl = b.gl[i];
+    float vni;
+    if (gu == gl) {
+      vni = fmaf(sigma, gu + s[0], vi);
+    } else {
+      const float t = fmaf(b.yhat[i] + vi, inv_sigma, s[0]);
+      if (t + gu > 0.0f) {
+        vni = fmaf(sigma, gu + s[0], vi);
+      } else if (t + gl < 0.0f) {
+        vni = fmaf(sigma, gl + s[0], vi);
+      } else {
+        vni = -b.yhat[i];
+      }
+    }
+    vn[i] = vni;
+    const float d = vni - vi;
+    a0 = fmaf(d, d, a0);
+    a1 = fmaf(d, s[1], a1);
+  };
+  TilePipe<float> pipe;
+  pipe.setup(dsmem);
+  if (!run_tiles<2, float>(pipe, b.csr, b.chunk_dual, scratch, gather, epi) &&
+      threadIdx.x == 0) {
+    raise_error(ctl);
+  }
+  double acc2[2] = {static_cast<double>(a0), static_cast<double>(a1)};
+  if (!arrive_last<2>(acc2, scratch, b.part_dual, &ctl->ticket[kTicketDual])) return;
+  a0 = a1 = 0.0f;
+  run_long_rows<2, float>(b.csr, b.chunk_dual, epi);
+  acc2[0] = a0;
+  acc2[1] = a1;
+  double longs[2], total[2];
+  block_sum<2>(acc2, scratch, longs);
+  sum_partials<2>(b.part_dual, gridDim.x, scratch, total);
+  if (threadIdx.x == 0) {
+    ctl->ticket[kTicketDual] = 0;
+    if (ctl->done == kRunning) {
+      const double movement = ctl->mv_primal + (0.5 * (total[0] + longs[0])) / omega;
+      step_decision(ctl, movement, fabs(total[1] + longs[1]));
+    }
+  }
+}
+
+// ---- Inner evaluation (correction form, FP64 accumulation) ---------------------------------
+__device__ __forceinline__ bool inner_eval_active(const Ctl* c) {
+  return c->eval_now != 0 && c->done == kRunning;
+}
+
+// Rows, no matrix: the dual candidates (current, average), the row half of the dual
+// violation (a multiplier on a row side that does not exist), |v - v_restart|^2.
+__global__ void __launch_bounds__(kTileThreads) k_evalf_rows0(MixedBuffers b) {
+  __shared__ double scratch[kScratch];
+  const Ctl* c = b.ctl;
+  if (!inner_eval_active(c)) return;
+  const int cur = c->cur;
+  const bool avg = c->averaged > 0;
+  const bool pend = c->pending_add != 0;
+  const float count = static_cast<float>(c->averaged);
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int i = grid_stride_begin(); i < b.m; i += gridDim.x * blockDim.x) {
+    const float vcur = b.v[cur][i];
+    float cand[2] = {vcur, 0.0f};
+    if (avg) cand[1] = (pend ? b.v_sum[i] + vcur : b.v_sum[i]) / count;
+    const float gu = b.gu[i], gl = b.gl[i], yh = b.yhat[i];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (q == 1 && !avg) break;
+      b.vc[q][i] = cand[q];
+      const double yc = static_cast<double>(yh) + static_cast<double>(cand[q]);
+      if ((yc > 0.0 && isinf(gu)) || (yc < 0.0 && isinf(gl))) acc[q] += yc * yc;
+    }
+    const double d = static_cast<double>(vcur) - static_cast<double>(b.v_rst[i]);
+    acc[2] += d * d;
+  }
+  double out[3];
+  block_sum<3>(acc, scratch, out);
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < 3; ++q) b.part_rows0[blockIdx.x * kEvalRowSlots + q] = out[q];
+  }
+}
+
+// Columns over the FP32 CSC: d_c = cf + A^T v_c of both candidates, the column dual
+// violation, the column half of the gap (sum d (x - bound) in correction units), |u-u_rst|^2.
+__global__ void __launch_bounds__(kTileThreads) k_evalf_cols(MixedBuffers b) {
+  extern __shared__ __align__(16) unsigned char dsmem[];
+  __shared__ double scratch[kScratch];
+  Ctl* c = b.ctl;
+  if (!inner_eval_active(c)) return;
+  const int cur = c->cur;
+  const bool avg = c->averaged > 0;
+  const bool pend = c->pending_add != 0;
+  const float count = static_cast<float>(c->averaged);
+  const float* __restrict__ vc0 = b.vc[0];
+  const float* __restrict__ vc1 = b.vc[1];
+  // dviol0, gapc0, dviol1, gapc1, du^2, c'u0, c'u1
+  double acc[7] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  auto gather = [&](int row, float a, float* s) {
+    s[0] = fmaf(a, vc0[row], s[0]);
+    if (avg) s[1] = fmaf(a, vc1[row], s[1]);
+  };
+  auto epi = [&](int j, const float* s) {
+    const float ucur = b.u[cur][j];
+    float cand[2] = {ucur, 0.0f};
+    if (avg) cand[1] = (pend ? b.u_sum[j] + ucur : b.u_sum[j]) / count;
+    const float lf = b.lf[j], uf = b.uf[j], cf = b.cf[j];
+    const double cj = b.cs[j];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (q == 1 && !avg) break;
+      b.uc[q][j] = cand[q];
+      const double d = static_cast<double>(cf) + static_cast<double>(s[q]);
+      const double uq = static_cast<double>(cand[q]);
+      if (d > 0.0) {
+        if (isinf(lf)) acc[2 * q] += d * d; else acc[2 * q + 1] += d * (uq - lf);
+      } else if (d < 0.0) {
+        if (isinf(uf)) acc[2 * q] += d * d; else acc[2 * q + 1] += d * (uq - uf);
+      }
+      acc[5 + q] += cj * uq;
+    }
+    const double d = static_cast<double>(ucur) - static_cast<double>(b.u_rst[j]);
+    acc[4] += d * d;
+  };
+  TilePipe<float> pipe;
+  pipe.setup(dsmem);
+  if (!run_tiles<2, float>(pipe, b.csc, b.chunk_cols, scratch, gather, epi) &&
+      threadIdx.x == 0) {
+    raise_error(c);
+  }
+  double out[7];
+  block_sum<7>(acc, scratch, out);
+  __shared__ int s_last;
+  if (threadIdx.x == 0) {
+    double* p = b.part_cols + blockIdx.x * kEvalColSlots;
+    for (int q = 0; q < 7; ++q) p[q] = out[q];
+    __threadfence();
+    s_last = atomicAdd(&c->ticket[kTicketEvalCols], 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int q = 0; q < 7; ++q) acc[q] = 0.0;
+  run_long_rows<2, float>(b.csc, b.chunk_cols, epi);
+  block_sum<7>(acc, scratch, out);
+  if (threadIdx.x == 0) {
+    double* p = b.part_cols + b.grid_primal * kEvalColSlots;
+    for (int q = 0; q < 7; ++q) p[q] = out[q];
+    c->ticket[kTicketEvalCols] = 0;
+  }
+}
+
+__device__ bool round_stop_test(const Ctl* c, const Residuals& r) {
+  return worst(r) <= c->round_target;
+}
+
+// Rows over the FP32 CSR: A u_c, the primal violation and the row half of the gap; the last
+// block assembles the scaled-problem KKT of xbar + u/dp, ybar + v/dd and decides.
+__global__ void __launch_bounds__(kTileThreads) k_evalf_rows1(MixedBuffers b) {
+  extern __shared__ __align__(16) unsigned char dsmem[];
+  __shared__ double scratch[kScratch];
+  Ctl* c = b.ctl;
+  if (!inner_eval_active(c)) return;
+  const bool avg = c->averaged > 0;
+  const float* __restrict__ uc0 = b.uc[0];
+  const float* __restrict__ uc1 = b.uc[1];
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};  // pviol0, gapr0, pviol1, gapr1
+  auto gather = [&](int col, float a, float* s) {
+    s[0] = fmaf(a, uc0[col], s[0]);
+    if (avg) s[1] = fmaf(a, uc1[col], s[1]);
+  };
+  auto epi = [&](int i, const float* s) {
+    const double gu = b.gu[i], gl = b.gl[i], yh = b.yhat[i];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (q == 1 && !avg) break;
+      const double a = s[q];
+      const double eu = gu + a;     // dp ((A x)_i - ru_i)
+      const double el = -(gl + a);  // dp (rl_i - (A x)_i)
+      const double viol = dmax(0.0, dmax(eu, el));
+      acc[2 * q] += viol * viol;
+      const double yc = yh + static_cast<double>(b.vc[q][i]);
+      if (yc > 0.0 && !isinf(gu)) acc[2 * q + 1] += yc * eu;
+      else if (yc < 0.0 && !isinf(gl)) acc[2 * q + 1] += yc * (gl + a);
+    }
+  };
+  TilePipe<float> pipe;
+  pipe.setup(dsmem);
+  if (!run_tiles<2, float>(pipe, b.csr, b.chunk_rows, scratch, gather, epi) &&
+      threadIdx.x == 0) {
+    raise_error(c);
+  }
+  double sums[4];
+  block_sum<4>(acc, scratch, sums);
+  __shared__ int s_last;
+  if (threadIdx.x == 0) {
+    double* p = b.part_rows1 + blockIdx.x * kEvalRowSlots;
+    for (int q = 0; q < 4; ++q) p[q] = sums[q];
+    __threadfence();
+    s_last = atomicAdd(&c->ticket[kTicketEvalRows], 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int q = 0; q < 4; ++q) acc[q] = 0.0;
+  run_long_rows<2, float>(b.csr, b.chunk_rows, epi);
+  double s[14];
+  for (int q = 0; q < 4; ++q) s[q] = acc[q];
+  for (int q = 4; q < 14; ++q) s[q] = 0.0;
+  for (int blk = threadIdx.x; blk < b.grid_dual; blk += blockDim.x) {
+    for (int q = 0; q < 4; ++q) s[q] += __ldcg(b.part_rows1 + blk * kEvalRowSlots + q);
+    for (int q = 0; q < 3; ++q) s[4 + q] += __ldcg(b.part_rows0 + blk * kEvalRowSlots + q);
+  }
+  for (int blk = threadIdx.x; blk <= b.grid_primal; blk += blockDim.x) {
+    for (int q = 0; q < 7; ++q) s[7 + q] += __ldcg(b.part_cols + blk * kEvalColSlots + q);
+  }
+  double t[14];
+  block_sum<14>(s, scratch, t);
+  if (threadIdx.x != 0) return;
+  c->ticket[kTicketEvalRows] = 0;
+  // t: [0] pviol0 [1] gapr0 [2] pviol1 [3] gapr1 [4] rviol0 [5] rviol1 [6] dv^2
+  //    [7] cviol0 [8] gapc0 [9] cviol1 [10] gapc1 [11] du^2 [12] c'u0 [13] c'u1
+  const double dp = c->dp, dd = c->dd;
+  auto assemble = [&](double pv, double gr, double rv, double cv, double gc, double cu) {
+    Residuals r;
+    r.absolute_primal = sqrt(pv) / dp;
+    r.primal = r.absolute_primal / (1.0 + c->bound_norm_s);
+    r.absolute_dual = sqrt(cv + rv) / dd;
+    r.dual = r.absolute_dual / (1.0 + c->cost_norm_s);
+    // Objective of xbar + u / dp; the gap from the complementarity products, so the
+    // large and nearly equal primal and dual objectives are never subtracted.
+    const double gap = (gc - gr) / (dp * dd);
+    r.primal_objective = c->pobj0 + cu / dp;
+    r.dual_objective = r.primal_objective - gap;
+    r.gap = fabs(gap) / (1.0 + fabs(r.primal_objective) + fabs(r.dual_objective));
+    r.gap_as_verified = fabs(gap) / dmax(1.0, fabs(r.primal_objective));
+    r.complementarity = 0.0;
+    return r;
+  };
+  const Residuals cur = assemble(t[0], t[1], t[4], t[7], t[8], t[12]);
+  Residuals av;
+  if (avg) av = assemble(t[2], t[3], t[5], t[9], t[10], t[13]);
+  tick_decisions(c, cur, avg ? &av : nullptr, round_stop_test, t[11], t[6], 1e-10, 1e10);
+}
+
+__global__ void k_evalf_apply(MixedBuffers b) {
+  const Ctl* c = b.ctl;
+  if (c->eval_now == 0) return;
+  const int copy = c->copy_best;
+  const bool restart = c->do_restart != 0;
+  if (copy == 0 && !restart) return;
+  const int cur = c->cur;
+  const int total = b.m > b.n ? b.m : b.n;
+  for (int k = grid_stride_begin(); k < total; k += gridDim.x * blockDim.x) {
+    if (k < b.n) {
+      if (copy) b.u_best[k] = b.uc[copy - 1][k];
+      if (restart) {
+        b.u_rst[k] = b.u[cur][k];
+        b.u_sum[k] = 0.0f;
+      }
+    }
+    if (k < b.m) {
+      if (copy) b.v_best[k] = b.vc[copy - 1][k];
+      if (restart) {
+        b.v_rst[k] = b.v[cur][k];
+        b.v_sum[k] = 0.0f;
+      }
+    }
+  }
+}
+
+// ---- Refinement rounds (FP64) --------------------------------------------------------------
+
+// Residual measures of the anchor: out[0] = max primal violation, out[1] = max dual
+// residual (reduced cost not absorbed by the bound the anchor sits on, or a multiplier on a
+// row side the activity does not touch), out[2] = c' xbar.
+__global__ void k_round_measure(RoundBuffers r) {
+  __shared__ double scratch[3 * (kTileThreads / 32)];
+  double mx[2] = {0.0, 0.0};
+  double obj[1] = {0.0};
+  const int total = r.m > r.n ? r.m : r.n;
+  for (int k = grid_stride_begin(); k < total; k += gridDim.x * blockDim.x) {
+    if (k < r.m) {
+      const double a = r.ax[k], rl = r.rls[k], ru = r.rus[k], y = r.ybar[k];
+      mx[0] = dmax(mx[0], dmax(rl - a, a - ru));
+      if (rl != ru) {
+        if (y > 0.0 && a < ru) mx[1] = dmax(mx[1], y);
+        if (y < 0.0 && a > rl) mx[1] = dmax(mx[1], -y);
+      }
+    }
+    if (k < r.n) {
+      const double d = r.cs[k] + r.aty[k], x = r.xbar[k], l = r.ls[k], u = r.us[k];
+      double res;
+      if (l == u) res = 0.0;
+      else if (x <= l) res = d < 0.0 ? -d : 0.0;
+      else if (x >= u) res = d > 0.0 ? d : 0.0;
+      else res = fabs(d);
+      mx[1] = dmax(mx[1], res);
+      obj[0] = fma(r.cs[k], x, obj[0]);
+    }
+  }
+  double m2[2], o1[1];
+  block_max<2>(mx, scratch, m2);
+  block_sum<1>(obj, scratch, o1);
+  __shared__ int s_last;
+  if (threadIdx.x == 0) {
+    r.part[3 * blockIdx.x] = m2[0];
+    r.part[3 * blockIdx.x + 1] = m2[1];
+    r.part[3 * blockIdx.x + 2] = o1[0];
+    __threadfence();
+    s_last = atomicAdd(r.ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  double a[2] = {0.0, 0.0}, o[1] = {0.0};
+  for (int blk = threadIdx.x; blk < gridDim.x; blk += blockDim.x) {
+    a[0] = dmax(a[0], __ldcg(r.part + 3 * blk));
+    a[1] = dmax(a[1], __ldcg(r.part + 3 * blk + 1));
+    o[0] += __ldcg(r.part + 3 * blk + 2);
+  }
+  block_max<2>(a, scratch, m2);
+  block_sum<1>(o, scratch, o1);
+  if (threadIdx.x == 0) {
+    r.out[0] = m2[0];
+    r.out[1] = m2[1];
+    r.out[2] = o1[0];
+    *r.ticket = 0;
+  }
+}
+
+__global__ void k_round_build(RoundBuffers r) {
+  const double dp = r.ctl->dp, dd = r.ctl->dd;
+  const int total = r.m > r.n ? r.m : r.n;
+  for (int k = grid_stride_begin(); k < total; k += gridDim.x * blockDim.x) {
+    if (k < r.n) {
+      const double x = r.xbar[k];
+      r.cf[k] = static_cast<float>(dd * (r.cs[k] + r.aty[k]));
+      r.lf[k] = static_cast<float>(dp * (r.ls[k] - x));
+      r.uf[k] = static_cast<float>(dp * (r.us[k] - x));
+    }
+    if (k < r.m) {
+      const double a = r.ax[k];
+      r.gu[k] = static_cast<float>(dp * (a - r.rus[k]));
+      r.gl[k] = static_cast<float>(dp * (a - r.rls[k]));
+      r.yhat[k] = static_cast<float>(dd * r.ybar[k]);
+    }
+  }
+}
+
+__global__ void k_round_update(RoundBuffers r) {
+  const double dp = r.ctl->dp, dd = r.ctl->dd;
+  const int total = r.m > r.n ? r.m : r.n;
+  for (int k = grid_stride_begin(); k < total; k += gridDim.x * blockDim.x) {
+    if (k < r.n) {
+      const double x = clamp_box(r.xbar[k] + static_cast<double>(r.u_src[k]) / dp, r.ls[k],
+                                 r.us[k]);
+      r.xbar[k] = x;
+      r.best_x[k] = x * r.dc[k];
+    }
+    if (k < r.m) {
+      const double y = r.ybar[k] + static_cast<double>(r.v_src[k]) / dd;
+      r.ybar[k] = y;
+      r.best_y[k] = y * r.dr[k];
+    }
+  }
+}
+
+__global__ void k_to_float(const double* src, float* dst, long long count) {
+  for (long long k = grid_stride_begin(); k < count; k += static_cast<long long>(gridDim.x) * blockDim.x) {
+    dst[k] = static_cast<float>(src[k]);
+  }
+}
+
+__global__ void k_fill_float(float* v, int count, float value) {
+  for (int k = grid_stride_begin(); k < count; k += gridDim.x * blockDim.x) v[k] = value;
+}
+
+int g_sms = 0;
+int egrid(long long count) {
+  if (g_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  long long blocks = (count + 255) / 256;
+  const long long cap = static_cast<long long>(g_sms) * 8;
+  if (blocks > cap) blocks = cap;
+  return blocks < 1 ? 1 : static_cast<int>(blocks);
+}
+
+}  // namespace
+
+void configure_mixed_kernels() {
+  static bool done = false;
+  if (done) return;
+  cudaFuncSetAttribute(k_primal_f, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemF);
+  cudaFuncSetAttribute(k_dual_f, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemF);
+  cudaFuncSetAttribute(k_evalf_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemF);
+  cudaFuncSetAttribute(k_evalf_rows1, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemF);
+  done = true;
+}
+
+int mixed_blocks_per_sm() {
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    configure_mixed_kernels();
+    int a = 0, b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_dual_f, kTileThreads, kSmemF);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_primal_f, kTileThreads, kSmemF);
+    per_sm = a < b ? a : b;
+    if (per_sm <= 0) per_sm = 1;
+  }
+  return per_sm;
+}
+
+void launch_mixed_primal(const MixedBuffers& b, cudaStream_t s) {
+  k_primal_f<<<b.grid_primal, kTileThreads, kSmemF, s>>>(b);
+}
+
+void launch_mixed_dual(const MixedBuffers& b, cudaStream_t s) {
+  k_dual_f<<<b.grid_dual, kTileThreads, kSmemF, s>>>(b);
+}
+
+void launch_mixed_step(const MixedBuffers& b, cudaStream_t s) {
+  launch_mixed_primal(b, s);
+  launch_mixed_dual(b, s);
+}
+
+void launch_mixed_evaluation(const MixedBuffers& b, cudaStream_t s) {
+  k_evalf_rows0<<<b.grid_dual, kTileThreads, 0, s>>>(b);
+  k_evalf_cols<<<b.grid_primal, kTileThreads, kSmemF, s>>>(b);
+  k_evalf_rows1<<<b.grid_dual, kTileThreads, kSmemF, s>>>(b);
+  k_evalf_apply<<<egrid(b.m > b.n ? b.m : b.n), 256, 0, s>>>(b);
+}
+
+void launch_round_measure(const RoundBuffers& r, cudaStream_t s) {
+  k_round_measure<<<r.grid, kTileThreads, 0, s>>>(r);
+}
+
+void launch_round_build(const RoundBuffers& r, cudaStream_t s) {
+  k_round_build<<<egrid(r.m > r.n ? r.m : r.n), 256, 0, s>>>(r);
+}
+
+void launch_round_update(const RoundBuffers& r, cudaStream_t s) {
+  k_round_update<<<egrid(r.m > r.n ? r.m : r.n), 256, 0, s>>>(r);
+}
+
+void launch_to_float(const double* src, float* dst, long long count, cudaStream_t s) {
+  if (count <= 0) return;
+  k_to_float<<<egrid(count), 256, 0, s>>>(src, dst, count);
+}
+
+void launch_fill_float(float* v, int count, float value, cudaStream_t s) {
+  if (count <= 0) return;
+  k_fill_float<<<egrid(count), 256, 0, s>>>(v, count, value);
+}
+
+}  // namespace sgb

@@ -18,6 +18,7 @@
 // entry as the method allows (one FMA per entry and product), to divide only where a row
 // is not an equality, and to keep every reduction deterministic.
 #include "common.cuh"
+#include "decisions.cuh"
 #include "kernels.cuh"
 #include "tiles.cuh"
 
@@ -38,36 +39,11 @@ __device__ __forceinline__ void raise_error(Ctl* c) {
   c->done = kFault;
 }
 
-// ---- Step decision, src/pdhg/pdhg.cpp:252-335 (one thread) --------------------------------
-__device__ void step_decision(Ctl* c, double movement, double interaction) {
-  c->movement = movement;
-  c->interaction = interaction;
-  const bool no_information = interaction <= 0.0;
-  const double limit = no_information ? __longlong_as_double(0x7ff0000000000000LL)
-                                      : movement / interaction;
-  const long long e = c->iteration + 1 > 2 ? c->iteration + 1 : 2;
-  const double exponent = static_cast<double>(e);
-  const double shrink = 1.0 - pow(exponent, -0.3);
-  const double grow = 1.0 + pow(exponent, -0.6);
-  const double proposed = dmin(shrink * limit, grow * c->eta);
-  const bool accept = c->eta <= limit;
-  if (accept) {
-    c->cur ^= 1;
-    c->iteration += 1;
-    c->averaged += 1;
-    c->pending_add = 1;
-  } else {
-    c->pending_add = 0;
-  }
-  if (!no_information) {
-    double eta = proposed;
-    eta = eta < 1e-12 ? 1e-12 : (c->eta_ceiling < eta ? c->eta_ceiling : eta);
-    c->eta = eta;
-  }
-  c->attempts += 1;
-  c->accepted = accept;
-  c->no_information = no_information;
-  c->eval_now = (c->iteration > 0) && ((c->iteration % 40) == 0 || no_information);
+// The reference's stopping test (src/pdhg/pdhg.cpp:424-425), or relative KKT alone.
+__device__ bool fp64_stop_test(const Ctl* c, const Residuals& r) {
+  return c->stop_rule == 1 ? worst(r) <= c->tolerance
+                           : meets_request(r, c->tolerance) &&
+                                 (c->stop_at_request || meets_project_standard(r));
 }
 
 // ---- k_primal ----------------------------------------------------------------------------
@@ -104,8 +80,8 @@ __global__ void __launch_bounds__(kTileThreads) k_primal(StepBuffers b) {
     const double xnj = clamp_box(__dsub_rn(xj, __dmul_rn(tau, gradient)), b.l[j], b.u[j]);
     xn[j] = xnj;
     const double d = xnj - xj;
-    b.dx[j] = d;
-    b.xbar[j] = fma(2.0, xnj, -xj);  // 2 x' is exact: one rounding, as 2.0 * x' - x
+    // 2 x' is exact, so the FMA rounds once, as the reference's 2.0 * x' - x does.
+    b.xd[j] = make_double2(fma(2.0, xnj, -xj), d);
     mv[0] = fma(d, d, mv[0]);
   };
   TilePipe<double> pipe;
@@ -135,15 +111,15 @@ __global__ void __launch_bounds__(kTileThreads) k_dual(StepBuffers b) {
   const int cur = ctl->cur;
   const double* __restrict__ y = b.y[cur];
   double* __restrict__ yn = b.y[cur ^ 1];
-  const double* __restrict__ xbar = b.xbar;
-  const double* __restrict__ dx = b.dx;
+  const double2* __restrict__ xd = b.xd;
   const double omega = ctl->omega;
   const double sigma = ctl->eta * omega;
   const bool add = ctl->pending_add != 0;
   double acc2[2] = {0.0, 0.0};  // sum dy^2, sum dy (A dx)
   auto gather = [&](int col, double v, double* acc) {
-    acc[0] = fma(v, __ldg(xbar + col), acc[0]);
-    acc[1] = fma(v, __ldg(dx + col), acc[1]);
+    const double2 p = __ldg(xd + col);
+    acc[0] = fma(v, p.x, acc[0]);
+    acc[1] = fma(v, p.y, acc[1]);
   };
   auto epi = [&](int i, const double* s) {
     const double yi = y[i];
@@ -434,65 +410,12 @@ __global__ void __launch_bounds__(kTileThreads) k_eval_rows1(EvalBuffers e) {
     c->model_objective = t15[14];
     return;
   }
-  c->evaluations += 1;
-  Residuals chosen = cur;
-  int which = 1;
+  Residuals av;
   if (avg) {
-    const Residuals av = assemble(t15[6], t15[10], t15[3], t15[11], t15[2], t15[12],
-                                  dmax(t4[1], t4[3]), e.bound_norm, e.cost_norm);
-    if (worst(av) < worst(cur)) {
-      chosen = av;
-      which = 2;
-    }
+    av = assemble(t15[6], t15[10], t15[3], t15[11], t15[2], t15[12], dmax(t4[1], t4[3]),
+                  e.bound_norm, e.cost_norm);
   }
-  int copy = 0;
-  if (worst(chosen) < worst(c->best)) {
-    c->best = chosen;
-    copy = which;
-  }
-  {
-    const long long slot = c->log_count % kLogRing;
-    c->log[slot].iteration = c->iteration;
-    c->log[slot].primal_objective = chosen.primal_objective;
-    c->log[slot].primal = chosen.primal;
-    c->log[slot].dual = chosen.dual;
-    c->log[slot].gap = chosen.gap;
-    c->log_count += 1;
-  }
-  const bool stop_here =
-      c->stop_rule == 1 ? worst(chosen) <= c->tolerance
-                        : meets_request(chosen, c->tolerance) &&
-                              (c->stop_at_request || meets_project_standard(chosen));
-  if (stop_here) {
-    c->best = chosen;
-    c->copy_best = which;
-    c->done = kConverged;
-    return;
-  }
-  c->copy_best = copy;
-  if (c->use_restarts) {
-    const double kkt = worst(chosen);
-    const long long since = c->iteration - c->last_restart;
-    const bool sufficient = kkt <= 0.2 * c->restart_kkt;
-    const long long f36 = static_cast<long long>(0.36 * static_cast<double>(c->iteration));
-    const bool artificial = since >= (f36 > 40 ? f36 : 40);
-    if (sufficient || artificial) {
-      const double dx_norm = sqrt(t15[13]);
-      const double dy_norm = sqrt(t15[4]);
-      if (dx_norm > 1e-12 && dy_norm > 1e-12) {
-        const double theta = 0.5;
-        double omega = exp(theta * log(dy_norm / dx_norm) + (1.0 - theta) * log(c->omega));
-        omega = omega < 1e-6 ? 1e-6 : (1e6 < omega ? 1e6 : omega);
-        c->omega = omega;
-      }
-      c->do_restart = 1;
-      c->averaged = 0;
-      c->pending_add = 0;
-      c->restart_kkt = kkt;
-      c->last_restart = c->iteration;
-      c->restarts += 1;
-    }
-  }
+  tick_decisions(c, cur, avg ? &av : nullptr, fp64_stop_test, t15[13], t15[4], 1e-6, 1e6);
 }
 
 // E4: the vector half of the decisions: best point copy, restart anchors, zeroed sums.

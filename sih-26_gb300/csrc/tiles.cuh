@@ -251,8 +251,9 @@ __device__ __forceinline__ bool run_tiles(TilePipe<V>& pipe, const TileSet<V>& t
   return true;
 }
 
-// Last block only: the long rows, each combined from its chunk partials in chunk order.
-template <int NP, typename V, typename Epi>
+// Last block only: the long rows, each combined from its chunk partials in chunk order (in
+// double), then handed to the epilogue in the accumulator type A.
+template <int NP, typename A = double, typename V, typename Epi>
 __device__ __forceinline__ void run_long_rows(const TileSet<V>& ts, const double* chunk_part,
                                               Epi epi) {
   for (int l = threadIdx.x; l < ts.nlong; l += blockDim.x) {
@@ -264,7 +265,10 @@ __device__ __forceinline__ void run_long_rows(const TileSet<V>& ts, const double
 #pragma unroll
       for (int q = 0; q < NP; ++q) acc[q] += __ldcg(chunk_part + (lr.chunk0 + c) * NP + q);
     }
-    epi(lr.row, acc);
+    A out[NP];
+#pragma unroll
+    for (int q = 0; q < NP; ++q) out[q] = static_cast<A>(acc[q]);
+    epi(lr.row, out);
   }
 }
 

@@ -32,6 +32,7 @@ _D = ctypes.POINTER(ctypes.c_double)
 _I = ctypes.POINTER(ctypes.c_int32)
 LOG_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_double,
                           ctypes.c_double, ctypes.c_double, ctypes.c_double)
+POLL_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong, ctypes.c_double)
 
 
 class EngineError(RuntimeError):
@@ -54,7 +55,7 @@ class CParams(ctypes.Structure):
                 ("precision", ctypes.c_int32), ("steps_per_poll", ctypes.c_int32),
                 ("stop_rule", ctypes.c_int32), ("reserved", ctypes.c_int32),
                 ("interrupt", ctypes.POINTER(ctypes.c_int32)), ("log", LOG_FN),
-                ("log_user", ctypes.c_void_p)]
+                ("log_user", ctypes.c_void_p), ("poll", POLL_FN), ("poll_user", ctypes.c_void_p)]
 
 
 class CResiduals(ctypes.Structure):
@@ -215,14 +216,18 @@ class PdhgEngine:
               time_limit: Optional[float] = None, restart: bool = True,
               stop_at_request: bool = False, random_seed: int = 0, precision: str = "fp64",
               steps_per_poll: int = 0, interrupt: Optional[np.ndarray] = None,
-              log: Optional[Callable] = None, stop_rule: str = "standard") -> Result:
+              log: Optional[Callable] = None, stop_rule: str = "standard",
+              poll: Optional[Callable] = None) -> Result:
+        """``poll(iteration, objective) -> bool`` is asked at every status snapshot; True
+        interrupts the solve."""
         cb = LOG_FN(lambda user, it, obj, p, d, s: log(it, obj, p, d, s)) if log else LOG_FN()
+        pcb = POLL_FN(lambda user, it, obj: int(bool(poll(it, obj)))) if poll else POLL_FN()
         intr = (interrupt.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
                 if interrupt is not None else ctypes.POINTER(ctypes.c_int32)())
         params = CParams(tolerance, iteration_limit,
                          1e308 if time_limit is None else float(time_limit), int(restart),
                          int(stop_at_request), random_seed, PRECISIONS[precision],
-                         steps_per_poll, STOP_RULES[stop_rule], 0, intr, cb, None)
+                         steps_per_poll, STOP_RULES[stop_rule], 0, intr, cb, None, pcb, None)
         r = CResult()
         _check(self._lib.sankhya_gb300_pdhg_solve(self._h, ctypes.byref(params), ctypes.byref(r)))
         return Result(r.status, STATUS_NAMES.get(r.status, str(r.status)), bool(r.converged),
