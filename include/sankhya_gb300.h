@@ -194,6 +194,24 @@ SGB_API int sankhya_gb300_pdhg_scaling(sankhya_gb300_pdhg* engine, int64_t rando
 SGB_API int sankhya_gb300_pdhg_spmv(sankhya_gb300_pdhg* engine, int32_t op, int32_t scaled,
                                     const double* in, double* out);
 
+/* The same product on DEVICE buffers, allocating nothing. It has no reference counterpart:
+ * the reference's products (src/la/sparse.cpp:232-259) are host-side only. It is for callers
+ * that hold their vectors in device memory and may not allocate: a device allocation
+ * synchronises the whole GPU and fails when a caching allocator has already reserved the
+ * memory. `device_in` (cols entries for op 0, rows for op 1) and `device_out` are device
+ * pointers; the work is enqueued on `stream` (a cudaStream_t; NULL = the engine's stream)
+ * and the call returns without waiting for it. Its only scratch is a fixed device array of
+ * SANKHYA_GB300_NOALLOC_MAX_CHUNKS partial sums (one per 2048 entries of each row longer than
+ * 2048) plus a counter; a matrix that needs more slots is refused with
+ * SANKHYA_GB300_ERROR_ARGUMENT. The first call on a device sets that scratch up (finds it and
+ * clears the counter, waiting for the stream) and must come before any stream capture.
+ * Calls on one device share the scratch: calls that overlap in time race, so order them
+ * (one stream, or events between streams). */
+#define SANKHYA_GB300_NOALLOC_MAX_CHUNKS 16384
+SGB_API int sankhya_gb300_pdhg_spmv_noalloc(sankhya_gb300_pdhg* engine, int32_t op,
+                                            int32_t scaled, const double* device_in,
+                                            double* device_out, void* stream);
+
 /* Measurement hook: time `reps` attempted PDHG steps on the state the last solve left,
  * each kernel bracketed by CUDA events on the engine's stream. ms[0] = mean duration of the
  * primal (column) pass, ms[1] = mean duration of the dual (row) pass, in milliseconds. The

@@ -156,6 +156,18 @@ SGB_API int sankhya_gb300_pdhg_spmv(sankhya_gb300_pdhg* engine, int32_t op, int3
   return guarded([&] { engine->engine->spmv(op, scaled, in, out); });
 }
 
+SGB_API int sankhya_gb300_pdhg_spmv_noalloc(sankhya_gb300_pdhg* engine, int32_t op,
+                                            int32_t scaled, const double* device_in,
+                                            double* device_out, void* stream) {
+  if (engine == nullptr || engine->engine == nullptr) {
+    return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null engine");
+  }
+  return guarded([&] {
+    engine->engine->spmv_noalloc(op, scaled, device_in, device_out,
+                                 static_cast<cudaStream_t>(stream));
+  });
+}
+
 SGB_API int sankhya_gb300_pdhg_time_kernels(sankhya_gb300_pdhg* engine, int32_t reps,
                                             double* ms) {
   if (engine == nullptr || ms == nullptr || reps <= 0) {

@@ -647,6 +647,41 @@ void Engine::spmv(int op, int scaled, const double* in, double* out) {
   SGB_CUDA(cudaStreamSynchronize(s));
 }
 
+static_assert(kNoAllocMaxChunks == SANKHYA_GB300_NOALLOC_MAX_CHUNKS,
+              "the header states the scratch size");
+
+void Engine::spmv_noalloc(int op, int scaled, const double* in, double* out,
+                          cudaStream_t stream) {
+  require_loaded();
+  if (op != 0 && op != 1) {
+    throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, format("op must be 0 or 1, not %d", op)};
+  }
+  if (scaled && !scaled_) {
+    throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no preconditioning has run yet"};
+  }
+  const int in_len = op == 0 ? n_ : m_;
+  const int out_len = op == 0 ? m_ : n_;
+  if ((in_len > 0 && in == nullptr) || (out_len > 0 && out == nullptr)) {
+    throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "null device buffer"};
+  }
+  TileSet<double> a = op == 0 ? step_.csr : step_.csc;
+  if (a.nchunks > kNoAllocMaxChunks) {
+    throw EngineError{
+        SANKHYA_GB300_ERROR_ARGUMENT,
+        format("this matrix needs %d long-row chunk slots (one per %d entries of a row longer "
+               "than %d); the allocation-free product holds at most %d",
+               a.nchunks, kCap, kCap, kNoAllocMaxChunks)};
+  }
+  SGB_CUDA(cudaSetDevice(device_));
+  cudaStream_t s = stream != nullptr ? stream : stream_;
+  double* chunks = nullptr;
+  unsigned int* ticket = nullptr;
+  SGB_CUDA(noalloc_scratch(device_, s, &chunks, &ticket));
+  if (!scaled) a.val = op == 0 ? csr_raw_.ptr : csc_raw_.ptr;
+  launch_spmv(a, in, out, chunks, ticket, s, op == 0 ? grid_csr_ : grid_csc_);
+  SGB_CUDA(cudaGetLastError());
+}
+
 void Engine::init_iterates(const sankhya_gb300_params& p) {
   cudaStream_t s = stream_;
   launch_project_start(n_, ls_.ptr, us_.ptr, x0_.ptr, s);

@@ -49,6 +49,9 @@ class Engine {
   void scaling(long long seed, double* row_scale, double* col_scale, double* scaled_values,
                double* spectral_norm);
   void spmv(int op, int scaled, const double* in, double* out);
+  // The same product on caller-owned DEVICE buffers, enqueued on `stream` (nullptr: the
+  // engine's stream) with the fixed scratch of noalloc_scratch(): allocates no memory.
+  void spmv_noalloc(int op, int scaled, const double* in, double* out, cudaStream_t stream);
   void time_kernels(int reps, double* ms);
 
   int device() const { return device_; }

@@ -156,6 +156,13 @@ void launch_scale_vectors(int m, int n, const double* cost, const double* l, con
                           cudaStream_t s);
 // y = A x with the tile kernel (CSR gives A x; CSC gives A^T x). chunk holds a.nchunks
 // doubles; ticket is one device counter that is zero on entry and on exit.
+// Fixed device scratch of the allocation-free product: chunk partials for at most
+// kNoAllocMaxChunks chunk tiles and its completion counter. Set up once per device (the
+// symbol addresses, and the counter cleared to zero) under a lock; later calls only read the
+// cached addresses.
+constexpr int kNoAllocMaxChunks = 16384;
+cudaError_t noalloc_scratch(int device, cudaStream_t s, double** chunks, unsigned int** ticket);
+
 void launch_spmv(TileSet<double> a, const double* x, double* y, double* chunk,
                  unsigned int* ticket, cudaStream_t s, int grid);
 // out[0] = sum v^2, deterministic; part holds grid doubles.

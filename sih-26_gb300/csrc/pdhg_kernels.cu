@@ -23,6 +23,7 @@
 #include "tiles.cuh"
 
 #include <cstdio>
+#include <mutex>
 
 namespace sgb {
 
@@ -699,6 +700,51 @@ void launch_spmv(TileSet<double> a, const double* x, double* y, double* chunk,
   if (a.nrows == 0) return;
   ++g_launches;
   k_spmv<<<grid, kTileThreads, kTileSmem, s>>>(a, x, y, chunk, ticket);
+}
+
+namespace {
+
+// The allocation-free product's scratch: file-scope device arrays, never cudaMalloc'd.
+static __device__ __align__(256) double g_noalloc_chunks[kNoAllocMaxChunks];
+static __device__ __align__(256) unsigned int g_noalloc_ticket[4];
+
+constexpr int kNoAllocMaxDevices = 64;
+struct NoAllocSlot {
+  bool ready;
+  double* chunks;
+  unsigned int* ticket;
+};
+std::mutex g_noalloc_mutex;
+NoAllocSlot g_noalloc_slots[kNoAllocMaxDevices];
+
+}  // namespace
+
+cudaError_t noalloc_scratch(int device, cudaStream_t s, double** chunks, unsigned int** ticket) {
+  if (device < 0 || device >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  NoAllocSlot& slot = g_noalloc_slots[device];
+  if (!slot.ready) {
+    cudaError_t err = cudaSetDevice(device);
+    if (err != cudaSuccess) return err;
+    void* c = nullptr;
+    void* t = nullptr;
+    err = cudaGetSymbolAddress(&c, g_noalloc_chunks);
+    if (err != cudaSuccess) return err;
+    err = cudaGetSymbolAddress(&t, g_noalloc_ticket);
+    if (err != cudaSuccess) return err;
+    // The completion counter must start at zero; k_spmv's last block puts it back to zero.
+    // The chunk partials need no clearing: each is written before it is read.
+    err = cudaMemsetAsync(t, 0, sizeof(g_noalloc_ticket), s);
+    if (err != cudaSuccess) return err;
+    err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) return err;
+    slot.chunks = static_cast<double*>(c);
+    slot.ticket = static_cast<unsigned int*>(t);
+    slot.ready = true;
+  }
+  *chunks = slot.chunks;
+  *ticket = slot.ticket;
+  return cudaSuccess;
 }
 
 void launch_sumsq(const double* v, int count, double* part, double* out, unsigned int* ticket,

@@ -86,6 +86,7 @@ EXPORTS = [
     "sankhya_gb300_estimate_memory", "sankhya_gb300_pdhg_create", "sankhya_gb300_pdhg_destroy",
     "sankhya_gb300_pdhg_load", "sankhya_gb300_pdhg_solve", "sankhya_gb300_pdhg_solution",
     "sankhya_gb300_pdhg_scaling", "sankhya_gb300_pdhg_spmv", "sankhya_gb300_pdhg_time_kernels",
+    "sankhya_gb300_pdhg_spmv_noalloc",
 ]
 
 _lib = None
@@ -123,6 +124,9 @@ def load_library():
         lib.sankhya_gb300_pdhg_spmv.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                                 _D, _D]
         lib.sankhya_gb300_pdhg_time_kernels.argtypes = [ctypes.c_void_p, ctypes.c_int32, _D]
+        lib.sankhya_gb300_pdhg_spmv_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int32,
+                                                        ctypes.c_int32, ctypes.c_void_p,
+                                                        ctypes.c_void_p, ctypes.c_void_p]
         for name in EXPORTS:
             if name not in ("sankhya_gb300_last_error", "sankhya_gb300_estimate_memory"):
                 getattr(lib, name).restype = ctypes.c_int
@@ -268,6 +272,15 @@ class PdhgEngine:
         out = np.zeros(lp.rows if op == 0 else lp.cols)
         _check(self._lib.sankhya_gb300_pdhg_spmv(self._h, op, int(scaled), _ptr(vec), _ptr(out)))
         return out
+
+    def spmv_device(self, op: int, device_in: int, device_out: int, scaled: bool = False,
+                    stream: Optional[int] = None):
+        """The product on caller-owned device buffers (raw device addresses), enqueued on
+        `stream` (a cudaStream_t handle; None = the engine's stream); allocates nothing and
+        does not wait for the work."""
+        _check(self._lib.sankhya_gb300_pdhg_spmv_noalloc(
+            self._h, op, int(scaled), ctypes.c_void_p(device_in), ctypes.c_void_p(device_out),
+            ctypes.c_void_p(stream) if stream else None))
 
 
 @dataclass
