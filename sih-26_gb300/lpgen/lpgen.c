@@ -16,6 +16,11 @@
  *                          k distinct uniform rows per column inside its block plus one +-1
  *                          linking entry into a uniform row of the next block (none for the
  *                          last block); otherwise as planted_uniform.
+ *   lpgen_planted_zipf     load-balance stress: row lengths from a Zipf law (P(L) ~ L^-a,
+ *                          drawn as min_len U^(-1/(a-1)) and clipped to [min_len, max_len]),
+ *                          scaled so the lengths sum to about target_nnz, distinct uniform
+ *                          columns per row, values +-10^U(-3,3) (log-uniform magnitude over
+ *                          [1e-3, 1e3], random sign), 0 <= x <= 10, equality rows.
  *   lpgen_planted_general  every row kind (equality, one-sided active/slack, range active at
  *                          either side, free) and every column kind (boxed, lower-only,
  *                          upper-only, free, fixed) for parity coverage.
@@ -135,6 +140,20 @@ static double det_cos_turns(double u) {
   }
   if (w <= 0.125) return sign * taylor_cos(two_pi * w);
   return sign * taylor_sin(two_pi * (0.25 - w)); /* cos(a) = sin(pi/2 - a) */
+}
+
+/* exp from IEEE basic operations and ldexp: x = k ln2 + r with |r| <= ln2 / 2, then the
+ * Taylor series of exp(r) (27 terms: far past double precision for |r| <= 0.35). */
+static double det_exp(double x) {
+  const double ln2 = 0.69314718055994530942;
+  const double kf = floor(x / ln2 + 0.5);
+  const double r = x - kf * ln2;
+  double term = 1.0, sum = 1.0;
+  for (int k = 1; k < 28; ++k) {
+    term *= r / (double)k;
+    sum += term;
+  }
+  return ldexp(sum, (int)kf);
 }
 
 /* Standard normal by Box-Muller (one value per call). */
@@ -384,6 +403,118 @@ int32_t lpgen_planted_general(int32_t m, int32_t n, int32_t k, int32_t flags, ui
   lp->fstar = f;
   free(act);
   free(z);
+  free(g);
+  return 0;
+}
+
+/* Row lengths of the Zipf shape, drawn first from the instance's generator so that the
+ * _nnz query and the generator agree. Returns the total. */
+static int64_t zipf_lengths(mt64* g, int32_t m, int32_t n, int64_t target_nnz, double exponent,
+                            int32_t min_len, int32_t max_len, int32_t* len) {
+  const double inv_tail = 1.0 / (exponent - 1.0);
+  double raw_total = 0.0;
+  double* raw = (double*)malloc(sizeof(double) * (size_t)m);
+  for (int32_t i = 0; i < m; ++i) {
+    const double u = ((double)(mt64_next(g) >> 11) + 1.0) * (1.0 / 9007199254740992.0);
+    double l = (double)min_len * det_exp(-inv_tail * det_log(u));
+    if (l > (double)max_len) l = (double)max_len;
+    raw[i] = floor(l);
+    raw_total += raw[i];
+  }
+  const double scale = (double)target_nnz / raw_total;
+  const int32_t cap = max_len < n ? max_len : n;
+  int64_t total = 0;
+  for (int32_t i = 0; i < m; ++i) {
+    double l = floor(raw[i] * scale + 0.5);
+    if (l < (double)min_len) l = (double)min_len;
+    if (l > (double)cap) l = (double)cap;
+    len[i] = (int32_t)l;
+    total += len[i];
+  }
+  free(raw);
+  return total;
+}
+
+static int zipf_args_ok(int32_t m, int32_t n, int64_t target_nnz, double exponent,
+                        int32_t min_len, int32_t max_len) {
+  return m > 0 && n > 0 && target_nnz > 0 && exponent > 1.0 && min_len >= 1 &&
+         max_len >= min_len && min_len <= n;
+}
+
+int64_t lpgen_planted_zipf_nnz(int32_t m, int32_t n, int64_t target_nnz, double exponent,
+                               int32_t min_len, int32_t max_len, uint64_t seed) {
+  if (!zipf_args_ok(m, n, target_nnz, exponent, min_len, max_len)) return -1;
+  mt64* g = (mt64*)malloc(sizeof(mt64));
+  mt64_seed(g, seed);
+  int32_t* len = (int32_t*)malloc(sizeof(int32_t) * (size_t)m);
+  const int64_t total = zipf_lengths(g, m, n, target_nnz, exponent, min_len, max_len, len);
+  free(len);
+  free(g);
+  return total;
+}
+
+int32_t lpgen_planted_zipf(int32_t m, int32_t n, int64_t target_nnz, double exponent,
+                           int32_t min_len, int32_t max_len, uint64_t seed, lpgen_lp* lp) {
+  if (!zipf_args_ok(m, n, target_nnz, exponent, min_len, max_len)) return 1;
+  mt64* g = (mt64*)malloc(sizeof(mt64));
+  mt64_seed(g, seed);
+  int32_t* len = (int32_t*)malloc(sizeof(int32_t) * (size_t)m);
+  const int64_t nnz = zipf_lengths(g, m, n, target_nnz, exponent, min_len, max_len, len);
+  if (nnz > INT32_MAX) {
+    free(len);
+    free(g);
+    return 2;
+  }
+  /* Row-major draw: distinct uniform columns per row (rejection against a per-row stamp)
+   * and the values, then a counting transpose into CSC. Rows are visited in ascending order,
+   * so every column's row indices come out ascending. */
+  int32_t* rcol = (int32_t*)malloc(sizeof(int32_t) * (size_t)nnz);
+  double* rval = (double*)malloc(sizeof(double) * (size_t)nnz);
+  int32_t* stamp = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+  for (int32_t j = 0; j < n; ++j) stamp[j] = -1;
+  const double ln10 = 2.30258509299404568402;
+  int64_t at = 0;
+  for (int32_t i = 0; i < m; ++i) {
+    for (int32_t t = 0; t < len[i]; ++t) {
+      int32_t c;
+      do {
+        c = unif_int(g, n);
+      } while (stamp[c] == i);
+      stamp[c] = i;
+      rcol[at] = c;
+      const double mag = det_exp(ln10 * unif_ab(g, -3.0, 3.0));
+      rval[at] = unif(g) < 0.5 ? -mag : mag;
+      ++at;
+    }
+  }
+  lp->rows = m;
+  lp->cols = n;
+  lp->nnz = nnz;
+  for (int32_t j = 0; j <= n; ++j) lp->col_starts[j] = 0;
+  for (int64_t k = 0; k < nnz; ++k) lp->col_starts[rcol[k] + 1] += 1;
+  for (int32_t j = 0; j < n; ++j) lp->col_starts[j + 1] += lp->col_starts[j];
+  for (int32_t j = 0; j < n; ++j) stamp[j] = lp->col_starts[j];
+  at = 0;
+  for (int32_t i = 0; i < m; ++i) {
+    for (int32_t t = 0; t < len[i]; ++t, ++at) {
+      const int32_t slot = stamp[rcol[at]]++;
+      lp->row_index[slot] = i;
+      lp->values[slot] = rval[at];
+    }
+  }
+  double* z = (double*)malloc(sizeof(double) * (size_t)n);
+  for (int32_t j = 0; j < n; ++j) {
+    box_point(g, &lp->x0[j], &z[j]);
+    lp->col_lower[j] = 0.0;
+    lp->col_upper[j] = 10.0;
+  }
+  for (int32_t i = 0; i < m; ++i) lp->lambda[i] = normal(g);
+  finish_equalities(lp, z);
+  free(z);
+  free(stamp);
+  free(rval);
+  free(rcol);
+  free(len);
   free(g);
   return 0;
 }

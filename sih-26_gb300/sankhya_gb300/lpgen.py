@@ -8,6 +8,9 @@ The shapes follow the synthetic workloads this engine is measured on:
 * ``planted_blocks(blocks, R, C, k, seed)`` -- block-angular multi-period structure with one
   +-1 inventory link per column into the next period (64 x 15,625 x 31,250 with k = 9 is the
   1,000,000 x 2,000,000 headline case).
+* ``planted_zipf(m, n, target_nnz, ...)`` -- Zipf-distributed row lengths, uniform columns,
+  badly scaled values (500,000 x 1,000,000 with about 3e7 nonzeros is the load-balance
+  stress case).
 * ``planted_general(m, n, k, seed)`` -- every row and column kind, for coverage.
 """
 from __future__ import annotations
@@ -53,6 +56,14 @@ def _load():
         lib.lpgen_planted_blocks.restype = ctypes.c_int32
         lib.lpgen_planted_blocks_nnz.argtypes = [ctypes.c_int32] * 4
         lib.lpgen_planted_blocks_nnz.restype = ctypes.c_int64
+        lib.lpgen_planted_zipf_nnz.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64,
+                                               ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
+                                               ctypes.c_uint64]
+        lib.lpgen_planted_zipf_nnz.restype = ctypes.c_int64
+        lib.lpgen_planted_zipf.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64,
+                                           ctypes.c_double, ctypes.c_int32, ctypes.c_int32,
+                                           ctypes.c_uint64, ctypes.POINTER(_CLp)]
+        lib.lpgen_planted_zipf.restype = ctypes.c_int32
         _lib = lib
     return _lib
 
@@ -95,6 +106,23 @@ def planted_blocks(blocks: int, rows_per_block: int, cols_per_block: int, k: int
                                 ctypes.byref(c)) != 0:
         raise ValueError("planted_blocks: bad shape")
     return _finish(arrays, c, f"planted_blocks_{blocks}x{rows_per_block}x{cols_per_block}")
+
+
+def planted_zipf(m: int, n: int, target_nnz: int, exponent: float = 1.5, min_len: int = 2,
+                 max_len: int = 100000, seed: int = 1) -> LP:
+    """Load-balance stress: Zipf row lengths (P(L) ~ L^-exponent, clipped to
+    [min_len, max_len], scaled to about target_nnz in total), uniform columns, values of
+    log-uniform magnitude over [1e-3, 1e3] with random sign, 0 <= x <= 10, equality rows.
+    500,000 x 1,000,000 with target 3e7 is the headline stress case."""
+    lib = _load()
+    nnz = lib.lpgen_planted_zipf_nnz(m, n, target_nnz, exponent, min_len, max_len, seed)
+    if nnz < 0:
+        raise ValueError("planted_zipf: bad shape")
+    arrays, c = _alloc(m, n, nnz)
+    if lib.lpgen_planted_zipf(m, n, target_nnz, exponent, min_len, max_len, seed,
+                              ctypes.byref(c)) != 0:
+        raise ValueError("planted_zipf: bad shape or more than 2^31 nonzeros")
+    return _finish(arrays, c, f"planted_zipf_{m}x{n}")
 
 
 def planted_general(m: int, n: int, k: int = 4, seed: int = 1, maximize: bool = False,
