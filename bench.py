@@ -53,12 +53,18 @@ def peaks():
 
 
 def ncu_traffic():
-    """Per-launch DRAM bytes of the step kernels from the committed ncu summary."""
+    """Per-launch DRAM bytes (read + write) of the step kernels at the full workload, from the
+    committed ncu summary profiles/step_kernels_traffic.txt (lines "<kernel> <bytes>")."""
+    out = {}
     try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            return json.load(f)
-    except Exception:
-        return {}
+        with open(os.path.join(ROOT, "profiles", "step_kernels_traffic.txt")) as f:
+            for line in f:
+                parts = line.split()
+                if len(parts) == 2 and not line.startswith("#"):
+                    out[parts[0]] = float(parts[1])
+    except OSError:
+        pass
+    return out
 
 
 def algorithmic_bytes(m, n, nnz, v, w):
@@ -141,6 +147,82 @@ def make_workload():
                                 WORKLOAD["cols_per_block"], WORKLOAD["k"], WORKLOAD["seed"])
 
 
+# Batched workloads: 4,096 independent planted LPs (m log-uniform in [50, 2,000], n = 2m,
+# 5 nonzeros per column) and 1,024 branch-and-bound node relaxations of one planted
+# 10,000 x 20,000 LP (1-20 bounds tightened to [0, floor x0_j] or [ceil x0_j, 10]).
+BATCH_LPS = 4096
+BATCH_NODES = 1024
+BATCH_TOLERANCE = 1e-6
+BATCH_SEQUENTIAL_SAMPLE = (12, 3)  # LPs of each part solved one at a time for the baseline
+
+
+def make_batch_lps(seed=2027):
+    from sankhya_gb300 import lpgen
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    ms = np.exp(rng.uniform(np.log(50), np.log(2000), size=BATCH_LPS)).astype(int)
+    return [lpgen.planted_uniform(int(m), 2 * int(m), 5, seed=seed * 10000 + k)
+            for k, m in enumerate(ms)]
+
+
+def make_batch_nodes(seed=2028):
+    from sankhya_gb300 import lpgen
+    from sankhya_gb300.model import LP
+    import numpy as np
+
+    base = lpgen.planted_uniform(10000, 20000, 5, seed=seed)
+    rng = np.random.default_rng(seed)
+    nodes = []
+    for _ in range(BATCH_NODES):
+        lo, up = base.col_lower.copy(), base.col_upper.copy()
+        for j in rng.choice(base.cols, size=int(rng.integers(1, 21)), replace=False):
+            if rng.random() < 0.5:
+                up[j] = np.floor(base.x0[j])
+            else:
+                lo[j] = np.ceil(base.x0[j])
+        nodes.append(LP(base.rows, base.cols, base.col_starts, base.row_index, base.values,
+                        base.col_cost, lo, up, base.row_lower, base.row_upper))
+    return nodes
+
+
+def batched_section(device):
+    """LPs/s of the batched engine against the same LPs solved one at a time by the single-LP
+    engine (a sample of each part, extrapolated); FP64, relative KKT <= 1e-6."""
+    from sankhya_gb300 import capi
+
+    out = {}
+    for name, make, sample in (("independent", make_batch_lps, BATCH_SEQUENTIAL_SAMPLE[0]),
+                               ("bnb_nodes", make_batch_nodes, BATCH_SEQUENTIAL_SAMPLE[1])):
+        lps = make()
+        with capi.BatchEngine(device) as eng:
+            t0 = time.perf_counter()
+            eng.load(lps)
+            t_load = time.perf_counter() - t0
+            items, dev_s = eng.solve(tolerance=BATCH_TOLERANCE, stop_rule="relative",
+                                     iteration_limit=200000)
+        statuses = {}
+        for it in items:
+            statuses[it.status_name] = statuses.get(it.status_name, 0) + 1
+        step = max(1, len(lps) // sample)
+        picked = lps[::step][:sample]
+        seq_s = 0.0
+        with capi.PdhgEngine(device) as one:
+            for lp in picked:
+                one.load(lp)
+                r = one.solve(tolerance=BATCH_TOLERANCE, stop_rule="relative",
+                              iteration_limit=200000)
+                seq_s += r.device_seconds
+        seq_rate = len(picked) / seq_s
+        out[name] = {"lps": len(lps), "device_s": dev_s, "load_s": t_load,
+                     "lps_per_s": len(lps) / dev_s, "statuses": statuses,
+                     "iterations_mean": sum(it.iterations for it in items) / len(items),
+                     "sequential_lps_per_s": seq_rate,
+                     "sequential_sample": len(picked),
+                     "speedup_vs_sequential": (len(lps) / dev_s) / seq_rate}
+    return out
+
+
 def workload_config(lp, precision):
     return {"workload": f"block-angular planted LP {lp.rows:,} x {lp.cols:,}, {lp.nnz:,} nnz, "
                         f"{WORKLOAD['blocks']} periods, seed {WORKLOAD['seed']}",
@@ -169,11 +251,14 @@ def cpu_reference(lp, iterations_sample, threads):
     return setup, per_it, sampled + setup
 
 
-def kernel_roofline(eng, lp, precision, peak):
+def kernel_roofline(eng, lp, precision, peak, staged=None):
+    """Mean CUDA-event durations of the two step passes (on the engine's stream, 20 steps on
+    the state the last solve left) and their achieved GB/s on the algorithmic bytes."""
     ms_primal, ms_dual = eng.time_kernels(20)
     v = w = 8 if precision == "fp64" else 4
     b_col, b_row = algorithmic_bytes(lp.rows, lp.cols, lp.nnz, v, w)
     return {"k_primal_ms": ms_primal, "k_dual_ms": ms_dual,
+            "staged_share": list(staged) if staged is not None else None,
             "k_primal_gbs": b_col / (ms_primal * 1e-3) / 1e9,
             "k_dual_gbs": b_row / (ms_dual * 1e-3) / 1e9,
             "k_primal_bytes": b_col, "k_dual_bytes": b_row,
@@ -191,6 +276,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison solve")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-iterations", type=int, default=20)
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-LP section")
     args = ap.parse_args()
     rank, world, local, dist = dist_setup()
     threads = os.cpu_count() or 1
@@ -243,12 +329,12 @@ def main():
     step_s = max(r.device_seconds for r in results)
     last = results[-1]
     launches = sum(r.kernel_launches for r in results)
-    roof = kernel_roofline(eng, lp, args.precision, peak)
+    roof = kernel_roofline(eng, lp, args.precision, peak, last.staged_fraction)
 
     fp64 = None
     if args.precision != "fp64" and not args.no_fp64:
         f = eng.solve(precision="fp64", **opts)
-        froof = kernel_roofline(eng, lp, "fp64", peak)
+        froof = kernel_roofline(eng, lp, "fp64", peak, f.staged_fraction)
         fp64 = {"seconds": f.device_seconds, "iterations": f.iterations, "status": f.status_name,
                 "objective": f.objective,
                 "relative_kkt": max(f.residuals["primal"], f.residuals["dual"],
@@ -277,6 +363,8 @@ def main():
         step_s, e2e_s = float(t[0]), float(t[1])
     if rank != 0:
         return
+
+    batched = None if args.no_batch else batched_section(local)
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -311,6 +399,7 @@ def main():
         "fp64": fp64,
         "spmv_gbs": roof,
         "lps_per_s": world / step_s,
+        "batched": batched,
         "roofline": {"bound": "hbm", "kernel": f"{dominant}{suffix}: {kname}",
                      "achieved": roof[dominant + "_gbs"], "peak": peak, "unit": "GB/s",
                      "frac": roof[dominant + "_gbs"] / peak, "traffic": traffic,

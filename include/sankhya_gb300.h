@@ -144,6 +144,9 @@ typedef struct sankhya_gb300_result {
   double solve_seconds;  /* the whole solve call, host clock */
   double device_seconds; /* the whole solve, CUDA events on the engine's stream */
   int64_t kernel_launches; /* engine kernels launched by this solve (graph nodes included) */
+  /* Share of the nonzeros whose gathered element the step pass of this precision reads from
+   * a staged shared-memory window rather than global memory: [0] column pass, [1] row pass. */
+  double staged_fraction[2];
   char message[512];
 } sankhya_gb300_result;
 
@@ -218,6 +221,44 @@ SGB_API int sankhya_gb300_pdhg_spmv_noalloc(sankhya_gb300_pdhg* engine, int32_t 
  * solve's results are restored afterwards. */
 SGB_API int sankhya_gb300_pdhg_time_kernels(sankhya_gb300_pdhg* engine, int32_t reps,
                                             double* ms);
+
+/* ---- Batched solves ------------------------------------------------------------------------
+ * Many LPs solved together on one device, each by one thread block in one persistent launch,
+ * with its own step size, primal weight, restart state and stopping test: the reference's
+ * PDHG (src/pdhg/pdhg.cpp), per LP, as solve_pdhg runs it. No reference counterpart: it is
+ * the batched engine of the branch-and-bound node relaxations (the reference solves those
+ * one at a time, src/mip/branch_and_bound_node.cpp) and of many small LPs. LPs whose
+ * col_starts / row_index / values pointers and sizes are equal share one device copy of the
+ * matrix (scaled and norm-estimated once). An LP whose dual iterate drifts along a Farkas ray
+ * is reported SANKHYA_GB300_INFEASIBLE. Options: tolerance, iteration_limit, restart,
+ * stop_at_request, random_seed, stop_rule; precision must be SANKHYA_GB300_FP64;
+ * time_limit, interrupt, log and poll are not used. */
+typedef struct sankhya_gb300_batch sankhya_gb300_batch;
+
+typedef struct sankhya_gb300_batch_item {
+  int32_t status; /* SANKHYA_GB300_OPTIMAL, FEASIBLE, INFEASIBLE or ITERATION_LIMIT */
+  int32_t converged;
+  int64_t iterations, attempts, restarts, evaluations;
+  double objective;  /* objective_offset + col_cost . x at the reported point */
+  double dual_bound; /* only when optimal, else -+inf */
+  sankhya_gb300_residuals final_residuals;
+  double spectral_norm;
+  double farkas_value; /* infeasible: the certificate's value over its terms' magnitude */
+} sankhya_gb300_batch_item;
+
+SGB_API int sankhya_gb300_batch_create(int32_t device, sankhya_gb300_batch** batch);
+SGB_API int sankhya_gb300_batch_destroy(sankhya_gb300_batch* batch);
+SGB_API int sankhya_gb300_batch_load(sankhya_gb300_batch* batch, int32_t count,
+                                     const sankhya_gb300_lp* lps);
+/* items has `count` entries; device_seconds (may be NULL) receives the solve's device time
+ * (CUDA events around the two launches). */
+SGB_API int sankhya_gb300_batch_solve(sankhya_gb300_batch* batch,
+                                      const sankhya_gb300_params* params,
+                                      sankhya_gb300_batch_item* items, double* device_seconds);
+/* The reported point of LP `index`, as sankhya_gb300_pdhg_solution. */
+SGB_API int sankhya_gb300_batch_solution(sankhya_gb300_batch* batch, int32_t index,
+                                         double* col_value, double* col_dual,
+                                         double* row_dual);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,363 @@
+// batch.cu -- BatchEngine: packs the LPs of a batch into device arrays (one copy per distinct
+// matrix) and runs the scaling and solve launches of batch_kernels.cu.
+#include "batch_engine.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <numeric>
+#include <random>
+#include <tuple>
+
+namespace sgb {
+
+namespace {
+
+bool finite_bound_host(double v) { return !(std::isinf(v) || std::fabs(v) >= 1e30); }
+
+}  // namespace
+
+BatchEngine::BatchEngine(int device) : device_(device) {
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+    cudaGetLastError();
+    throw EngineError{SANKHYA_GB300_ERROR_DEVICE, "no CUDA device is available"};
+  }
+  if (device < 0 || device >= count) {
+    throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no such device"};
+  }
+  SGB_CUDA(cudaSetDevice(device));
+  SGB_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  SGB_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device));
+  SGB_CUDA(cudaEventCreate(&timing_[0]));
+  SGB_CUDA(cudaEventCreate(&timing_[1]));
+}
+
+BatchEngine::~BatchEngine() {
+  cudaSetDevice(device_);
+  for (cudaEvent_t e : timing_) {
+    if (e != nullptr) cudaEventDestroy(e);
+  }
+  if (stream_ != nullptr) cudaStreamDestroy(stream_);
+}
+
+void BatchEngine::require_loaded() const {
+  if (count_ == 0) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no LPs are loaded"};
+}
+
+void BatchEngine::load(int count, const sankhya_gb300_lp* lps) {
+  if (count <= 0 || lps == nullptr) {
+    throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "a batch needs at least one LP"};
+  }
+  for (int k = 0; k < count; ++k) validate_lp(lps[k]);
+  SGB_CUDA(cudaSetDevice(device_));
+  count_ = 0;
+  solved_ = false;
+  mats_.clear();
+  inst_.clear();
+
+  // Distinct matrices, by identity of the caller's arrays.
+  using Key = std::tuple<const int32_t*, const int32_t*, const double*, int, int>;
+  std::map<Key, int> seen;
+  std::vector<int> first_lp;  // an LP holding each distinct matrix
+  std::vector<int> mat_of(static_cast<size_t>(count));
+  for (int k = 0; k < count; ++k) {
+    const sankhya_gb300_lp& lp = lps[k];
+    const Key key{lp.col_starts, lp.row_index, lp.values, lp.rows, lp.cols};
+    auto it = seen.find(key);
+    if (it == seen.end()) {
+      it = seen.emplace(key, static_cast<int>(first_lp.size())).first;
+      first_lp.push_back(k);
+    }
+    mat_of[static_cast<size_t>(k)] = it->second;
+  }
+
+  // Matrices: CSC as given, CSR by the counting-sort transpose (src/la/sparse.cpp:271-302).
+  std::vector<int> cptr, cidx, rptr, ridx;
+  std::vector<double> cval, rval;
+  long long nz = 0, cp = 0, rp = 0;
+  mat_n_ = mat_m_ = 0;
+  for (int lpk : first_lp) {
+    const sankhya_gb300_lp& lp = lps[lpk];
+    const int m = lp.rows, n = lp.cols;
+    const long long nnz = lp.col_starts[n];
+    BatchMatrix M{};
+    M.m = m;
+    M.n = n;
+    M.cptr = cp;
+    M.rptr = rp;
+    M.col = mat_n_;
+    M.row = mat_m_;
+    M.nz = nz;
+    M.nnz = nnz;
+    M.spectral_norm = 1.0;
+    mats_.push_back(M);
+    cptr.insert(cptr.end(), lp.col_starts, lp.col_starts + n + 1);
+    cidx.insert(cidx.end(), lp.row_index, lp.row_index + nnz);
+    cval.insert(cval.end(), lp.values, lp.values + nnz);
+    std::vector<int> r(static_cast<size_t>(m) + 1, 0);
+    for (long long k = 0; k < nnz; ++k) ++r[static_cast<size_t>(lp.row_index[k]) + 1];
+    for (int i = 0; i < m; ++i) r[i + 1] += r[i];
+    std::vector<int> next(r.begin(), r.end() - 1);
+    const size_t base = ridx.size();
+    ridx.resize(base + static_cast<size_t>(nnz));
+    rval.resize(base + static_cast<size_t>(nnz));
+    for (int j = 0; j < n; ++j) {
+      for (int k = lp.col_starts[j]; k < lp.col_starts[j + 1]; ++k) {
+        const int slot = next[lp.row_index[k]]++;
+        ridx[base + slot] = j;
+        rval[base + slot] = lp.values[k];
+      }
+    }
+    rptr.insert(rptr.end(), r.begin(), r.end());
+    nz += nnz;
+    cp += n + 1;
+    rp += m + 1;
+    mat_n_ += n;
+    mat_m_ += m;
+  }
+
+  // LPs: their vectors, in the minimise-space of src/pdhg/pdhg.cpp:95-111.
+  std::vector<double> cost, col_cost, l, u, rl, ru;
+  total_n_ = total_m_ = 0;
+  for (int k = 0; k < count; ++k) {
+    const sankhya_gb300_lp& lp = lps[k];
+    const int m = lp.rows, n = lp.cols;
+    const double sense = lp.sense < 0.0 ? -1.0 : 1.0;
+    BatchInstance I{};
+    I.matrix = mat_of[static_cast<size_t>(k)];
+    I.m = m;
+    I.n = n;
+    I.col = total_n_;
+    I.row = total_m_;
+    I.sense = sense;
+    I.offset = lp.objective_offset;
+    double cost_sq = 0.0, bound_sq = 0.0;
+    for (int j = 0; j < n; ++j) {
+      const double c = sense * lp.col_cost[j];
+      cost.push_back(c);
+      cost_sq += c * c;
+    }
+    for (int i = 0; i < m; ++i) {
+      const double b = finite_bound_host(lp.row_lower[i])
+                           ? lp.row_lower[i]
+                           : (finite_bound_host(lp.row_upper[i]) ? lp.row_upper[i] : 0.0);
+      bound_sq += b * b;
+    }
+    I.cost_norm = std::sqrt(cost_sq);
+    I.bound_norm = std::sqrt(bound_sq);
+    col_cost.insert(col_cost.end(), lp.col_cost, lp.col_cost + n);
+    l.insert(l.end(), lp.col_lower, lp.col_lower + n);
+    u.insert(u.end(), lp.col_upper, lp.col_upper + n);
+    rl.insert(rl.end(), lp.row_lower, lp.row_lower + m);
+    ru.insert(ru.end(), lp.row_upper, lp.row_upper + m);
+    inst_.push_back(I);
+    total_n_ += n;
+    total_m_ += m;
+  }
+  // Largest LPs first, so the last blocks to finish hold small ones.
+  std::vector<int> order(static_cast<size_t>(count));
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    const BatchMatrix& ma = mats_[static_cast<size_t>(inst_[a].matrix)];
+    const BatchMatrix& mb = mats_[static_cast<size_t>(inst_[b].matrix)];
+    return ma.nnz + ma.m + ma.n > mb.nnz + mb.m + mb.n;
+  });
+
+  cudaStream_t s = stream_;
+  const size_t N = static_cast<size_t>(std::max(total_n_, 1LL));
+  const size_t M = static_cast<size_t>(std::max(total_m_, 1LL));
+  d_mats_.upload(mats_.data(), mats_.size(), s);
+  d_mats_out_.upload(mats_.data(), mats_.size(), s);
+  d_inst_.upload(inst_.data(), inst_.size(), s);
+  d_order_.upload(order.data(), order.size(), s);
+  d_queue_.allocate(4);
+  csc_ptr_.upload(cptr.data(), cptr.size(), s);
+  csc_idx_.upload(cidx.data(), cidx.size(), s);
+  csc_raw_.upload(cval.data(), cval.size(), s);
+  csr_ptr_.upload(rptr.data(), rptr.size(), s);
+  csr_idx_.upload(ridx.data(), ridx.size(), s);
+  csr_raw_.upload(rval.data(), rval.size(), s);
+  csc_s_.allocate(std::max<size_t>(cval.size(), 1));
+  csr_s_.allocate(std::max<size_t>(rval.size(), 1));
+  for (DeviceArray<double>* a : {&dc_, &col_acc_, &power_v_}) {
+    a->allocate(static_cast<size_t>(std::max(mat_n_, 1LL)));
+  }
+  for (DeviceArray<double>* a : {&dr_, &row_acc_, &power_av_}) {
+    a->allocate(static_cast<size_t>(std::max(mat_m_, 1LL)));
+  }
+  cost_.upload(cost.data(), cost.size(), s);
+  col_cost_.upload(col_cost.data(), col_cost.size(), s);
+  l_.upload(l.data(), l.size(), s);
+  u_.upload(u.data(), u.size(), s);
+  rl_.upload(rl.data(), rl.size(), s);
+  ru_.upload(ru.data(), ru.size(), s);
+  for (DeviceArray<double>* a : {&cs_, &ls_, &us_, &x0_, &x1_, &x_sum_, &x_rst_, &xu0_, &xu1_,
+                                 &best_x_, &reduced_}) {
+    a->allocate(N);
+  }
+  xd_.allocate(N);
+  for (DeviceArray<double>* a : {&rls_, &rus_, &y0_, &y1_, &y_sum_, &y_rst_, &yu0_, &yu1_,
+                                 &best_y_, &ray_}) {
+    a->allocate(M);
+  }
+  outcome_.allocate(static_cast<size_t>(count));
+  SGB_CUDA(cudaStreamSynchronize(s));
+  count_ = count;
+}
+
+void BatchEngine::solve(const sankhya_gb300_params& p, sankhya_gb300_batch_item* items,
+                        double* device_seconds) {
+  require_loaded();
+  if (p.precision != SANKHYA_GB300_FP64) {
+    throw EngineError{SANKHYA_GB300_ERROR_OPTION, "batched solves run the FP64 method"};
+  }
+  SGB_CUDA(cudaSetDevice(device_));
+  cudaStream_t s = stream_;
+  // The power iteration's start vectors: the reference's std::mt19937(seed + 1) stream with
+  // uniform_real_distribution(-1, 1) (src/la/scaling.cpp:168-170), one per matrix.
+  std::vector<double> v0(static_cast<size_t>(std::max(mat_n_, 1LL)));
+  for (const BatchMatrix& M : mats_) {
+    std::mt19937 rng(static_cast<unsigned>(p.random_seed) + 1u);
+    std::uniform_real_distribution<double> spread(-1.0, 1.0);
+    for (int j = 0; j < M.n; ++j) v0[static_cast<size_t>(M.col + j)] = spread(rng);
+  }
+  if (mat_n_ > 0) {
+    SGB_CUDA(cudaMemcpyAsync(power_v_.ptr, v0.data(), static_cast<size_t>(mat_n_) * sizeof(double),
+                             cudaMemcpyHostToDevice, s));
+  }
+  SGB_CUDA(cudaMemsetAsync(d_queue_.ptr, 0, 4 * sizeof(unsigned int), s));
+
+  BatchBuffers b{};
+  b.nmatrices = static_cast<int>(mats_.size());
+  b.ninstances = count_;
+  b.matrices = d_mats_.ptr;
+  b.matrices_out = d_mats_out_.ptr;
+  b.instances = d_inst_.ptr;
+  b.order = d_order_.ptr;
+  b.queue = d_queue_.ptr;
+  b.csc_ptr = csc_ptr_.ptr;
+  b.csc_idx = csc_idx_.ptr;
+  b.csr_ptr = csr_ptr_.ptr;
+  b.csr_idx = csr_idx_.ptr;
+  b.csc_raw = csc_raw_.ptr;
+  b.csr_raw = csr_raw_.ptr;
+  b.csc_s = csc_s_.ptr;
+  b.csr_s = csr_s_.ptr;
+  b.dr = dr_.ptr;
+  b.dc = dc_.ptr;
+  b.row_acc = row_acc_.ptr;
+  b.col_acc = col_acc_.ptr;
+  b.power_v = power_v_.ptr;
+  b.power_av = power_av_.ptr;
+  b.cost = cost_.ptr;
+  b.col_cost = col_cost_.ptr;
+  b.l = l_.ptr;
+  b.u = u_.ptr;
+  b.rl = rl_.ptr;
+  b.ru = ru_.ptr;
+  b.cs = cs_.ptr;
+  b.ls = ls_.ptr;
+  b.us = us_.ptr;
+  b.rls = rls_.ptr;
+  b.rus = rus_.ptr;
+  b.x0 = x0_.ptr;
+  b.x1 = x1_.ptr;
+  b.x_sum = x_sum_.ptr;
+  b.x_rst = x_rst_.ptr;
+  b.xu0 = xu0_.ptr;
+  b.xu1 = xu1_.ptr;
+  b.best_x = best_x_.ptr;
+  b.reduced = reduced_.ptr;
+  b.xd = xd_.ptr;
+  b.y0 = y0_.ptr;
+  b.y1 = y1_.ptr;
+  b.y_sum = y_sum_.ptr;
+  b.y_rst = y_rst_.ptr;
+  b.yu0 = yu0_.ptr;
+  b.yu1 = yu1_.ptr;
+  b.best_y = best_y_.ptr;
+  b.ray = ray_.ptr;
+  b.outcome = outcome_.ptr;
+  b.tolerance = p.tolerance;
+  b.iteration_limit = p.iteration_limit < 0 ? 1000000 : p.iteration_limit;
+  b.use_restarts = p.restart != 0;
+  b.stop_at_request = p.stop_at_request != 0;
+  b.stop_rule = p.stop_rule == SANKHYA_GB300_STOP_RELATIVE ? 1 : 0;
+  b.detect_infeasibility = 1;
+
+  SGB_CUDA(cudaEventRecord(timing_[0], s));
+  const int scale_grid = std::max(1, std::min(b.nmatrices, num_sms_ * 8));
+  launch_batch_scaling(b, scale_grid, s);
+  const int solve_grid = std::max(1, std::min(count_, num_sms_ * batch_blocks_per_sm()));
+  launch_batch_solve(b, solve_grid, s);
+  SGB_CUDA(cudaGetLastError());
+  SGB_CUDA(cudaEventRecord(timing_[1], s));
+  std::vector<BatchOutcome> out(static_cast<size_t>(count_));
+  std::vector<BatchMatrix> mats(mats_.size());
+  SGB_CUDA(cudaMemcpyAsync(out.data(), outcome_.ptr, out.size() * sizeof(BatchOutcome),
+                           cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaMemcpyAsync(mats.data(), d_mats_out_.ptr, mats.size() * sizeof(BatchMatrix),
+                           cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.0f;
+  SGB_CUDA(cudaEventElapsedTime(&ms, timing_[0], timing_[1]));
+  if (device_seconds != nullptr) *device_seconds = 1e-3 * ms;
+  for (int k = 0; k < count_; ++k) {
+    const BatchOutcome& o = out[static_cast<size_t>(k)];
+    sankhya_gb300_batch_item& it = items[k];
+    it.status = o.status;
+    it.converged = o.converged;
+    it.iterations = o.iterations;
+    it.attempts = o.attempts;
+    it.restarts = o.restarts;
+    it.evaluations = o.evaluations;
+    it.objective = o.objective;
+    it.dual_bound = o.dual_bound;
+    const Residuals& f = o.final_residuals;
+    it.final_residuals = sankhya_gb300_residuals{f.primal,          f.dual,           f.gap,
+                                                 f.primal_objective, f.dual_objective,
+                                                 f.absolute_primal,  f.absolute_dual,
+                                                 f.gap_as_verified,  f.complementarity};
+    it.spectral_norm = mats[static_cast<size_t>(inst_[static_cast<size_t>(k)].matrix)].spectral_norm;
+    it.farkas_value = o.farkas_value;
+  }
+  solved_ = true;
+}
+
+void BatchEngine::solution(int index, double* col_value, double* col_dual, double* row_dual) {
+  require_loaded();
+  if (!solved_) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no solve has run"};
+  if (index < 0 || index >= count_) {
+    throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no such LP in the batch"};
+  }
+  SGB_CUDA(cudaSetDevice(device_));
+  cudaStream_t s = stream_;
+  const BatchInstance& I = inst_[static_cast<size_t>(index)];
+  const size_t n = static_cast<size_t>(I.n), m = static_cast<size_t>(I.m);
+  std::vector<double> red(n), by(m);
+  if (col_value && n > 0) {
+    SGB_CUDA(cudaMemcpyAsync(col_value, best_x_.ptr + I.col, n * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+  }
+  if (n > 0) {
+    SGB_CUDA(cudaMemcpyAsync(red.data(), reduced_.ptr + I.col, n * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+  }
+  if (m > 0) {
+    SGB_CUDA(cudaMemcpyAsync(by.data(), best_y_.ptr + I.row, m * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+  }
+  SGB_CUDA(cudaStreamSynchronize(s));
+  if (col_dual) {
+    for (size_t j = 0; j < n; ++j) col_dual[j] = I.sense * red[j];
+  }
+  if (row_dual) {
+    for (size_t i = 0; i < m; ++i) row_dual[i] = I.sense * (-by[i]);
+  }
+}
+
+}  // namespace sgb

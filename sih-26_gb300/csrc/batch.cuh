@@ -1,0 +1,91 @@
+// batch.cuh -- many LPs in one persistent launch.
+//
+// A batch is a list of LPs, each solved by ONE thread block from start to finish: the block
+// takes the next LP from a queue (largest first), runs the reference's restarted PDHG on it
+// -- the same steps, step-size rule, evaluations, restarts and stopping tests as the
+// single-LP engine (src/pdhg/pdhg.cpp:76-567), written for one block with block-wide
+// deterministic reductions -- and takes the next LP when it is done. Every LP keeps its own
+// step size, primal weight, restart anchor and counters (its own Ctl), so thousands of LPs of
+// uneven sizes and iteration counts share the GPU with no host round trip per iteration.
+//
+// LPs may share their constraint matrix (branch-and-bound node relaxations differ only in
+// their bounds): the matrix is stored, scaled and its norm estimated once, by a first
+// persistent launch over the distinct matrices, and the LPs keep only their own vectors.
+//
+// An LP whose iterates drift along a dual ray is reported infeasible: at every evaluation
+// the change of the dual iterate since the restart anchor, d, is tested as a Farkas
+// certificate of the unscaled problem (min over the box of (A^T d)'x minus the support of
+// the row box along d must be positive); see batch_farkas in batch_kernels.cu.
+#pragma once
+
+#include "kernels.cuh"
+
+namespace sgb {
+
+constexpr int kBatchThreads = 256;
+
+// A distinct constraint matrix. Offsets index the packed arrays of BatchBuffers.
+struct BatchMatrix {
+  int m, n;
+  long long cptr;  // offset of its n + 1 column starts (relative to its own entries)
+  long long rptr;  // offset of its m + 1 row starts
+  long long col;   // offset of its n-vectors (Dc, column scratch, power vector)
+  long long row;   // offset of its m-vectors (Dr, row scratch)
+  long long nz;    // offset of its entries in the packed index / value arrays
+  long long nnz;
+  double spectral_norm;  // written by the scaling launch
+  double scaled_min_abs, scaled_max_abs;
+};
+
+// One LP of the batch.
+struct BatchInstance {
+  int matrix;
+  int m, n;
+  long long col;  // offset of its n-vectors
+  long long row;  // offset of its m-vectors
+  double sense, offset;
+  double bound_norm, cost_norm;  // of the unscaled minimise-space problem
+};
+
+// What the block leaves for the host, per LP.
+struct BatchOutcome {
+  int status;     // SANKHYA_GB300_* solve status
+  int converged;
+  long long iterations, attempts, restarts, evaluations;
+  double objective, dual_bound;
+  Residuals final_residuals;
+  double farkas_value;  // the certificate's normalised value when status is infeasible
+  int error;            // nonzero: a device-side inconsistency (reported as an error)
+};
+
+struct BatchBuffers {
+  int nmatrices, ninstances;
+  const BatchMatrix* matrices;
+  BatchMatrix* matrices_out;  // spectral norms written by the scaling launch
+  const BatchInstance* instances;
+  const int* order;           // instance solve order (largest first)
+  unsigned int* queue;        // [0] next matrix, [1] next instance (reset by the host)
+  // Matrix arrays (offsets from BatchMatrix).
+  const int *csc_ptr, *csc_idx, *csr_ptr, *csr_idx;
+  const double *csc_raw, *csr_raw;
+  double *csc_s, *csr_s;
+  double *dr, *dc, *row_acc, *col_acc, *power_v, *power_av;
+  // LP arrays (offsets from BatchInstance).
+  const double *cost, *col_cost, *l, *u, *rl, *ru;  // unscaled, minimise-space cost
+  double *cs, *ls, *us, *rls, *rus;                  // scaled
+  double *x0, *x1, *x_sum, *x_rst, *xu0, *xu1, *best_x, *reduced;
+  double2* xd;
+  double *y0, *y1, *y_sum, *y_rst, *yu0, *yu1, *best_y;
+  double* ray;  // the unscaled dual change tested as a Farkas certificate (m per LP)
+  BatchOutcome* outcome;
+  // Options.
+  double tolerance;
+  long long iteration_limit;
+  int use_restarts, stop_at_request, stop_rule, detect_infeasibility;
+};
+
+void launch_batch_scaling(const BatchBuffers& b, int grid, cudaStream_t s);
+void launch_batch_solve(const BatchBuffers& b, int grid, cudaStream_t s);
+int batch_blocks_per_sm();
+
+}  // namespace sgb

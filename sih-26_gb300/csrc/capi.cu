@@ -11,11 +11,16 @@
 #include <new>
 #include <string>
 
+#include "batch_engine.hpp"
 #include "engine.hpp"
 #include "sankhya_gb300.h"
 
 struct sankhya_gb300_pdhg {
   sgb::Engine* engine;
+};
+
+struct sankhya_gb300_batch {
+  sgb::BatchEngine* engine;
 };
 
 namespace {
@@ -174,6 +179,47 @@ SGB_API int sankhya_gb300_pdhg_time_kernels(sankhya_gb300_pdhg* engine, int32_t 
     return fail(SANKHYA_GB300_ERROR_ARGUMENT, "bad time_kernels arguments");
   }
   return guarded([&] { engine->engine->time_kernels(reps, ms); });
+}
+
+SGB_API int sankhya_gb300_batch_create(int32_t device, sankhya_gb300_batch** out) {
+  if (out == nullptr) return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null output handle");
+  *out = nullptr;
+  return guarded([&] {
+    sgb::BatchEngine* e = new sgb::BatchEngine(device);
+    *out = new sankhya_gb300_batch{e};
+  });
+}
+
+SGB_API int sankhya_gb300_batch_destroy(sankhya_gb300_batch* batch) {
+  if (batch == nullptr) return SANKHYA_GB300_OK;
+  return guarded([&] {
+    delete batch->engine;
+    delete batch;
+  });
+}
+
+SGB_API int sankhya_gb300_batch_load(sankhya_gb300_batch* batch, int32_t count,
+                                     const sankhya_gb300_lp* lps) {
+  if (batch == nullptr || lps == nullptr || count <= 0) {
+    return fail(SANKHYA_GB300_ERROR_ARGUMENT, "bad batch_load arguments");
+  }
+  return guarded([&] { batch->engine->load(count, lps); });
+}
+
+SGB_API int sankhya_gb300_batch_solve(sankhya_gb300_batch* batch,
+                                      const sankhya_gb300_params* params,
+                                      sankhya_gb300_batch_item* items, double* device_seconds) {
+  if (batch == nullptr || params == nullptr || items == nullptr) {
+    return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null argument");
+  }
+  return guarded([&] { batch->engine->solve(*params, items, device_seconds); });
+}
+
+SGB_API int sankhya_gb300_batch_solution(sankhya_gb300_batch* batch, int32_t index,
+                                         double* col_value, double* col_dual,
+                                         double* row_dual) {
+  if (batch == nullptr) return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null batch");
+  return guarded([&] { batch->engine->solution(index, col_value, col_dual, row_dual); });
 }
 
 }  // extern "C"

@@ -14,6 +14,8 @@
 // SolveControl interrupt flag, at every snapshot (every `steps_per_poll` steps).
 #include "engine.hpp"
 
+#include "batch.cuh"
+
 #include <algorithm>
 #include <cstdarg>
 #include <cstddef>
@@ -21,8 +23,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <limits>
 #include <random>
+#include <thread>
 
 namespace sgb {
 
@@ -74,6 +78,9 @@ template struct DeviceArray<unsigned int>;
 template struct DeviceArray<double>;
 template struct DeviceArray<float>;
 template struct DeviceArray<Ctl>;
+template struct DeviceArray<BatchMatrix>;
+template struct DeviceArray<BatchInstance>;
+template struct DeviceArray<BatchOutcome>;
 
 namespace {
 
@@ -86,15 +93,15 @@ bool finite_bound_host(double v) { return !(std::isinf(v) || std::fabs(v) >= 1e3
 
 }  // namespace
 
-// Greedy row tiles: consecutive rows while the tile has at most kTileThreads rows and at
-// most kCap nonzeros; a row longer than kCap becomes chunk tiles of kCap entries each,
+// Greedy row tiles: consecutive rows while the tile has at most min(kMaxTileRows,
+// threads / lanes) rows and at most kCap nonzeros; a row longer than kCap becomes chunk tiles of kCap entries each,
 // listed as a LongRow so its chunk partials can be combined in chunk order.
-void build_tiles(const std::vector<int>& ptr, int lines, int lanes, std::vector<Tile>* tiles,
-                 std::vector<LongRow>* longs, int* nchunks) {
+void build_tiles(const std::vector<int>& ptr, int lines, int lanes, int threads,
+                 std::vector<Tile>* tiles, std::vector<LongRow>* longs, int* nchunks) {
   tiles->clear();
   longs->clear();
   *nchunks = 0;
-  const int max_rows = kTileThreads / lanes;
+  const int max_rows = std::min(kMaxTileRows, threads / lanes);
   int r = 0;
   while (r < lines) {
     const int len = ptr[r + 1] - ptr[r];
@@ -118,6 +125,107 @@ void build_tiles(const std::vector<int>& ptr, int lines, int lanes, std::vector<
     }
     tiles->push_back(Tile{begin, r, ptr[begin], ptr[r]});
   }
+}
+
+// Windows: first every tile's own best range -- the start lo for which [lo, lo + wmax) holds
+// the most of the tile's entries, centred among the starts that do and rounded down to a
+// multiple of 4 -- computed on all host threads (tiles are independent). Then, in tile
+// order, a tile joins the current window when its own best start lies within wmax / 16 of
+// the window's; otherwise it opens a new window at its own best start. A tile with fewer
+// than 1/8 of its entries in its best range gathers from global memory. A window whose tiles
+// would gather fewer than wmax / 32 entries from it is dropped: staging costs one bulk copy
+// of the whole window, about a thirty-second of a random gather per element.
+long long build_windows(const std::vector<Tile>& tiles, const int* idx, int extent, int wmax,
+                        std::vector<int>* tile_win, std::vector<int2>* windows) {
+  const int ntiles = static_cast<int>(tiles.size());
+  tile_win->assign(static_cast<size_t>(ntiles), -1);
+  windows->clear();
+  if (wmax <= 0 || ntiles == 0 || extent <= 0) return 0;
+  const int ext4 = (extent + 3) & ~3;
+  if (ext4 <= wmax) {  // the whole vector fits: one window for every tile
+    windows->push_back(make_int2(0, ext4));
+    tile_win->assign(static_cast<size_t>(ntiles), 0);
+    long long all = 0;
+    for (const Tile& t : tiles) all += t.k1 - t.k0;
+    return all;
+  }
+  std::vector<int> best_lo(static_cast<size_t>(ntiles)), best_count(static_cast<size_t>(ntiles));
+  const auto scan = [&](int t0, int t1) {
+    std::vector<int> v;
+    for (int t = t0; t < t1; ++t) {
+      const Tile& tile = tiles[static_cast<size_t>(t)];
+      v.assign(idx + tile.k0, idx + tile.k1);
+      std::sort(v.begin(), v.end());
+      int best = 0, bl = 0, br = 0;
+      for (int r = 0, l = 0; r < static_cast<int>(v.size()); ++r) {
+        while (v[r] - v[l] >= wmax) ++l;
+        if (r - l + 1 > best) {
+          best = r - l + 1;
+          bl = l;
+          br = r;
+        }
+      }
+      long long lo = 0;
+      if (best > 0) {
+        const long long lo_min = static_cast<long long>(v[br]) - wmax + 1, lo_max = v[bl];
+        lo = lo_min + (lo_max - lo_min) / 2;
+      }
+      lo = std::max(0LL, std::min(lo, static_cast<long long>(ext4 - wmax)));
+      best_lo[static_cast<size_t>(t)] = static_cast<int>(lo) & ~3;
+      best_count[static_cast<size_t>(t)] = best;
+    }
+  };
+  const int workers = std::max(1, std::min<int>(16, static_cast<int>(std::thread::hardware_concurrency())));
+  if (workers == 1 || ntiles < 64) {
+    scan(0, ntiles);
+  } else {
+    std::vector<std::thread> pool;
+    for (int w = 0; w < workers; ++w) {
+      const int t0 = static_cast<int>(static_cast<long long>(ntiles) * w / workers);
+      const int t1 = static_cast<int>(static_cast<long long>(ntiles) * (w + 1) / workers);
+      pool.emplace_back(scan, t0, t1);
+    }
+    for (auto& th : pool) th.join();
+  }
+  std::vector<long long> used;  // entries each window serves (its tiles' best counts)
+  int current = -1;
+  for (int t = 0; t < ntiles; ++t) {
+    const Tile& tile = tiles[static_cast<size_t>(t)];
+    const int entries = tile.k1 - tile.k0;
+    const int best = best_count[static_cast<size_t>(t)];
+    if (entries == 0 || best * 8 < entries) continue;
+    const int lo = best_lo[static_cast<size_t>(t)];
+    if (current < 0 || std::abs(lo - (*windows)[static_cast<size_t>(current)].x) > wmax / 16) {
+      windows->push_back(make_int2(lo, wmax));
+      used.push_back(0);
+      current = static_cast<int>(windows->size()) - 1;
+    }
+    (*tile_win)[static_cast<size_t>(t)] = current;
+    used[static_cast<size_t>(current)] += best;
+  }
+  // Drop windows that do not pay for their staging, renumbering the rest.
+  std::vector<int> remap(windows->size(), -1);
+  std::vector<int2> kept;
+  for (size_t w = 0; w < windows->size(); ++w) {
+    if (used[w] * 32 >= wmax) {
+      remap[w] = static_cast<int>(kept.size());
+      kept.push_back((*windows)[w]);
+    }
+  }
+  for (int& w : *tile_win) {
+    if (w >= 0) w = remap[static_cast<size_t>(w)];
+  }
+  windows->swap(kept);
+  long long covered = 0;
+  for (int t = 0; t < ntiles; ++t) {
+    const int w = (*tile_win)[static_cast<size_t>(t)];
+    if (w < 0) continue;
+    const int2 r = (*windows)[static_cast<size_t>(w)];
+    for (int k = tiles[static_cast<size_t>(t)].k0; k < tiles[static_cast<size_t>(t)].k1; ++k) {
+      covered += static_cast<unsigned>(idx[k] - r.x) < static_cast<unsigned>(r.y);
+    }
+  }
+  return covered;
 }
 
 namespace {
@@ -163,6 +271,7 @@ Engine::Engine(int device) : device_(device) {
   }
   SGB_CUDA(cudaSetDevice(device));
   SGB_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  SGB_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
   SGB_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device));
   SGB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&snapshot_), 2 * sizeof(Ctl),
                          cudaHostAllocDefault));
@@ -189,6 +298,7 @@ Engine::~Engine() {
   }
   if (snapshot_ != nullptr) cudaFreeHost(snapshot_);
   if (snapshot_mixed_ != nullptr) cudaFreeHost(snapshot_mixed_);
+  if (capture_stream_ != nullptr) cudaStreamDestroy(capture_stream_);
   if (stream_ != nullptr) cudaStreamDestroy(stream_);
 }
 
@@ -213,15 +323,15 @@ void Engine::allocate_mixed() {
   const size_t m = static_cast<size_t>(m_);
   csc_f_.allocate_padded(z, kPad, s);
   csr_f_.allocate_padded(z, kPad, s);
+  // kPad elements of padding, as for the FP64 vectors (staged slices and windows).
   for (DeviceArray<float>* a : {&u0f_, &u1f_, &usumf_, &urstf_, &cf_, &lf_, &uf_, &uc0_, &uc1_,
-                                &ubest_, &csf_}) {
-    a->allocate(n);
+                                &ubest_, &csf_, &ubarf_}) {
+    a->allocate(n + kPad);
   }
   for (DeviceArray<float>* a : {&v0f_, &v1f_, &vsumf_, &vrstf_, &gu_, &gl_, &yhat_, &vc0_, &vc1_,
-                                &vbest_}) {
-    a->allocate(m);
+                                &vbest_, &auf0_, &auf1_}) {
+    a->allocate(m + kPad);
   }
-  udf_.allocate(n);
   for (DeviceArray<double>* a : {&anchor_x_, &aty64_}) a->allocate(n);
   for (DeviceArray<double>* a : {&anchor_y_, &ax64_}) a->allocate(m);
   fill_mixed_buffers();
@@ -245,7 +355,9 @@ void Engine::fill_mixed_buffers() {
   b.v_sum = vsumf_.ptr;
   b.u_rst = urstf_.ptr;
   b.v_rst = vrstf_.ptr;
-  b.ud = udf_.ptr;
+  b.ubar = ubarf_.ptr;
+  b.au[0] = auf0_.ptr;
+  b.au[1] = auf1_.ptr;
   b.cf = cf_.ptr;
   b.lf = lf_.ptr;
   b.uf = uf_.ptr;
@@ -268,8 +380,18 @@ void Engine::fill_mixed_buffers() {
   b.part_rows1 = part_rows1_.ptr;
   b.chunk_cols = chunk_cols_.ptr;
   b.chunk_rows = chunk_rows_.ptr;
+  b.csc.tile_win = step_csc_f_.tile_win.ptr;
+  b.csc.windows = step_csc_f_.windows.ptr;
+  b.csc.wmax = step_csc_f_.wmax;
+  b.csr.tile_win = step_csr_f_.tile_win.ptr;
+  b.csr.windows = step_csr_f_.windows.ptr;
+  b.csr.wmax = step_csr_f_.wmax;
   b.grid_primal = grid_csc_f_;
   b.grid_dual = grid_csr_f_;
+  b.grid_step_primal = step_csc_f_.grid;
+  b.grid_step_dual = step_csr_f_.grid;
+  b.smem_primal = step_csc_f_.smem;
+  b.smem_dual = step_csr_f_.smem;
   b.m = m_;
   b.n = n_;
 }
@@ -284,8 +406,11 @@ void Engine::build_mixed_graphs(int steps) {
     cudaGraph_t graph = nullptr;
     SGB_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < steps; ++k) {
-      launch_mixed_step(mixed_, stream_);
-      launch_mixed_evaluation(mixed_, stream_);
+      MixedBuffers mb = mixed_;
+      mb.cond = step_condition();
+      mb.use_cond = 1;
+      launch_mixed_step(mb, stream_);
+      capture_if(mb.cond, [&](cudaStream_t cs) { launch_mixed_evaluation(mixed_, cs); });
     }
     cudaMemcpyAsync(snapshot_mixed_ + slot, ctl_mixed_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost,
                     stream_);
@@ -302,7 +427,9 @@ void Engine::require_loaded() const {
   if (!loaded_) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no LP has been loaded"};
 }
 
-void Engine::load(const sankhya_gb300_lp& lp) {
+// Model::validate's structural and numeric checks (src/core/model.cpp:175-183 and the bound
+// checks) on an LP handed across the boundary.
+void validate_lp(const sankhya_gb300_lp& lp) {
   if (lp.rows < 0 || lp.cols < 0 || lp.col_starts == nullptr) {
     throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "bad LP dimensions or null column starts"};
   }
@@ -316,7 +443,6 @@ void Engine::load(const sankhya_gb300_lp& lp) {
       throw EngineError{SANKHYA_GB300_ERROR_MODEL, "column starts are not monotone"};
     }
   }
-  // Model::validate's numeric checks (src/core/model.cpp:175-183 and the bound checks).
   for (long long k = 0; k < nnz; ++k) {
     const int i = lp.row_index[k];
     if (i < 0 || i >= m) {
@@ -349,6 +475,12 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   if (nnz > std::numeric_limits<int>::max()) {
     throw EngineError{SANKHYA_GB300_ERROR_MODEL, "more nonzeros than int32 indices address"};
   }
+}
+
+void Engine::load(const sankhya_gb300_lp& lp) {
+  validate_lp(lp);
+  const int m = lp.rows, n = lp.cols;
+  const long long nnz = lp.col_starts[n];
   SGB_CUDA(cudaSetDevice(device_));
   destroy_graphs();
   loaded_ = solved_ = scaled_ = mixed_ready_ = false;
@@ -384,14 +516,14 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   int unused_chunks = 0;
   lanes_csc_ = 1;
   lanes_csr_ = 1;
-  lanes_csc_f_ = choose_lanes(n > 0 ? static_cast<double>(nnz) / n : 1.0);
-  lanes_csr_f_ = choose_lanes(m > 0 ? static_cast<double>(nnz) / m : 1.0);
-  build_tiles(cptr, n, lanes_csc_, &ctiles, &clongs, &nchunks_csc_);
-  build_tiles(rptr, m, lanes_csr_, &rtiles, &rlongs, &nchunks_csr_);
+  lanes_csc_f_ = choose_lanes(n > 0 ? static_cast<double>(nnz) / n : 1.0, kWideThreads);
+  lanes_csr_f_ = choose_lanes(m > 0 ? static_cast<double>(nnz) / m : 1.0, kWideThreads);
+  build_tiles(cptr, n, lanes_csc_, kTileThreads, &ctiles, &clongs, &nchunks_csc_);
+  build_tiles(rptr, m, lanes_csr_, kTileThreads, &rtiles, &rlongs, &nchunks_csr_);
   {
     std::vector<LongRow> same;
-    build_tiles(cptr, n, lanes_csc_f_, &ctiles_f, &same, &unused_chunks);
-    build_tiles(rptr, m, lanes_csr_f_, &rtiles_f, &same, &unused_chunks);
+    build_tiles(cptr, n, lanes_csc_f_, kWideThreads, &ctiles_f, &same, &unused_chunks);
+    build_tiles(rptr, m, lanes_csr_f_, kWideThreads, &rtiles_f, &same, &unused_chunks);
   }
   ntiles_csc_ = static_cast<int>(ctiles.size());
   ntiles_csr_ = static_cast<int>(rtiles.size());
@@ -405,7 +537,7 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   const int resident_f = mixed_blocks_per_sm() * num_sms_;
   grid_csc_f_ = std::max(1, std::min(ntiles_csc_f_, resident_f));
   grid_csr_f_ = std::max(1, std::min(ntiles_csr_f_, resident_f));
-  const int grid_c = std::max(grid_csc_, grid_csc_f_), grid_r = std::max(grid_csr_, grid_csr_f_);
+  int grid_c = std::max(grid_csc_, grid_csc_f_), grid_r = std::max(grid_csr_, grid_csr_f_);
 
   // Minimise-space cost and the norms of src/pdhg/pdhg.cpp:95-111, summed in the
   // reference's order on the host (they are computed once).
@@ -427,8 +559,54 @@ void Engine::load(const sankhya_gb300_lp& lp) {
 
   cudaStream_t s = stream_;
   const size_t z = static_cast<size_t>(nnz);
-  csc_ptr_.upload(cptr.data(), cptr.size(), s);
-  csr_ptr_.upload(rptr.data(), rptr.size(), s);
+
+  // The step passes' windows of the gathered vector: the column passes gather y (m rows),
+  // the row passes the packed (2x' - x, x' - x) (n columns). SANKHYA_GB300_WINDOW_CAP caps
+  // the capacity (0 turns staging off), so tests can force partial windows on small LPs.
+  int cap = -1;
+  if (const char* env = std::getenv("SANKHYA_GB300_WINDOW_CAP")) cap = std::max(0, std::atoi(env)) & ~3;
+  const auto make_layout = [&](StepLayout& L, const std::vector<Tile>& tiles, const int* idx,
+                               int extent, int pass, bool mixed) {
+    int wmax = mixed ? mixed_window_capacity(pass) : fp64_window_capacity(pass);
+    if (cap >= 0) wmax = std::min(wmax, cap);
+    std::vector<int> tile_win;
+    std::vector<int2> windows;
+    long long covered = build_windows(tiles, idx, extent, wmax, &tile_win, &windows);
+    // A window leaves room for one block per SM, whose few warps cannot hide the latency of
+    // the gathers that miss it; below kMinStagedShare the unstaged form (several blocks per
+    // SM, every gather from L2) is faster, so the layout keeps no window. A fixed rule, not a
+    // timing: the grid decides the order of the block partial sums, so it must not vary from
+    // run to run.
+    // (A capacity set through SANKHYA_GB300_WINDOW_CAP keeps its windows whatever their
+    // share, so tests can run the partly staged form.)
+    constexpr double kMinStagedShare = 0.95;
+    if (cap < 0 && nnz > 0 &&
+        static_cast<double>(covered) < kMinStagedShare * static_cast<double>(nnz)) {
+      tile_win.assign(tile_win.size(), -1);
+      windows.clear();
+      covered = 0;
+    }
+    L.staged = nnz > 0 ? static_cast<double>(covered) / static_cast<double>(nnz) : 0.0;
+    L.nwindows = static_cast<int>(windows.size());
+    L.wmax = 0;
+    for (const int2& w : windows) L.wmax = std::max(L.wmax, w.y);
+    L.smem = mixed ? mixed_step_smem(pass, L.wmax) : fp64_step_smem(pass, L.wmax);
+    const int per_sm = mixed ? mixed_step_blocks_per_sm(pass, L.smem)
+                             : fp64_step_blocks_per_sm(pass, L.smem);
+    L.grid = std::max(1, std::min(static_cast<int>(tiles.size()), per_sm * num_sms_));
+    L.tile_win.upload(tile_win.data(), tile_win.size(), s);
+    L.windows.upload(windows.data(), windows.size(), s);
+  };
+  make_layout(step_csc_, ctiles, lp.row_index, m, 0, false);
+  make_layout(step_csr_, rtiles, ridx.data(), n, 1, false);
+  make_layout(step_csc_f_, ctiles_f, lp.row_index, m, 0, true);
+  make_layout(step_csr_f_, rtiles_f, ridx.data(), n, 1, true);
+  grid_c = std::max({grid_c, step_csc_.grid, step_csc_f_.grid});
+  grid_r = std::max({grid_r, step_csr_.grid, step_csr_f_.grid});
+
+  // Row pointers are staged per tile in 16-byte units too: kPad entries of padding.
+  csc_ptr_.upload_padded(cptr.data(), cptr.size(), kPad, s);
+  csr_ptr_.upload_padded(rptr.data(), rptr.size(), kPad, s);
   // Index and value arrays carry kPad zero entries: a tile copy widened to 16-byte
   // boundaries may read up to 3 entries past the last nonzero.
   csc_idx_.upload_padded(lp.row_index, z, kPad, s);
@@ -449,14 +627,17 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   u_.upload(lp.col_upper, static_cast<size_t>(n), s);
   rl_.upload(lp.row_lower, static_cast<size_t>(m), s);
   ru_.upload(lp.row_upper, static_cast<size_t>(m), s);
+  // Every per-row and per-column vector carries kPad elements of padding: the step passes
+  // stage a tile's operand slices widened to 4-element bounds, and their windows of the
+  // gathered vector may end up to 3 elements past the last one.
   for (DeviceArray<double>* a : {&cs_, &ls_, &us_, &dc_, &col_acc_, &x0_, &x1_, &x_sum_, &x_rst_,
                                  &xu0_, &xu1_, &reduced_, &best_x_, &power_v_}) {
-    a->allocate(static_cast<size_t>(n));
+    a->allocate(static_cast<size_t>(n) + kPad);
   }
-  xd_.allocate(static_cast<size_t>(n));
+  xd_.allocate(static_cast<size_t>(n) + kPad);
   for (DeviceArray<double>* a : {&rls_, &rus_, &dr_, &row_acc_, &y0_, &y1_, &y_sum_, &y_rst_,
                                  &yu0_, &yu1_, &best_y_, &power_av_}) {
-    a->allocate(static_cast<size_t>(m));
+    a->allocate(static_cast<size_t>(m) + kPad);
   }
   const int pgrid = std::max(grid_c, grid_r) + num_sms_ * 8;
   part_primal_.allocate(static_cast<size_t>(grid_c));
@@ -505,8 +686,16 @@ void Engine::fill_buffers() {
   b.part_dual = part_dual_.ptr;
   b.chunk_primal = chunk_primal_.ptr;
   b.chunk_dual = chunk_dual_.ptr;
-  b.grid_primal = grid_csc_;
-  b.grid_dual = grid_csr_;
+  b.csc.tile_win = step_csc_.tile_win.ptr;
+  b.csc.windows = step_csc_.windows.ptr;
+  b.csc.wmax = step_csc_.wmax;
+  b.csr.tile_win = step_csr_.tile_win.ptr;
+  b.csr.windows = step_csr_.windows.ptr;
+  b.csr.wmax = step_csr_.wmax;
+  b.grid_primal = step_csc_.grid;
+  b.grid_dual = step_csr_.grid;
+  b.smem_primal = step_csc_.smem;
+  b.smem_dual = step_csr_.smem;
 
   EvalBuffers& e = eval_;
   e.ctl = ctl_.ptr;
@@ -698,6 +887,46 @@ void Engine::init_iterates(const sankhya_gb300_params& p) {
   (void)p;
 }
 
+// During a capture on stream_: creates the conditional handle of the next step (its value
+// is 0 at every graph launch unless the step's last block sets it).
+cudaGraphConditionalHandle Engine::step_condition() {
+  cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
+  cudaGraph_t graph = nullptr;
+  SGB_CUDA(cudaStreamGetCaptureInfo(stream_, &status, nullptr, &graph, nullptr, nullptr,
+                                    nullptr));
+  cudaGraphConditionalHandle h = 0;
+  SGB_CUDA(cudaGraphConditionalHandleCreate(&h, graph, 0, cudaGraphCondAssignDefault));
+  return h;
+}
+
+// During a capture on stream_: appends an IF node on `h` after the work captured so far,
+// whose body -- captured on a second stream -- is what `body` launches, and makes the node
+// the dependency of what is captured next.
+template <typename F>
+void Engine::capture_if(cudaGraphConditionalHandle h, F body) {
+  cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
+  cudaGraph_t graph = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  SGB_CUDA(cudaStreamGetCaptureInfo(stream_, &status, nullptr, &graph, &deps, nullptr, &ndeps));
+  std::vector<cudaGraphNode_t> dep_list(deps, deps + ndeps);
+  cudaGraphNodeParams params{};
+  params.type = cudaGraphNodeTypeConditional;
+  params.conditional.handle = h;
+  params.conditional.type = cudaGraphCondTypeIf;
+  params.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  SGB_CUDA(cudaGraphAddNode(&node, graph, dep_list.data(), nullptr, dep_list.size(), &params));
+  cudaGraph_t inner = params.conditional.phGraph_out[0];
+  SGB_CUDA(cudaStreamBeginCaptureToGraph(capture_stream_, inner, nullptr, nullptr, 0,
+                                         cudaStreamCaptureModeRelaxed));
+  body(capture_stream_);
+  cudaGraph_t captured = nullptr;
+  SGB_CUDA(cudaStreamEndCapture(capture_stream_, &captured));
+  SGB_CUDA(cudaStreamUpdateCaptureDependencies(stream_, &node, nullptr, 1,
+                                               cudaStreamSetCaptureDependencies));
+}
+
 void Engine::build_graphs(int steps) {
   if (graph_steps_ == steps && graph_exec_[0] != nullptr) return;
   destroy_graphs();
@@ -705,8 +934,11 @@ void Engine::build_graphs(int steps) {
     cudaGraph_t graph = nullptr;
     SGB_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < steps; ++k) {
-      launch_pdhg_step(step_, stream_);
-      launch_evaluation(eval_, stream_);
+      StepBuffers sb = step_;
+      sb.cond = step_condition();
+      sb.use_cond = 1;
+      launch_pdhg_step(sb, stream_);
+      capture_if(sb.cond, [&](cudaStream_t cs) { launch_evaluation(eval_, cs); });
     }
     cudaMemcpyAsync(snapshot_ + slot, ctl_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_);
     const cudaError_t end = cudaStreamEndCapture(stream_, &graph);
@@ -898,8 +1130,11 @@ void Engine::solve_fp64(const sankhya_gb300_params& p, sankhya_gb300_result* r, 
   SGB_CUDA(cudaEventElapsedTime(&device_ms, timing_[0], timing_[1]));
   r->device_seconds = 1e-3 * device_ms;
   launches_ = launches_setup + (kernel_launch_count() - count_after_capture) +
-              graphs_launched_ * static_cast<long long>(graph_steps_) * kKernelsPerStep;
+              graphs_launched_ * static_cast<long long>(graph_steps_) * kStepKernels +
+              c.evaluations * kEvalKernels;
   r->kernel_launches = launches_;
+  r->staged_fraction[0] = step_csc_.staged;
+  r->staged_fraction[1] = step_csr_.staged;
   if (c.error) {
     throw EngineError{SANKHYA_GB300_ERROR_DEVICE, "a tile copy did not complete in time"};
   }
@@ -1060,8 +1295,10 @@ void Engine::solve_mixed(const sankhya_gb300_params& p, sankhya_gb300_result* r,
     SGB_CUDA(cudaMemcpyAsync(ctl_mixed_.ptr, &c, sizeof(Ctl), cudaMemcpyHostToDevice, s));
     launch_round_build(rb, s);
     for (DeviceArray<float>* a : {&u0f_, &usumf_, &urstf_, &ubest_}) launch_fill_float(a->ptr, n_, 0.0f, s);
-    for (DeviceArray<float>* a : {&v0f_, &vsumf_, &vrstf_, &vbest_}) launch_fill_float(a->ptr, m_, 0.0f, s);
-    extra_launches_ += 9;
+    for (DeviceArray<float>* a : {&v0f_, &vsumf_, &vrstf_, &vbest_, &auf0_}) {
+      launch_fill_float(a->ptr, m_, 0.0f, s);
+    }
+    extra_launches_ += 10;
     SGB_CUDA(cudaGetLastError());
     int round_stop = SANKHYA_GB300_ITERATION_LIMIT;
     run_graphs(p, t0, mgraph_exec_, snapshot_mixed_, false, 0, &round_stop);
@@ -1113,8 +1350,11 @@ void Engine::solve_mixed(const sankhya_gb300_params& p, sankhya_gb300_result* r,
   SGB_CUDA(cudaEventElapsedTime(&device_ms, timing_[0], timing_[1]));
   r->device_seconds = 1e-3 * device_ms;
   launches_ = launches_setup + extra_launches_ +
-              graphs_launched_ * static_cast<long long>(mgraph_steps_) * kKernelsPerStep;
+              graphs_launched_ * static_cast<long long>(mgraph_steps_) * kStepKernels +
+              c.evaluations * kEvalKernels;
   r->kernel_launches = launches_;
+  r->staged_fraction[0] = step_csc_f_.staged;
+  r->staged_fraction[1] = step_csr_f_.staged;
   r->iterations = total_it;
   r->attempts = total_att;
   r->restarts = restarts;

@@ -61,6 +61,9 @@ class Engine {
   void precondition(long long seed);
   double power_iteration(long long seed);
   void init_iterates(const sankhya_gb300_params& p);
+  cudaGraphConditionalHandle step_condition();
+  template <typename F>
+  void capture_if(cudaGraphConditionalHandle h, F body);
   void build_graphs(int steps);
   void build_mixed_graphs(int steps);
   void destroy_graphs();
@@ -80,6 +83,7 @@ class Engine {
 
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
+  cudaStream_t capture_stream_ = nullptr;  // captures the bodies of conditional graph nodes
   int num_sms_ = 0;
   bool loaded_ = false;
   bool solved_ = false;
@@ -100,6 +104,19 @@ class Engine {
   int lanes_csr_f_ = 1, lanes_csc_f_ = 1;
   int grid_csr_f_ = 1, grid_csc_f_ = 1;
   DeviceArray<Tile> csc_tiles_f_, csr_tiles_f_;
+  // The step passes' gathered-vector windows per layout (FP64 CSC / CSR, FP32 CSC / CSR):
+  // tile -> window id, the {lo, len} list, the capacity, and the grid and dynamic shared
+  // memory of the step kernel that stages them.
+  struct StepLayout {
+    DeviceArray<int> tile_win;
+    DeviceArray<int2> windows;
+    int wmax = 0;
+    int nwindows = 0;
+    int grid = 1;
+    int smem = 0;
+    double staged = 0.0;  // share of the nonzeros gathered from a staged window
+  };
+  StepLayout step_csc_, step_csr_, step_csc_f_, step_csr_f_;
 
   // Pattern (shared by scaled and unscaled values).
   DeviceArray<int> csc_ptr_, csc_idx_, csr_ptr_, csr_idx_;
@@ -141,7 +158,8 @@ class Engine {
   DeviceArray<float> u0f_, u1f_, v0f_, v1f_, usumf_, vsumf_, urstf_, vrstf_;
   DeviceArray<float> cf_, lf_, uf_, gu_, gl_, yhat_, uc0_, uc1_, vc0_, vc1_, ubest_, vbest_;
   DeviceArray<float> csf_;   // scaled cost in FP32
-  DeviceArray<float2> udf_;  // (2u' - u, u' - u) per column
+  DeviceArray<float> ubarf_;         // 2u' - u per column
+  DeviceArray<float> auf0_, auf1_;   // A u per row, double-buffered with u
   DeviceArray<double> anchor_x_, anchor_y_, ax64_, aty64_;
   DeviceArray<Ctl> ctl_mixed_;
   Ctl* snapshot_mixed_ = nullptr;  // pinned host, two slots
@@ -153,8 +171,17 @@ class Engine {
 
 size_t estimate_memory(long long rows, long long cols, long long nnz, int precision);
 
+// Throws EngineError (ARGUMENT / MODEL) when an LP is malformed.
+void validate_lp(const sankhya_gb300_lp& lp);
+
 // Row tiles of a CSR / CSC pattern (see tiles.cuh).
-void build_tiles(const std::vector<int>& ptr, int lines, int lanes, std::vector<Tile>* tiles,
-                 std::vector<LongRow>* longs, int* nchunks);
+void build_tiles(const std::vector<int>& ptr, int lines, int lanes, int threads,
+                 std::vector<Tile>* tiles, std::vector<LongRow>* longs, int* nchunks);
+
+// Gathered-vector windows of one tile layout (see tiles.cuh): `idx` is the layout's index
+// array over a gathered vector of `extent` elements, `wmax` the window capacity.
+// Returns the number of nonzeros whose index falls in their tile's window.
+long long build_windows(const std::vector<Tile>& tiles, const int* idx, int extent, int wmax,
+                        std::vector<int>* tile_win, std::vector<int2>* windows);
 
 }  // namespace sgb

@@ -107,6 +107,11 @@ struct StepBuffers {
   double* chunk_primal;  // [csc.nchunks]
   double* chunk_dual;    // [csr.nchunks * 2]
   int grid_primal, grid_dual;
+  int smem_primal, smem_dual;  // dynamic shared memory: pipeline + staged window
+  // Inside a CUDA graph, k_dual's last block sets `cond` to 1 when the step's evaluation
+  // must run: the evaluation kernels sit in a conditional node and are skipped otherwise.
+  cudaGraphConditionalHandle cond;
+  int use_cond;
 };
 
 struct EvalBuffers {
@@ -140,7 +145,8 @@ void launch_pdhg_step(const StepBuffers& b, cudaStream_t s);
 void launch_primal_pass(const StepBuffers& b, cudaStream_t s);
 void launch_dual_pass(const StepBuffers& b, cudaStream_t s);
 // Kernels launched per attempted step inside a graph (2 step + 4 evaluation kernels).
-constexpr int kKernelsPerStep = 6;
+constexpr int kStepKernels = 2;  // k_primal, k_dual (every attempted step)
+constexpr int kEvalKernels = 4;  // the evaluation kernels (evaluation ticks only)
 // Running count of kernel launches issued by the launchers of this file (host side).
 long long kernel_launch_count();
 // The evaluation tick (no-op on the device unless ctl->eval_now or ctl->final_mode).
@@ -176,6 +182,12 @@ void launch_fill(double* v, int count, double value, cudaStream_t s);
 
 // Resident tile blocks per SM of the step kernels (occupancy query).
 int tile_blocks_per_sm();
+// The FP64 step passes (pass 0 = column pass, 1 = row pass): the gathered-vector window
+// that fits beside their pipeline, their dynamic shared memory for a window of `wmax`
+// elements, and how many of their blocks fit one SM with it.
+int fp64_window_capacity(int pass);
+int fp64_step_smem(int pass, int wmax);
+int fp64_step_blocks_per_sm(int pass, int smem);
 // Sets the dynamic shared-memory limit of the tile kernels once per process.
 void configure_tile_kernels();
 

@@ -36,7 +36,11 @@ struct MixedBuffers {
   float* v_sum;
   float* u_rst;
   float* v_rst;
-  float2* ud;                  // (2u' - u, u' - u) per column, gathered by the row pass
+  float* ubar;                 // 2u' - u per column, gathered by the row pass
+  // A u of the iterate, double-buffered with u: the row pass forms A(u' - u) = (A ubar - A u)
+  // / 2 and A u' = (A ubar + A u) / 2 from the one product it gathers (u = 0, so A u = 0, at
+  // the start of every round).
+  float* au[2];
   const float *cf, *lf, *uf;   // correction cost and box (n)
   const float* cs;             // scaled cost c-hat (n): the objective of the correction
   const float *gu, *gl, *yhat; // correction row data (m)
@@ -53,7 +57,11 @@ struct MixedBuffers {
   double* part_rows1;    // [grid_dual * kEvalRowSlots]
   double* chunk_cols;    // [csc.nchunks * 2]
   double* chunk_rows;    // [csr.nchunks * 2]
-  int grid_primal, grid_dual;
+  int grid_primal, grid_dual;     // evaluation passes
+  int grid_step_primal, grid_step_dual;  // step passes (one block per SM when staging)
+  int smem_primal, smem_dual;     // step passes' dynamic shared memory
+  cudaGraphConditionalHandle cond;  // as StepBuffers::cond, set by k_dual_f
+  int use_cond;
   int m, n;
 };
 
@@ -91,5 +99,10 @@ void launch_fill_float(float* v, int count, float value, cudaStream_t s);
 void configure_mixed_kernels();
 // Resident FP32 tile blocks per SM (occupancy query).
 int mixed_blocks_per_sm();
+// The FP32 step passes (pass 0 = column pass, 1 = row pass): window capacity, dynamic shared
+// memory for a window of `wmax` elements, and blocks per SM with it.
+int mixed_window_capacity(int pass);
+int mixed_step_smem(int pass, int wmax);
+int mixed_step_blocks_per_sm(int pass, int smem);
 
 }  // namespace sgb

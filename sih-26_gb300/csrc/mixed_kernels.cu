@@ -2,9 +2,11 @@
 //
 // The step kernels mirror k_primal / k_dual with FP32 values, iterates and FP32-accumulated
 // products; the movement and interaction partials are promoted to FP64 at the block level,
-// and the step-size decision, restarts and primal weight (decisions.cuh) are FP64. In FP32
-// the row pass gathers u and u' and forms 2u' - u and u' - u per entry itself: the ALU cost
-// is negligible and no extra vector has to be written, which keeps the pass HBM-bound.
+// and the step-size decision, restarts and primal weight (decisions.cuh) are FP64. The column
+// pass writes ubar = 2u' - u per column; the row pass gathers only ubar (4 bytes per
+// nonzero, measured markedly faster on GB300 than an 8-byte (ubar, du) gather) and gets
+// A(u' - u) from the identity A ubar = 2 A u' - A u, with A u carried per row
+// (MixedBuffers::au).
 #include "common.cuh"
 #include "decisions.cuh"
 #include "kernels.cuh"
@@ -15,8 +17,16 @@ namespace sgb {
 
 namespace {
 
-constexpr int kScratch = 16 * (kTileThreads / 32);
-constexpr int kSmemF = tile_smem_bytes<float>();
+constexpr int kScratch = 16 * (kWideBlockThreads / 32);
+// The FP32 tile blocks run 16 consumer warps (the FP32 layouts' lanes are chosen for them).
+using EvalPipeF = TilePipe<float, 2, 0, kWideThreads>;
+constexpr int kSmemF = EvalPipeF::bytes();
+// The step passes keep two tiles in flight beside the staged window; each tile brings its
+// rows' operands: u, cf, lf, uf, u_sum (column pass) and v, gu, gl, yhat, v_sum, A u (row
+// pass).
+constexpr int kStepStagesF = 3;
+using PrimalPipeF = TilePipe<float, kStepStagesF, 5, kWideThreads>;
+using DualPipeF = TilePipe<float, kStepStagesF, 6, kWideThreads>;
 
 __device__ __forceinline__ void raise_error(Ctl* c) {
   c->error = 1;
@@ -28,7 +38,7 @@ __device__ __forceinline__ int grid_stride_begin() {
 }
 
 // ---- Inner step ----------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTileThreads) k_primal_f(MixedBuffers b) {
+__global__ void __launch_bounds__(kWideBlockThreads) k_primal_f(MixedBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kScratch];
   Ctl* ctl = b.ctl;
@@ -43,27 +53,33 @@ __global__ void __launch_bounds__(kTileThreads) k_primal_f(MixedBuffers b) {
     return;
   }
   const int cur = ctl->cur;
-  const float* __restrict__ u = b.u[cur];
   float* __restrict__ un = b.u[cur ^ 1];
   const float* __restrict__ v = b.v[cur];
   const double omega = ctl->omega;
   const float tau = static_cast<float>(ctl->eta / omega);
   const bool add = ctl->pending_add != 0;
   float mvf = 0.0f;
-  auto gather = [&](int row, float a, float* acc) { acc[0] = fmaf(a, __ldg(v + row), acc[0]); };
+  PrimalPipeF pipe;
+  pipe.setup(dsmem);
+  pipe.rsrc[0] = b.u[cur];
+  pipe.rsrc[1] = b.cf;
+  pipe.rsrc[2] = b.lf;
+  pipe.rsrc[3] = b.uf;
+  pipe.rsrc[4] = b.u_sum;
+  Window<float> win;
+  win.setup(v, pipe, dsmem);
+  auto gather = [&](int row, float a, float* acc) { acc[0] = fmaf(a, win.get(row), acc[0]); };
   auto epi = [&](int j, const float* s) {
-    const float uj = u[j];
-    if (add) b.u_sum[j] += uj;
-    const float g = b.cf[j] + s[0];
-    const float unj = clamp_box(fmaf(-tau, g, uj), b.lf[j], b.uf[j]);
+    const float uj = pipe.row(0, j);
+    if (add) b.u_sum[j] = pipe.row(4, j) + uj;
+    const float g = pipe.row(1, j) + s[0];
+    const float unj = clamp_box(fmaf(-tau, g, uj), pipe.row(2, j), pipe.row(3, j));
     un[j] = unj;
     const float d = unj - uj;
-    b.ud[j] = make_float2(fmaf(2.0f, unj, -uj), d);
+    b.ubar[j] = fmaf(2.0f, unj, -uj);
     mvf = fmaf(d, d, mvf);
   };
-  TilePipe<float> pipe;
-  pipe.setup(dsmem);
-  if (!run_tiles<1, float>(pipe, b.csc, b.chunk_primal, scratch, gather, epi) &&
+  if (!run_tiles<1, float>(pipe, b.csc, win, b.chunk_primal, gather, epi) &&
       threadIdx.x == 0) {
     raise_error(ctl);
   }
@@ -81,57 +97,64 @@ __global__ void __launch_bounds__(kTileThreads) k_primal_f(MixedBuffers b) {
   }
 }
 
-__global__ void __launch_bounds__(kTileThreads) k_dual_f(MixedBuffers b) {
+__global__ void __launch_bounds__(kWideBlockThreads) k_dual_f(MixedBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kScratch];
   Ctl* ctl = b.ctl;
   if (ctl->done != kRunning) return;
   const int cur = ctl->cur;
-  const float2* __restrict__ ud = b.ud;
-  const float* __restrict__ v = b.v[cur];
   float* __restrict__ vn = b.v[cur ^ 1];
+  float* __restrict__ aun = b.au[cur ^ 1];
   const double omega = ctl->omega;
   const float sigma = static_cast<float>(ctl->eta * omega);
   const float inv_sigma = 1.0f / sigma;
   const bool add = ctl->pending_add != 0;
   float a0 = 0.0f, a1 = 0.0f;  // sum dv^2, sum dv (A du)
-  auto gather = [&](int col, float a, float* acc) {
-    const float2 p = __ldg(ud + col);
-    acc[0] = fmaf(a, p.x, acc[0]);
-    acc[1] = fmaf(a, p.y, acc[1]);
-  };
+  DualPipeF pipe;
+  pipe.setup(dsmem);
+  pipe.rsrc[0] = b.v[cur];
+  pipe.rsrc[1] = b.gu;
+  pipe.rsrc[2] = b.gl;
+  pipe.rsrc[3] = b.yhat;
+  pipe.rsrc[4] = b.v_sum;
+  pipe.rsrc[5] = b.au[cur];
+  Window<float> win;
+  win.setup(b.ubar, pipe, dsmem);
+  auto gather = [&](int col, float a, float* acc) { acc[0] = fmaf(a, win.get(col), acc[0]); };
   auto epi = [&](int i, const float* s) {
-    const float vi = v[i];
-    if (add) b.v_sum[i] += vi;
-    const float gu = b.gu[i], gl = b.gl[i];
+    const float vi = pipe.row(0, i);
+    if (add) b.v_sum[i] = pipe.row(4, i) + vi;
+    const float gu = pipe.row(1, i), gl = pipe.row(2, i);
+    const float au = pipe.row(5, i);
+    const float adu = 0.5f * (s[0] - au);
+    aun[i] = 0.5f * (s[0] + au);
     float vni;
     if (gu == gl) {
       vni = fmaf(sigma, gu + s[0], vi);
     } else {
-      const float t = fmaf(b.yhat[i] + vi, inv_sigma, s[0]);
+      const float yhat = pipe.row(3, i);
+      const float t = fmaf(yhat + vi, inv_sigma, s[0]);
       if (t + gu > 0.0f) {
         vni = fmaf(sigma, gu + s[0], vi);
       } else if (t + gl < 0.0f) {
         vni = fmaf(sigma, gl + s[0], vi);
       } else {
-        vni = -b.yhat[i];
+        vni = -yhat;
       }
     }
     vn[i] = vni;
     const float d = vni - vi;
     a0 = fmaf(d, d, a0);
-    a1 = fmaf(d, s[1], a1);
+    a1 = fmaf(d, adu, a1);
   };
-  TilePipe<float> pipe;
-  pipe.setup(dsmem);
-  if (!run_tiles<2, float>(pipe, b.csr, b.chunk_dual, scratch, gather, epi) &&
+  if (!run_tiles<1, float>(pipe, b.csr, win, b.chunk_dual, gather, epi) &&
       threadIdx.x == 0) {
     raise_error(ctl);
   }
   double acc2[2] = {static_cast<double>(a0), static_cast<double>(a1)};
   if (!arrive_last<2>(acc2, scratch, b.part_dual, &ctl->ticket[kTicketDual])) return;
   a0 = a1 = 0.0f;
-  run_long_rows<2, float>(b.csr, b.chunk_dual, epi);
+  run_long_rows<1, float>(b.csr, b.chunk_dual, epi);
   acc2[0] = a0;
   acc2[1] = a1;
   double longs[2], total[2];
@@ -142,6 +165,9 @@ __global__ void __launch_bounds__(kTileThreads) k_dual_f(MixedBuffers b) {
     if (ctl->done == kRunning) {
       const double movement = ctl->mv_primal + (0.5 * (total[0] + longs[0])) / omega;
       step_decision(ctl, movement, fabs(total[1] + longs[1]));
+    }
+    if (b.use_cond) {
+      cudaGraphSetConditional(b.cond, ctl->eval_now != 0 && ctl->done == kRunning ? 1u : 0u);
     }
   }
 }
@@ -186,7 +212,7 @@ __global__ void __launch_bounds__(kTileThreads) k_evalf_rows0(MixedBuffers b) {
 
 // Columns over the FP32 CSC: d_c = cf + A^T v_c of both candidates, the column dual
 // violation, the column half of the gap (sum d (x - bound) in correction units), |u-u_rst|^2.
-__global__ void __launch_bounds__(kTileThreads) k_evalf_cols(MixedBuffers b) {
+__global__ void __launch_bounds__(kWideBlockThreads) k_evalf_cols(MixedBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kScratch];
   Ctl* c = b.ctl;
@@ -225,9 +251,9 @@ __global__ void __launch_bounds__(kTileThreads) k_evalf_cols(MixedBuffers b) {
     const double d = static_cast<double>(ucur) - static_cast<double>(b.u_rst[j]);
     acc[4] += d * d;
   };
-  TilePipe<float> pipe;
+  EvalPipeF pipe;
   pipe.setup(dsmem);
-  if (!run_tiles<2, float>(pipe, b.csc, b.chunk_cols, scratch, gather, epi) &&
+  if (!run_tiles<2, float>(pipe, b.csc, b.chunk_cols, gather, epi) &&
       threadIdx.x == 0) {
     raise_error(c);
   }
@@ -259,7 +285,7 @@ __device__ bool round_stop_test(const Ctl* c, const Residuals& r) {
 
 // Rows over the FP32 CSR: A u_c, the primal violation and the row half of the gap; the last
 // block assembles the scaled-problem KKT of xbar + u/dp, ybar + v/dd and decides.
-__global__ void __launch_bounds__(kTileThreads) k_evalf_rows1(MixedBuffers b) {
+__global__ void __launch_bounds__(kWideBlockThreads) k_evalf_rows1(MixedBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kScratch];
   Ctl* c = b.ctl;
@@ -287,9 +313,9 @@ __global__ void __launch_bounds__(kTileThreads) k_evalf_rows1(MixedBuffers b) {
       else if (yc < 0.0 && !isinf(gl)) acc[2 * q + 1] += yc * (gl + a);
     }
   };
-  TilePipe<float> pipe;
+  EvalPipeF pipe;
   pipe.setup(dsmem);
-  if (!run_tiles<2, float>(pipe, b.csr, b.chunk_rows, scratch, gather, epi) &&
+  if (!run_tiles<2, float>(pipe, b.csr, b.chunk_rows, gather, epi) &&
       threadIdx.x == 0) {
     raise_error(c);
   }
@@ -497,8 +523,10 @@ int egrid(long long count) {
 void configure_mixed_kernels() {
   static bool done = false;
   if (done) return;
-  cudaFuncSetAttribute(k_primal_f, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemF);
-  cudaFuncSetAttribute(k_dual_f, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemF);
+  cudaFuncSetAttribute(k_primal_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       max_dynamic_smem(reinterpret_cast<const void*>(k_primal_f)));
+  cudaFuncSetAttribute(k_dual_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       max_dynamic_smem(reinterpret_cast<const void*>(k_dual_f)));
   cudaFuncSetAttribute(k_evalf_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemF);
   cudaFuncSetAttribute(k_evalf_rows1, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemF);
   done = true;
@@ -509,20 +537,41 @@ int mixed_blocks_per_sm() {
   if (per_sm == 0) {
     configure_mixed_kernels();
     int a = 0, b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_dual_f, kTileThreads, kSmemF);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_primal_f, kTileThreads, kSmemF);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_evalf_rows1, kWideBlockThreads, kSmemF);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_evalf_cols, kWideBlockThreads, kSmemF);
     per_sm = a < b ? a : b;
     if (per_sm <= 0) per_sm = 1;
   }
   return per_sm;
 }
 
+int mixed_window_capacity(int pass) {
+  configure_mixed_kernels();
+  return pass == 0 ? window_capacity(reinterpret_cast<const void*>(k_primal_f),
+                                     PrimalPipeF::bytes(), sizeof(float))
+                   : window_capacity(reinterpret_cast<const void*>(k_dual_f),
+                                     DualPipeF::bytes(), sizeof(float));
+}
+
+int mixed_step_smem(int pass, int wmax) {
+  return (pass == 0 ? PrimalPipeF::bytes() : DualPipeF::bytes()) +
+         window_bytes(wmax, sizeof(float));
+}
+
+int mixed_step_blocks_per_sm(int pass, int smem) {
+  configure_mixed_kernels();
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, pass == 0 ? k_primal_f : k_dual_f, kWideBlockThreads, static_cast<size_t>(smem));
+  return per_sm > 0 ? per_sm : 1;
+}
+
 void launch_mixed_primal(const MixedBuffers& b, cudaStream_t s) {
-  k_primal_f<<<b.grid_primal, kTileThreads, kSmemF, s>>>(b);
+  k_primal_f<<<b.grid_step_primal, kWideBlockThreads, b.smem_primal, s>>>(b);
 }
 
 void launch_mixed_dual(const MixedBuffers& b, cudaStream_t s) {
-  k_dual_f<<<b.grid_dual, kTileThreads, kSmemF, s>>>(b);
+  k_dual_f<<<b.grid_step_dual, kWideBlockThreads, b.smem_dual, s>>>(b);
 }
 
 void launch_mixed_step(const MixedBuffers& b, cudaStream_t s) {
@@ -532,8 +581,8 @@ void launch_mixed_step(const MixedBuffers& b, cudaStream_t s) {
 
 void launch_mixed_evaluation(const MixedBuffers& b, cudaStream_t s) {
   k_evalf_rows0<<<b.grid_dual, kTileThreads, 0, s>>>(b);
-  k_evalf_cols<<<b.grid_primal, kTileThreads, kSmemF, s>>>(b);
-  k_evalf_rows1<<<b.grid_dual, kTileThreads, kSmemF, s>>>(b);
+  k_evalf_cols<<<b.grid_primal, kWideBlockThreads, kSmemF, s>>>(b);
+  k_evalf_rows1<<<b.grid_dual, kWideBlockThreads, kSmemF, s>>>(b);
   k_evalf_apply<<<egrid(b.m > b.n ? b.m : b.n), 256, 0, s>>>(b);
 }
 

@@ -33,7 +33,13 @@ long long g_launches = 0;
 int g_tile_blocks_per_sm = 0;
 int g_num_sms = 0;
 
-constexpr int kScratch = 16 * (kTileThreads / 32);
+constexpr int kScratch = 16 * (kBlockThreads / 32);
+// The step passes keep one tile in flight beside the staged window (a larger window pays
+// more in FP64 than a deeper pipeline); each tile brings its
+// rows' operands: x, c, l, u, x_sum (column pass) and y, rl, ru, y_sum (row pass).
+constexpr int kStepStages = 2;
+using PrimalPipe = TilePipe<double, kStepStages, 5>;
+using DualPipe = TilePipe<double, kStepStages, 4>;
 
 __device__ __forceinline__ void raise_error(Ctl* c) {
   c->error = 1;
@@ -48,7 +54,7 @@ __device__ bool fp64_stop_test(const Ctl* c, const Residuals& r) {
 }
 
 // ---- k_primal ----------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTileThreads) k_primal(StepBuffers b) {
+__global__ void __launch_bounds__(kBlockThreads) k_primal(StepBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kScratch];
   Ctl* ctl = b.ctl;
@@ -65,29 +71,37 @@ __global__ void __launch_bounds__(kTileThreads) k_primal(StepBuffers b) {
     return;
   }
   const int cur = ctl->cur;
-  const double* __restrict__ x = b.x[cur];
+  const double* x = b.x[cur];
   double* __restrict__ xn = b.x[cur ^ 1];
   const double* __restrict__ y = b.y[cur];
   const double omega = ctl->omega;
   const double tau = ctl->eta / omega;
   const bool add = ctl->pending_add != 0;
   double mv[1] = {0.0};  // sum of dx^2
-  auto gather = [&](int row, double v, double* acc) { acc[0] = fma(v, __ldg(y + row), acc[0]); };
+  PrimalPipe pipe;
+  pipe.setup(dsmem);
+  pipe.rsrc[0] = x;
+  pipe.rsrc[1] = b.c;
+  pipe.rsrc[2] = b.l;
+  pipe.rsrc[3] = b.u;
+  pipe.rsrc[4] = b.x_sum;
+  Window<double> win;
+  win.setup(y, pipe, dsmem);
+  auto gather = [&](int row, double v, double* acc) { acc[0] = fma(v, win.get(row), acc[0]); };
   auto epi = [&](int j, const double* s) {
-    const double xj = x[j];
-    if (add) b.x_sum[j] += xj;
-    const double gradient = b.c[j] + s[0];
+    const double xj = pipe.row(0, j);
+    if (add) b.x_sum[j] = pipe.row(4, j) + xj;
+    const double gradient = pipe.row(1, j) + s[0];
     // Unfused, as src/pdhg/pdhg.cpp:232-233 rounds it.
-    const double xnj = clamp_box(__dsub_rn(xj, __dmul_rn(tau, gradient)), b.l[j], b.u[j]);
+    const double xnj =
+        clamp_box(__dsub_rn(xj, __dmul_rn(tau, gradient)), pipe.row(2, j), pipe.row(3, j));
     xn[j] = xnj;
     const double d = xnj - xj;
     // 2 x' is exact, so the FMA rounds once, as the reference's 2.0 * x' - x does.
     b.xd[j] = make_double2(fma(2.0, xnj, -xj), d);
     mv[0] = fma(d, d, mv[0]);
   };
-  TilePipe<double> pipe;
-  pipe.setup(dsmem);
-  if (!run_tiles<1, double>(pipe, b.csc, b.chunk_primal, scratch, gather, epi) &&
+  if (!run_tiles<1, double>(pipe, b.csc, win, b.chunk_primal, gather, epi) &&
       threadIdx.x == 0) {
     raise_error(ctl);
   }
@@ -104,7 +118,7 @@ __global__ void __launch_bounds__(kTileThreads) k_primal(StepBuffers b) {
 }
 
 // ---- k_dual ------------------------------------------------------------------------------
-__global__ void __launch_bounds__(kTileThreads) k_dual(StepBuffers b) {
+__global__ void __launch_bounds__(kBlockThreads) k_dual(StepBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kScratch];
   Ctl* ctl = b.ctl;
@@ -117,15 +131,23 @@ __global__ void __launch_bounds__(kTileThreads) k_dual(StepBuffers b) {
   const double sigma = ctl->eta * omega;
   const bool add = ctl->pending_add != 0;
   double acc2[2] = {0.0, 0.0};  // sum dy^2, sum dy (A dx)
+  DualPipe pipe;
+  pipe.setup(dsmem);
+  pipe.rsrc[0] = y;
+  pipe.rsrc[1] = b.rl;
+  pipe.rsrc[2] = b.ru;
+  pipe.rsrc[3] = b.y_sum;
+  Window<double2> win;
+  win.setup(xd, pipe, dsmem);
   auto gather = [&](int col, double v, double* acc) {
-    const double2 p = __ldg(xd + col);
+    const double2 p = win.get(col);
     acc[0] = fma(v, p.x, acc[0]);
     acc[1] = fma(v, p.y, acc[1]);
   };
   auto epi = [&](int i, const double* s) {
-    const double yi = y[i];
-    if (add) b.y_sum[i] += yi;
-    const double rl = b.rl[i], ru = b.ru[i];
+    const double yi = pipe.row(0, i);
+    if (add) b.y_sum[i] = pipe.row(3, i) + yi;
+    const double rl = pipe.row(1, i), ru = pipe.row(2, i);
     // Unfused, as the reference rounds it (src/pdhg/pdhg.cpp:244-245): a fused
     // v - sigma * (v / sigma) would leave the division's rounding error on a free row. On
     // an equality row the projection is the bound whatever v is, so no division is needed.
@@ -137,9 +159,7 @@ __global__ void __launch_bounds__(kTileThreads) k_dual(StepBuffers b) {
     acc2[0] = fma(d, d, acc2[0]);
     acc2[1] = fma(d, s[1], acc2[1]);
   };
-  TilePipe<double> pipe;
-  pipe.setup(dsmem);
-  if (!run_tiles<2, double>(pipe, b.csr, b.chunk_dual, scratch, gather, epi) &&
+  if (!run_tiles<2, double>(pipe, b.csr, win, b.chunk_dual, gather, epi) &&
       threadIdx.x == 0) {
     raise_error(ctl);
   }
@@ -154,6 +174,9 @@ __global__ void __launch_bounds__(kTileThreads) k_dual(StepBuffers b) {
     if (ctl->done == kRunning) {
       const double movement = ctl->mv_primal + (0.5 * (total[0] + longs[0])) / omega;
       step_decision(ctl, movement, fabs(total[1] + longs[1]));
+    }
+    if (b.use_cond) {
+      cudaGraphSetConditional(b.cond, ctl->eval_now != 0 && ctl->done == kRunning ? 1u : 0u);
     }
   }
 }
@@ -212,7 +235,7 @@ __global__ void __launch_bounds__(kTileThreads) k_eval_rows0(EvalBuffers e) {
 // E1: columns over the unscaled CSC. Reduced costs d = c + A^T y of both candidates, the
 // column half of the dual violation / dual objective / complementarity, the primal objective
 // (src/pdhg/pdhg_evaluate.cpp:54-78,111-139) and |x - x_restart|^2.
-__global__ void __launch_bounds__(kTileThreads) k_eval_cols(EvalBuffers e) {
+__global__ void __launch_bounds__(kBlockThreads) k_eval_cols(EvalBuffers e) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kScratch];
   Ctl* c = e.ctl;
@@ -267,7 +290,7 @@ __global__ void __launch_bounds__(kTileThreads) k_eval_cols(EvalBuffers e) {
   };
   TilePipe<double> pipe;
   pipe.setup(dsmem);
-  if (!run_tiles<2, double>(pipe, e.csc, e.chunk_cols, scratch, gather, epi) &&
+  if (!run_tiles<2, double>(pipe, e.csc, e.chunk_cols, gather, epi) &&
       threadIdx.x == 0) {
     raise_error(c);
   }
@@ -320,7 +343,7 @@ __device__ Residuals assemble(double pviol, double cviol, double rviol, double b
 // E2: rows over the unscaled CSR. Activities of both candidates, primal violation and the
 // row complementarity (src/pdhg/pdhg_evaluate.cpp:29-45,99-110). The last block assembles
 // the Residuals and takes the best / stop / restart decisions (src/pdhg/pdhg.cpp:349-483).
-__global__ void __launch_bounds__(kTileThreads) k_eval_rows1(EvalBuffers e) {
+__global__ void __launch_bounds__(kBlockThreads) k_eval_rows1(EvalBuffers e) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kScratch];
   Ctl* c = e.ctl;
@@ -353,7 +376,7 @@ __global__ void __launch_bounds__(kTileThreads) k_eval_rows1(EvalBuffers e) {
   };
   TilePipe<double> pipe;
   pipe.setup(dsmem);
-  if (!run_tiles<2, double>(pipe, e.csr, e.chunk_rows, scratch, gather, epi) &&
+  if (!run_tiles<2, double>(pipe, e.csr, e.chunk_rows, gather, epi) &&
       threadIdx.x == 0) {
     raise_error(c);
   }
@@ -506,7 +529,7 @@ __global__ void k_scale_vectors(int m, int n, const double* cost, const double* 
 }
 
 // y = A x with products summed in ascending index order per row.
-__global__ void __launch_bounds__(kTileThreads) k_spmv(TileSet<double> a, const double* x,
+__global__ void __launch_bounds__(kBlockThreads) k_spmv(TileSet<double> a, const double* x,
                                                        double* y, double* chunk,
                                                        unsigned int* ticket) {
   extern __shared__ __align__(16) unsigned char dsmem[];
@@ -515,7 +538,7 @@ __global__ void __launch_bounds__(kTileThreads) k_spmv(TileSet<double> a, const 
   auto epi = [&](int r, const double* s) { y[r] = 0.0 + s[0]; };
   TilePipe<double> pipe;
   pipe.setup(dsmem);
-  run_tiles<1, double>(pipe, a, chunk, scratch, gather, epi);
+  run_tiles<1, double>(pipe, a, chunk, gather, epi);
   if (a.nlong == 0) return;
   __shared__ int s_last;
   if (threadIdx.x == 0) {
@@ -621,15 +644,17 @@ int elementwise_grid(int count) {
   return blocks < 1 ? 1 : blocks;
 }
 
-constexpr int kTileSmem = tile_smem_bytes<double>();
+constexpr int kTileSmem = TilePipe<double>::bytes();
 
 }  // namespace
 
 void configure_tile_kernels() {
   static bool done = false;
   if (done) return;
-  cudaFuncSetAttribute(k_primal, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
-  cudaFuncSetAttribute(k_dual, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
+  cudaFuncSetAttribute(k_primal, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       max_dynamic_smem(reinterpret_cast<const void*>(k_primal)));
+  cudaFuncSetAttribute(k_dual, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       max_dynamic_smem(reinterpret_cast<const void*>(k_dual)));
   cudaFuncSetAttribute(k_eval_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
   cudaFuncSetAttribute(k_eval_rows1, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
   cudaFuncSetAttribute(k_spmv, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
@@ -640,7 +665,7 @@ int tile_blocks_per_sm() {
   if (g_tile_blocks_per_sm == 0) {
     configure_tile_kernels();
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dual, kTileThreads, kTileSmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval_rows1, kBlockThreads, kTileSmem);
     g_tile_blocks_per_sm = per_sm > 0 ? per_sm : 1;
   }
   return g_tile_blocks_per_sm;
@@ -648,13 +673,34 @@ int tile_blocks_per_sm() {
 
 long long kernel_launch_count() { return g_launches; }
 
+int fp64_window_capacity(int pass) {
+  configure_tile_kernels();
+  return pass == 0 ? window_capacity(reinterpret_cast<const void*>(k_primal),
+                                     PrimalPipe::bytes(), sizeof(double))
+                   : window_capacity(reinterpret_cast<const void*>(k_dual), DualPipe::bytes(),
+                                     sizeof(double2));
+}
+
+int fp64_step_smem(int pass, int wmax) {
+  return pass == 0 ? PrimalPipe::bytes() + window_bytes(wmax, sizeof(double))
+                   : DualPipe::bytes() + window_bytes(wmax, sizeof(double2));
+}
+
+int fp64_step_blocks_per_sm(int pass, int smem) {
+  configure_tile_kernels();
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, pass == 0 ? k_primal : k_dual, kBlockThreads, static_cast<size_t>(smem));
+  return per_sm > 0 ? per_sm : 1;
+}
+
 void launch_primal_pass(const StepBuffers& b, cudaStream_t s) {
-  k_primal<<<b.grid_primal, kTileThreads, kTileSmem, s>>>(b);
+  k_primal<<<b.grid_primal, kBlockThreads, b.smem_primal, s>>>(b);
   ++g_launches;
 }
 
 void launch_dual_pass(const StepBuffers& b, cudaStream_t s) {
-  k_dual<<<b.grid_dual, kTileThreads, kTileSmem, s>>>(b);
+  k_dual<<<b.grid_dual, kBlockThreads, b.smem_dual, s>>>(b);
   ++g_launches;
 }
 
@@ -666,8 +712,8 @@ void launch_pdhg_step(const StepBuffers& b, cudaStream_t s) {
 void launch_evaluation(const EvalBuffers& e, cudaStream_t s) {
   g_launches += 4;
   k_eval_rows0<<<e.grid_rows, kTileThreads, 0, s>>>(e);
-  k_eval_cols<<<e.grid_cols, kTileThreads, kTileSmem, s>>>(e);
-  k_eval_rows1<<<e.grid_rows, kTileThreads, kTileSmem, s>>>(e);
+  k_eval_cols<<<e.grid_cols, kBlockThreads, kTileSmem, s>>>(e);
+  k_eval_rows1<<<e.grid_rows, kBlockThreads, kTileSmem, s>>>(e);
   const int total = e.m > e.n ? e.m : e.n;
   k_eval_apply<<<elementwise_grid(total), 256, 0, s>>>(e);
 }
@@ -699,7 +745,7 @@ void launch_spmv(TileSet<double> a, const double* x, double* y, double* chunk,
                  unsigned int* ticket, cudaStream_t s, int grid) {
   if (a.nrows == 0) return;
   ++g_launches;
-  k_spmv<<<grid, kTileThreads, kTileSmem, s>>>(a, x, y, chunk, ticket);
+  k_spmv<<<grid, kBlockThreads, kTileSmem, s>>>(a, x, y, chunk, ticket);
 }
 
 namespace {

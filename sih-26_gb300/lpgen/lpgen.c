@@ -21,6 +21,12 @@
  *                          scaled so the lengths sum to about target_nnz, distinct uniform
  *                          columns per row, values +-10^U(-3,3) (log-uniform magnitude over
  *                          [1e-3, 1e3], random sign), 0 <= x <= 10, equality rows.
+ *   lpgen_planted_nondegenerate  as planted_uniform, but with a unique and nondegenerate
+ *                          optimum: exactly m basic columns (x0 in U(0.1, 9.9), z = 0), the
+ *                          p-th of which has an entry of magnitude 1 + |N(0,1)| in row p (so
+ *                          the basis matrix has a heavy diagonal and is nonsingular); every
+ *                          other column sits at 0 or 10 with |z| in U(0.1, 1). x*, y* are then
+ *                          differentiable in c, b and the bounds.
  *   lpgen_planted_general  every row kind (equality, one-sided active/slack, range active at
  *                          either side, free) and every column kind (boxed, lower-only,
  *                          upper-only, free, fixed) for parity coverage.
@@ -515,6 +521,86 @@ int32_t lpgen_planted_zipf(int32_t m, int32_t n, int64_t target_nnz, double expo
   free(rval);
   free(rcol);
   free(len);
+  free(g);
+  return 0;
+}
+
+int64_t lpgen_planted_nondegenerate_nnz(int32_t m, int32_t n, int32_t k) {
+  (void)m;
+  return (int64_t)n * k;
+}
+
+int32_t lpgen_planted_nondegenerate(int32_t m, int32_t n, int32_t k, uint64_t seed,
+                                    lpgen_lp* lp) {
+  if (m <= 0 || n < m || k <= 0 || k > m) return 1;
+  mt64* g = (mt64*)malloc(sizeof(mt64));
+  mt64_seed(g, seed);
+  double* z = (double*)malloc(sizeof(double) * (size_t)n);
+  int32_t* basic_row = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+  int32_t* perm = (int32_t*)malloc(sizeof(int32_t) * (size_t)n);
+  for (int32_t j = 0; j < n; ++j) perm[j] = j;
+  for (int32_t j = n - 1; j > 0; --j) { /* Fisher-Yates */
+    const int32_t r = unif_int(g, j + 1);
+    const int32_t t = perm[j];
+    perm[j] = perm[r];
+    perm[r] = t;
+  }
+  for (int32_t j = 0; j < n; ++j) basic_row[j] = -1;
+  for (int32_t p = 0; p < m; ++p) basic_row[perm[p]] = p;
+  lp->rows = m;
+  lp->cols = n;
+  lp->nnz = (int64_t)n * k;
+  int64_t at = 0;
+  for (int32_t j = 0; j < n; ++j) {
+    lp->col_starts[j] = (int32_t)at;
+    int32_t* rows = lp->row_index + at;
+    const int32_t p = basic_row[j];
+    if (p >= 0) {
+      /* Row p plus k - 1 distinct others, ascending. */
+      int32_t t = 0;
+      rows[t++] = p;
+      while (t < k) {
+        const int32_t r = unif_int(g, m);
+        int dup = 0;
+        for (int32_t s = 0; s < t; ++s) dup |= rows[s] == r;
+        if (!dup) rows[t++] = r;
+      }
+      for (int32_t a = 1; a < k; ++a) { /* insertion sort */
+        const int32_t v = rows[a];
+        int32_t b = a;
+        while (b > 0 && rows[b - 1] > v) {
+          rows[b] = rows[b - 1];
+          --b;
+        }
+        rows[b] = v;
+      }
+      for (int32_t s = 0; s < k; ++s) {
+        const double v = normal(g);
+        lp->values[at + s] = rows[s] == p ? (v < 0.0 ? -1.0 + v : 1.0 + v) : v;
+      }
+      lp->x0[j] = unif_ab(g, 0.1, 9.9);
+      z[j] = 0.0;
+    } else {
+      pick_rows(g, 0, m, k, rows);
+      for (int32_t s = 0; s < k; ++s) lp->values[at + s] = normal(g);
+      if (unif(g) < 0.75) {
+        lp->x0[j] = 0.0;
+        z[j] = unif_ab(g, 0.1, 1.0);
+      } else {
+        lp->x0[j] = 10.0;
+        z[j] = -unif_ab(g, 0.1, 1.0);
+      }
+    }
+    at += k;
+    lp->col_lower[j] = 0.0;
+    lp->col_upper[j] = 10.0;
+  }
+  lp->col_starts[n] = (int32_t)at;
+  for (int32_t i = 0; i < m; ++i) lp->lambda[i] = normal(g);
+  finish_equalities(lp, z);
+  free(perm);
+  free(basic_row);
+  free(z);
   free(g);
   return 0;
 }

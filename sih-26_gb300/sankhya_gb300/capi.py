@@ -77,7 +77,17 @@ class CResult(ctypes.Structure):
                 ("scaled_max_abs", ctypes.c_double), ("setup_seconds", ctypes.c_double),
                 ("loop_seconds", ctypes.c_double), ("solve_seconds", ctypes.c_double),
                 ("device_seconds", ctypes.c_double), ("kernel_launches", ctypes.c_int64),
+                ("staged_fraction", ctypes.c_double * 2),
                 ("message", ctypes.c_char * 512)]
+
+
+class CBatchItem(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("converged", ctypes.c_int32),
+                ("iterations", ctypes.c_int64), ("attempts", ctypes.c_int64),
+                ("restarts", ctypes.c_int64), ("evaluations", ctypes.c_int64),
+                ("objective", ctypes.c_double), ("dual_bound", ctypes.c_double),
+                ("final_residuals", CResiduals), ("spectral_norm", ctypes.c_double),
+                ("farkas_value", ctypes.c_double)]
 
 
 EXPORTS = [
@@ -86,7 +96,9 @@ EXPORTS = [
     "sankhya_gb300_estimate_memory", "sankhya_gb300_pdhg_create", "sankhya_gb300_pdhg_destroy",
     "sankhya_gb300_pdhg_load", "sankhya_gb300_pdhg_solve", "sankhya_gb300_pdhg_solution",
     "sankhya_gb300_pdhg_scaling", "sankhya_gb300_pdhg_spmv", "sankhya_gb300_pdhg_time_kernels",
-    "sankhya_gb300_pdhg_spmv_noalloc",
+    "sankhya_gb300_pdhg_spmv_noalloc", "sankhya_gb300_batch_create",
+    "sankhya_gb300_batch_destroy", "sankhya_gb300_batch_load", "sankhya_gb300_batch_solve",
+    "sankhya_gb300_batch_solution",
 ]
 
 _lib = None
@@ -124,6 +136,15 @@ def load_library():
         lib.sankhya_gb300_pdhg_spmv.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                                 _D, _D]
         lib.sankhya_gb300_pdhg_time_kernels.argtypes = [ctypes.c_void_p, ctypes.c_int32, _D]
+        lib.sankhya_gb300_batch_create.argtypes = [ctypes.c_int32,
+                                                   ctypes.POINTER(ctypes.c_void_p)]
+        lib.sankhya_gb300_batch_destroy.argtypes = [ctypes.c_void_p]
+        lib.sankhya_gb300_batch_load.argtypes = [ctypes.c_void_p, ctypes.c_int32,
+                                                 ctypes.POINTER(CLp)]
+        lib.sankhya_gb300_batch_solve.argtypes = [ctypes.c_void_p, ctypes.POINTER(CParams),
+                                                  ctypes.POINTER(CBatchItem), _D]
+        lib.sankhya_gb300_batch_solution.argtypes = [ctypes.c_void_p, ctypes.c_int32, _D, _D,
+                                                     _D]
         lib.sankhya_gb300_pdhg_spmv_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int32,
                                                         ctypes.c_int32, ctypes.c_void_p,
                                                         ctypes.c_void_p, ctypes.c_void_p]
@@ -177,6 +198,7 @@ class Result:
     solve_seconds: float
     device_seconds: float
     kernel_launches: int
+    staged_fraction: tuple
     message: str
 
 
@@ -239,6 +261,7 @@ class PdhgEngine:
                       r.objective, r.dual_bound, r.final_residuals.as_dict(), r.spectral_norm,
                       r.scaled_min_abs, r.scaled_max_abs, r.setup_seconds, r.loop_seconds,
                       r.solve_seconds, r.device_seconds, r.kernel_launches,
+                      (r.staged_fraction[0], r.staged_fraction[1]),
                       r.message.decode(errors="replace"))
 
     def time_kernels(self, reps: int = 20):
@@ -281,6 +304,91 @@ class PdhgEngine:
         _check(self._lib.sankhya_gb300_pdhg_spmv_noalloc(
             self._h, op, int(scaled), ctypes.c_void_p(device_in), ctypes.c_void_p(device_out),
             ctypes.c_void_p(stream) if stream else None))
+
+
+@dataclass
+class BatchItem:
+    status: int
+    status_name: str
+    converged: bool
+    iterations: int
+    attempts: int
+    restarts: int
+    evaluations: int
+    objective: float
+    dual_bound: float
+    residuals: dict
+    spectral_norm: float
+    farkas_value: float
+
+
+class BatchEngine:
+    """Many LPs solved together, one thread block per LP (sankhya_gb300_batch_*). LPs whose
+    matrix arrays are the same numpy objects share one device copy of the matrix."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self._lib.sankhya_gb300_batch_create(device, ctypes.byref(h)))
+        self._h = h
+        self._lps = []
+        self._keep = None
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.sankhya_gb300_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def load(self, lps):
+        lps = [lp.contiguous() for lp in lps]
+        arr = (CLp * len(lps))()
+        for k, lp in enumerate(lps):
+            arr[k] = CLp(lp.rows, lp.cols, _ptr(lp.col_starts, ctypes.c_int32),
+                         _ptr(lp.row_index, ctypes.c_int32), _ptr(lp.values), _ptr(lp.col_cost),
+                         _ptr(lp.col_lower), _ptr(lp.col_upper), _ptr(lp.row_lower),
+                         _ptr(lp.row_upper), lp.sense, lp.objective_offset)
+        _check(self._lib.sankhya_gb300_batch_load(self._h, len(lps), arr))
+        self._lps = lps
+
+    def solve(self, tolerance: float = 1e-4, iteration_limit: int = -1, restart: bool = True,
+              stop_at_request: bool = False, random_seed: int = 0,
+              stop_rule: str = "standard"):
+        """Returns ([BatchItem] in load order, device seconds of the solve)."""
+        params = CParams(tolerance, iteration_limit, 1e308, int(restart), int(stop_at_request),
+                         random_seed, PRECISIONS["fp64"], 0, STOP_RULES[stop_rule], 0,
+                         ctypes.POINTER(ctypes.c_int32)(), LOG_FN(), None, POLL_FN(), None)
+        items = (CBatchItem * len(self._lps))()
+        sec = np.zeros(1)
+        _check(self._lib.sankhya_gb300_batch_solve(self._h, ctypes.byref(params), items,
+                                                   _ptr(sec)))
+        out = []
+        for it in items:
+            out.append(BatchItem(it.status, STATUS_NAMES.get(it.status, str(it.status)),
+                                 bool(it.converged), it.iterations, it.attempts, it.restarts,
+                                 it.evaluations, it.objective, it.dual_bound,
+                                 it.final_residuals.as_dict(), it.spectral_norm,
+                                 it.farkas_value))
+        return out, float(sec[0])
+
+    def solution(self, index: int):
+        lp = self._lps[index]
+        x = np.zeros(lp.cols)
+        d = np.zeros(lp.cols)
+        y = np.zeros(lp.rows)
+        _check(self._lib.sankhya_gb300_batch_solution(self._h, index, _ptr(x), _ptr(d), _ptr(y)))
+        return x, d, y
 
 
 @dataclass

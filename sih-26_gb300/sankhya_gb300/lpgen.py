@@ -43,7 +43,8 @@ def _load():
         if not os.path.exists(_paths.LPGEN_LIB):
             raise RuntimeError(f"{_paths.LPGEN_LIB} is not built; run __graft_entry__.build()")
         lib = ctypes.CDLL(_paths.LPGEN_LIB)
-        for name in ("lpgen_planted_uniform", "lpgen_planted_general"):
+        for name in ("lpgen_planted_uniform", "lpgen_planted_general",
+                     "lpgen_planted_nondegenerate"):
             getattr(lib, name + "_nnz").argtypes = [ctypes.c_int32] * 3
             getattr(lib, name + "_nnz").restype = ctypes.c_int64
             getattr(lib, name).restype = ctypes.c_int32
@@ -51,6 +52,8 @@ def _load():
                                                                      ctypes.POINTER(_CLp)]
         lib.lpgen_planted_general.argtypes = [ctypes.c_int32] * 4 + [ctypes.c_uint64,
                                                                      ctypes.POINTER(_CLp)]
+        lib.lpgen_planted_nondegenerate.argtypes = [ctypes.c_int32] * 3 + [
+            ctypes.c_uint64, ctypes.POINTER(_CLp)]
         lib.lpgen_planted_blocks.argtypes = [ctypes.c_int32] * 4 + [ctypes.c_uint64,
                                                                     ctypes.POINTER(_CLp)]
         lib.lpgen_planted_blocks.restype = ctypes.c_int32
@@ -106,6 +109,17 @@ def planted_blocks(blocks: int, rows_per_block: int, cols_per_block: int, k: int
                                 ctypes.byref(c)) != 0:
         raise ValueError("planted_blocks: bad shape")
     return _finish(arrays, c, f"planted_blocks_{blocks}x{rows_per_block}x{cols_per_block}")
+
+
+def planted_nondegenerate(m: int, n: int, k: int = 5, seed: int = 1) -> LP:
+    """As planted_uniform with a unique, nondegenerate optimum (exactly m basic columns with
+    a heavy diagonal in the basis): x* and y* are differentiable in the data."""
+    lib = _load()
+    nnz = lib.lpgen_planted_nondegenerate_nnz(m, n, k)
+    arrays, c = _alloc(m, n, nnz)
+    if lib.lpgen_planted_nondegenerate(m, n, k, seed, ctypes.byref(c)) != 0:
+        raise ValueError("planted_nondegenerate: bad shape")
+    return _finish(arrays, c, f"planted_nondegenerate_{m}x{n}")
 
 
 def planted_zipf(m: int, n: int, target_nnz: int, exponent: float = 1.5, min_len: int = 2,
