@@ -187,8 +187,9 @@ def make_batch_nodes(seed=2028):
 
 
 def batched_section(device):
-    """LPs/s of the batched engine against the same LPs solved one at a time by the single-LP
-    engine (a sample of each part, extrapolated); FP64, relative KKT <= 1e-6."""
+    """LPs/s of the batched engine (mixed precision: FP32 iterations on FP64 refinement
+    rounds) against the same LPs solved one at a time by the single-LP engine's plain FP64
+    method (a sample of each part, extrapolated); relative KKT <= 1e-6."""
     from sankhya_gb300 import capi
 
     out = {}
@@ -200,7 +201,7 @@ def batched_section(device):
             eng.load(lps)
             t_load = time.perf_counter() - t0
             items, dev_s = eng.solve(tolerance=BATCH_TOLERANCE, stop_rule="relative",
-                                     iteration_limit=200000)
+                                     iteration_limit=200000, precision="mixed")
         statuses = {}
         for it in items:
             statuses[it.status_name] = statuses.get(it.status_name, 0) + 1
@@ -214,12 +215,95 @@ def batched_section(device):
                               iteration_limit=200000)
                 seq_s += r.device_seconds
         seq_rate = len(picked) / seq_s
-        out[name] = {"lps": len(lps), "device_s": dev_s, "load_s": t_load,
+        out[name] = {"lps": len(lps), "precision": "mixed", "device_s": dev_s, "load_s": t_load,
                      "lps_per_s": len(lps) / dev_s, "statuses": statuses,
                      "iterations_mean": sum(it.iterations for it in items) / len(items),
                      "sequential_lps_per_s": seq_rate,
                      "sequential_sample": len(picked),
                      "speedup_vs_sequential": (len(lps) / dev_s) / seq_rate}
+    return out
+
+
+# Differentiation: 256 planted LPs of 5,000 x 10,000 with 5 nonzeros per column and a unique,
+# nondegenerate optimum (the differentiable form of the planted generator), solved in FP64 to
+# relative KKT 1e-7 in one batch and polished at their active sets; L = w'x* + v'y* + f* with
+# w, v ~ N(0,1).
+ADJOINT_LPS = 256
+ADJOINT_SHAPE = (5000, 10000)
+
+
+def adjoint_section(device, lps_count=ADJOINT_LPS, shape=ADJOINT_SHAPE, fd_lps=2, fd_coords=8):
+    """Forward + adjoint times, and the gradients' agreement with (a) the basis solves of the
+    planted optimum (every LP, every coordinate, sparse LU on the host) and (b) central finite
+    differences through SciPy's HiGHS (a sample of coordinates)."""
+    import numpy as np
+    from sankhya_gb300 import capi, lpgen
+
+    m, n = shape
+    lps = [lpgen.planted_nondegenerate(m, n, 5, seed=5000 + k) for k in range(lps_count)]
+    rng = np.random.default_rng(4)
+    gx = [rng.standard_normal(n) for _ in lps]
+    gy = [rng.standard_normal(m) for _ in lps]
+    with capi.BatchEngine(device) as eng:
+        eng.load(lps)
+        items, fwd_s = eng.solve(tolerance=1e-7, stop_rule="relative", iteration_limit=2000000)
+        t0 = time.perf_counter()
+        items, polish_info = eng.polish()
+        polish_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        res = eng.adjoint(gx, gy, np.ones(len(lps)))
+        adj_s = time.perf_counter() - t0
+    out = {"lps": len(lps), "shape": [m, n], "forward_device_s": fwd_s, "polish_s": polish_s,
+           "adjoint_s": adj_s, "statuses": {}, "adjoint_status": {}, "cg_iterations_max": 0,
+           "polished": sum(1 for p in polish_info if p["status"] == 0)}
+    for it, r in zip(items, res):
+        out["statuses"][it.status_name] = out["statuses"].get(it.status_name, 0) + 1
+        out["adjoint_status"][str(r["status"])] = out["adjoint_status"].get(str(r["status"]), 0) + 1
+        out["cg_iterations_max"] = max(out["cg_iterations_max"], max(r["iterations"]))
+    try:
+        import scipy.sparse as sp
+        import scipy.sparse.linalg as spl
+        import scipy.optimize as so
+    except ImportError:
+        out["reference"] = "scipy unavailable"
+        return out
+    worst = 0.0
+    for lp, g_x, g_y, r in zip(lps, gx, gy, res):
+        A = sp.csc_matrix((lp.values, lp.row_index, lp.col_starts), shape=(m, n))
+        B = (lp.x0 > lp.col_lower) & (lp.x0 < lp.col_upper)
+        lu = spl.splu(A[:, B].tocsc())
+        p = lu.solve(g_x[B], trans="T")
+        q = lu.solve(g_y)
+        d = lp.col_cost - A.T @ lp.lam
+        dc = lp.x0.copy()
+        dc[B] += q
+        db = p + lp.lam
+        dbound = g_x - A.T @ p + d
+        dl = np.where(~B & (lp.x0 <= lp.col_lower), dbound, 0.0)
+        du = np.where(~B & (lp.x0 >= lp.col_upper), dbound, 0.0)
+        for got, want in ((r["dc"], dc), (r["drl"] + r["dru"], db), (r["dl"], dl),
+                          (r["du"], du)):
+            worst = max(worst, float(np.max(np.abs(got - want) / np.maximum(1.0, np.abs(want)))))
+    out["max_rel_err_vs_basis_solves"] = worst
+    fd_worst = 0.0
+    for k in range(min(fd_lps, len(lps))):
+        lp, r = lps[k], res[k]
+        A = sp.csc_matrix((lp.values, lp.row_index, lp.col_starts), shape=(m, n))
+
+        def loss(c, b, lo, up):
+            h = so.linprog(c, A_eq=A, b_eq=b, bounds=np.column_stack([lo, up]), method="highs")
+            return gx[k] @ h.x + gy[k] @ h.eqlin.marginals + h.fun
+
+        for j in rng.choice(n, fd_coords, replace=False):
+            h = 1e-6
+            cp, cm = lp.col_cost.copy(), lp.col_cost.copy()
+            cp[j] += h
+            cm[j] -= h
+            fd = (loss(cp, lp.row_lower, lp.col_lower, lp.col_upper)
+                  - loss(cm, lp.row_lower, lp.col_lower, lp.col_upper)) / (2 * h)
+            fd_worst = max(fd_worst, abs(r["dc"][j] - fd) / max(1.0, abs(fd)))
+    out["fd_max_rel_err"] = fd_worst
+    out["fd_sample"] = f"{min(fd_lps, len(lps))} LPs x {fd_coords} cost coordinates, step 1e-6"
     return out
 
 
@@ -277,6 +361,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-iterations", type=int, default=20)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-LP section")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint section")
     args = ap.parse_args()
     rank, world, local, dist = dist_setup()
     threads = os.cpu_count() or 1
@@ -365,6 +450,7 @@ def main():
         return
 
     batched = None if args.no_batch else batched_section(local)
+    adjoint = None if args.no_adjoint else adjoint_section(local)
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -400,6 +486,7 @@ def main():
         "spmv_gbs": roof,
         "lps_per_s": world / step_s,
         "batched": batched,
+        "adjoint": adjoint,
         "roofline": {"bound": "hbm", "kernel": f"{dominant}{suffix}: {kname}",
                      "achieved": roof[dominant + "_gbs"], "peak": peak, "unit": "GB/s",
                      "frac": roof[dominant + "_gbs"] / peak, "traffic": traffic,

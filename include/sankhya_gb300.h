@@ -231,8 +231,9 @@ SGB_API int sankhya_gb300_pdhg_time_kernels(sankhya_gb300_pdhg* engine, int32_t 
  * col_starts / row_index / values pointers and sizes are equal share one device copy of the
  * matrix (scaled and norm-estimated once). An LP whose dual iterate drifts along a Farkas ray
  * is reported SANKHYA_GB300_INFEASIBLE. Options: tolerance, iteration_limit, restart,
- * stop_at_request, random_seed, stop_rule; precision must be SANKHYA_GB300_FP64;
- * time_limit, interrupt, log and poll are not used. */
+ * stop_at_request, random_seed, stop_rule and precision (SANKHYA_GB300_MIXED runs the mixed
+ * method per LP: FP32 iterations on FP64 refinement rounds); time_limit, interrupt, log and
+ * poll are not used. */
 typedef struct sankhya_gb300_batch sankhya_gb300_batch;
 
 typedef struct sankhya_gb300_batch_item {
@@ -244,6 +245,7 @@ typedef struct sankhya_gb300_batch_item {
   sankhya_gb300_residuals final_residuals;
   double spectral_norm;
   double farkas_value; /* infeasible: the certificate's value over its terms' magnitude */
+  int64_t refinements; /* mixed precision: refinement rounds of this LP */
 } sankhya_gb300_batch_item;
 
 SGB_API int sankhya_gb300_batch_create(int32_t device, sankhya_gb300_batch** batch);
@@ -259,6 +261,43 @@ SGB_API int sankhya_gb300_batch_solve(sankhya_gb300_batch* batch,
 SGB_API int sankhya_gb300_batch_solution(sankhya_gb300_batch* batch, int32_t index,
                                          double* col_value, double* col_dual,
                                          double* row_dual);
+
+/* Gradients through the last batch solve (no reference counterpart: the reference has no
+ * differentiation). For L(x, y, f) at the optimum, with x = col_value, y = row_dual (the
+ * derivative of f by a row bound) and f = objective, given per LP the upstream gradients
+ * dl_dx[k] (cols), dl_dy[k] (rows) and dl_df[k], returns dL/dc, dL/d(row_lower),
+ * dL/d(row_upper), dL/d(col_lower), dL/d(col_upper) by implicit differentiation of the
+ * optimum: at the active set the PDHG fixed point reduces to two square linear systems with
+ * the basis matrix A_RB, solved on the device by preconditioned conjugate gradients on the
+ * normal equations (masked SpMVs). An equality row's dL/db is dl_drl + dl_dru (only the side
+ * its multiplier's sign names is nonzero). Any upstream pointer may be NULL (zero); any
+ * output pointer may be NULL. Minimisation LPs only (status 3 otherwise). */
+typedef struct sankhya_gb300_adjoint_info {
+  int32_t status;      /* 0 ok, 1 degenerate optimum (|B| != |R|), 2 CG not converged, 3 max */
+  int32_t basic_cols;  /* |B| */
+  int32_t active_rows; /* |R| */
+  int32_t iterations[2];
+  double residual[2];
+} sankhya_gb300_adjoint_info;
+
+/* Active-set polish of the last batch solve (no reference counterpart; it plays the part
+ * of the reference's PDHG -> interior-point polish hand-off, src/core/solve.cpp:239-308, for
+ * nondegenerate LPs): at each converged LP's active sets, x_B and the multipliers are
+ * re-solved from the basis matrix A_RB (masked conjugate gradients on the device); the
+ * polished point replaces the reported one when it is primal and dual feasible within 1e-9,
+ * and items (may be NULL) receive the new status, objective and residuals. info[k].status:
+ * 0 polished, 1 degenerate optimum, 2 CG not converged, 3 maximisation, 4 LP not converged,
+ * 5 polished point rejected. Minimisation LPs only. */
+SGB_API int sankhya_gb300_batch_polish(sankhya_gb300_batch* batch,
+                                       sankhya_gb300_batch_item* items,
+                                       sankhya_gb300_adjoint_info* info);
+
+SGB_API int sankhya_gb300_batch_adjoint(sankhya_gb300_batch* batch,
+                                        const double* const* dl_dx, const double* const* dl_dy,
+                                        const double* dl_df, double* const* dl_dc,
+                                        double* const* dl_drl, double* const* dl_dru,
+                                        double* const* dl_dl, double* const* dl_du,
+                                        sankhya_gb300_adjoint_info* info);
 
 #ifdef __cplusplus
 }

@@ -212,11 +212,31 @@ void BatchEngine::load(int count, const sankhya_gb300_lp* lps) {
 void BatchEngine::solve(const sankhya_gb300_params& p, sankhya_gb300_batch_item* items,
                         double* device_seconds) {
   require_loaded();
-  if (p.precision != SANKHYA_GB300_FP64) {
-    throw EngineError{SANKHYA_GB300_ERROR_OPTION, "batched solves run the FP64 method"};
+  if (p.precision != SANKHYA_GB300_FP64 && p.precision != SANKHYA_GB300_MIXED) {
+    throw EngineError{SANKHYA_GB300_ERROR_OPTION, "pdhg_precision must be fp64 or mixed"};
   }
+  const bool mixed = p.precision == SANKHYA_GB300_MIXED;
   SGB_CUDA(cudaSetDevice(device_));
   cudaStream_t s = stream_;
+  if (mixed && !mixed_ready_) {
+    const size_t N = static_cast<size_t>(std::max(total_n_, 1LL));
+    const size_t M = static_cast<size_t>(std::max(total_m_, 1LL));
+    long long nz = 0;
+    for (const BatchMatrix& mm : mats_) nz += mm.nnz;
+    csc_f_.allocate(static_cast<size_t>(std::max(nz, 1LL)));
+    csr_f_.allocate(static_cast<size_t>(std::max(nz, 1LL)));
+    for (DeviceArray<float>* a : {&u0_, &u1_, &u_sum_, &u_rst_, &cf_, &lf_, &uf_, &uc0_, &uc1_,
+                                  &u_best_}) {
+      a->allocate(N);
+    }
+    ud_.allocate(N);
+    for (DeviceArray<float>* a : {&v0_, &v1_, &v_sum_, &v_rst_, &gu_, &gl_, &yhat_, &vc0_, &vc1_,
+                                  &v_best_}) {
+      a->allocate(M);
+    }
+    refinements_.allocate(static_cast<size_t>(count_));
+    mixed_ready_ = true;
+  }
   // The power iteration's start vectors: the reference's std::mt19937(seed + 1) stream with
   // uniform_real_distribution(-1, 1) (src/la/scaling.cpp:168-170), one per matrix.
   std::vector<double> v0(static_cast<size_t>(std::max(mat_n_, 1LL)));
@@ -288,16 +308,53 @@ void BatchEngine::solve(const sankhya_gb300_params& p, sankhya_gb300_batch_item*
   b.stop_at_request = p.stop_at_request != 0;
   b.stop_rule = p.stop_rule == SANKHYA_GB300_STOP_RELATIVE ? 1 : 0;
   b.detect_infeasibility = 1;
+  if (mixed) {
+    b.csc_f = csc_f_.ptr;
+    b.csr_f = csr_f_.ptr;
+    b.u0 = u0_.ptr;
+    b.u1 = u1_.ptr;
+    b.u_sum = u_sum_.ptr;
+    b.u_rst = u_rst_.ptr;
+    b.cf = cf_.ptr;
+    b.lf = lf_.ptr;
+    b.uf = uf_.ptr;
+    b.uc0 = uc0_.ptr;
+    b.uc1 = uc1_.ptr;
+    b.u_best = u_best_.ptr;
+    b.ud = ud_.ptr;
+    b.v0 = v0_.ptr;
+    b.v1 = v1_.ptr;
+    b.v_sum = v_sum_.ptr;
+    b.v_rst = v_rst_.ptr;
+    b.gu = gu_.ptr;
+    b.gl = gl_.ptr;
+    b.yhat = yhat_.ptr;
+    b.vc0 = vc0_.ptr;
+    b.vc1 = vc1_.ptr;
+    b.v_best = v_best_.ptr;
+    b.refinements = refinements_.ptr;
+  }
 
+  buffers_ = b;
   SGB_CUDA(cudaEventRecord(timing_[0], s));
   const int scale_grid = std::max(1, std::min(b.nmatrices, num_sms_ * 8));
   launch_batch_scaling(b, scale_grid, s);
-  const int solve_grid = std::max(1, std::min(count_, num_sms_ * batch_blocks_per_sm()));
-  launch_batch_solve(b, solve_grid, s);
+  if (mixed) {
+    const int grid = std::max(1, std::min(count_, num_sms_ * batch_mixed_blocks_per_sm()));
+    launch_batch_solve_mixed(b, grid, s);
+  } else {
+    const int grid = std::max(1, std::min(count_, num_sms_ * batch_blocks_per_sm()));
+    launch_batch_solve(b, grid, s);
+  }
   SGB_CUDA(cudaGetLastError());
   SGB_CUDA(cudaEventRecord(timing_[1], s));
   std::vector<BatchOutcome> out(static_cast<size_t>(count_));
   std::vector<BatchMatrix> mats(mats_.size());
+  std::vector<long long> rounds(static_cast<size_t>(count_), 0);
+  if (mixed) {
+    SGB_CUDA(cudaMemcpyAsync(rounds.data(), refinements_.ptr, rounds.size() * sizeof(long long),
+                             cudaMemcpyDeviceToHost, s));
+  }
   SGB_CUDA(cudaMemcpyAsync(out.data(), outcome_.ptr, out.size() * sizeof(BatchOutcome),
                            cudaMemcpyDeviceToHost, s));
   SGB_CUDA(cudaMemcpyAsync(mats.data(), d_mats_out_.ptr, mats.size() * sizeof(BatchMatrix),
@@ -324,6 +381,7 @@ void BatchEngine::solve(const sankhya_gb300_params& p, sankhya_gb300_batch_item*
                                                  f.gap_as_verified,  f.complementarity};
     it.spectral_norm = mats[static_cast<size_t>(inst_[static_cast<size_t>(k)].matrix)].spectral_norm;
     it.farkas_value = o.farkas_value;
+    it.refinements = rounds[static_cast<size_t>(k)];
   }
   solved_ = true;
 }
@@ -357,6 +415,172 @@ void BatchEngine::solution(int index, double* col_value, double* col_dual, doubl
   }
   if (row_dual) {
     for (size_t i = 0; i < m; ++i) row_dual[i] = I.sense * (-by[i]);
+  }
+}
+
+void BatchEngine::adjoint(const double* const* dl_dx, const double* const* dl_dy,
+                          const double* dl_df, double* const* dl_dc, double* const* dl_drl,
+                          double* const* dl_dru, double* const* dl_dl, double* const* dl_du,
+                          sankhya_gb300_adjoint_info* info) {
+  require_loaded();
+  if (!solved_) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no solve has run"};
+  SGB_CUDA(cudaSetDevice(device_));
+  cudaStream_t s = stream_;
+  const size_t N = static_cast<size_t>(std::max(total_n_, 1LL));
+  const size_t M = static_cast<size_t>(std::max(total_m_, 1LL));
+  ensure_adjoint_buffers();
+  // Upstream gradients, packed in the LPs' vector order.
+  std::vector<double> gx(N, 0.0), gy(M, 0.0), gf(static_cast<size_t>(count_), 0.0);
+  for (int k = 0; k < count_; ++k) {
+    const BatchInstance& I = inst_[static_cast<size_t>(k)];
+    if (dl_dx != nullptr && dl_dx[k] != nullptr) {
+      std::copy(dl_dx[k], dl_dx[k] + I.n, gx.begin() + I.col);
+    }
+    if (dl_dy != nullptr && dl_dy[k] != nullptr) {
+      std::copy(dl_dy[k], dl_dy[k] + I.m, gy.begin() + I.row);
+    }
+    if (dl_df != nullptr) gf[static_cast<size_t>(k)] = dl_df[k];
+  }
+  SGB_CUDA(cudaMemcpyAsync(a_gx_.ptr, gx.data(), N * sizeof(double), cudaMemcpyHostToDevice, s));
+  SGB_CUDA(cudaMemcpyAsync(a_gy_.ptr, gy.data(), M * sizeof(double), cudaMemcpyHostToDevice, s));
+  SGB_CUDA(cudaMemcpyAsync(a_gf_.ptr, gf.data(), gf.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, s));
+  AdjointBuffers a = adjoint_buffers();
+  SGB_CUDA(cudaMemsetAsync(d_queue_.ptr + 2, 0, sizeof(unsigned int), s));
+  const int grid = std::max(1, std::min(count_, num_sms_ * batch_blocks_per_sm()));
+  launch_batch_adjoint(buffers_, a, grid, s);
+  SGB_CUDA(cudaGetLastError());
+  finish_adjoint(dl_dc, dl_drl, dl_dru, dl_dl, dl_du, info);
+}
+
+void BatchEngine::ensure_adjoint_buffers() {
+  if (adjoint_ready_) return;
+  const size_t N = static_cast<size_t>(std::max(total_n_, 1LL));
+  const size_t M = static_cast<size_t>(std::max(total_m_, 1LL));
+  for (DeviceArray<double>* a : {&a_gx_, &a_dc_, &a_dl_, &a_du_}) a->allocate(N);
+  for (DeviceArray<double>* a : {&a_gy_, &a_drl_, &a_dru_}) a->allocate(M);
+  for (auto& a : a_cn_) a.allocate(N);
+  for (auto& a : a_rm_) a.allocate(M);
+  a_gf_.allocate(static_cast<size_t>(count_));
+  a_cs_.allocate(N);
+  a_rs_.allocate(M);
+  a_out_.allocate(static_cast<size_t>(count_));
+  adjoint_ready_ = true;
+}
+
+AdjointBuffers BatchEngine::adjoint_buffers() {
+  AdjointBuffers a{};
+  a.gx = a_gx_.ptr;
+  a.gy = a_gy_.ptr;
+  a.gf = a_gf_.ptr;
+  a.dc = a_dc_.ptr;
+  a.dl = a_dl_.ptr;
+  a.du = a_du_.ptr;
+  a.drl = a_drl_.ptr;
+  a.dru = a_dru_.ptr;
+  a.cn0 = a_cn_[0].ptr;
+  a.cn1 = a_cn_[1].ptr;
+  a.cn2 = a_cn_[2].ptr;
+  a.cn3 = a_cn_[3].ptr;
+  a.cn4 = a_cn_[4].ptr;
+  a.cn5 = a_cn_[5].ptr;
+  a.rm0 = a_rm_[0].ptr;
+  a.rm1 = a_rm_[1].ptr;
+  a.rm2 = a_rm_[2].ptr;
+  a.rm3 = a_rm_[3].ptr;
+  a.rm4 = a_rm_[4].ptr;
+  a.rm5 = a_rm_[5].ptr;
+  a.col_state = a_cs_.ptr;
+  a.row_state = a_rs_.ptr;
+  a.outcome = a_out_.ptr;
+  a.max_iterations = 20000;
+  a.cg_tolerance = 1e-13;
+  return a;
+}
+
+void BatchEngine::finish_adjoint(double* const* dl_dc, double* const* dl_drl,
+                                 double* const* dl_dru, double* const* dl_dl,
+                                 double* const* dl_du, sankhya_gb300_adjoint_info* info) {
+  cudaStream_t s = stream_;
+  const size_t N = static_cast<size_t>(std::max(total_n_, 1LL));
+  const size_t M = static_cast<size_t>(std::max(total_m_, 1LL));
+  std::vector<double> dc(N), dl(N), du(N), drl(M), dru(M);
+  std::vector<AdjointOutcome> out(static_cast<size_t>(count_));
+  SGB_CUDA(cudaMemcpyAsync(dc.data(), a_dc_.ptr, N * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaMemcpyAsync(dl.data(), a_dl_.ptr, N * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaMemcpyAsync(du.data(), a_du_.ptr, N * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaMemcpyAsync(drl.data(), a_drl_.ptr, M * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaMemcpyAsync(dru.data(), a_dru_.ptr, M * sizeof(double), cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaMemcpyAsync(out.data(), a_out_.ptr, out.size() * sizeof(AdjointOutcome),
+                           cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaStreamSynchronize(s));
+  const auto put = [](double* const* dst, int k, const std::vector<double>& src, long long off,
+                      int len) {
+    if (dst != nullptr && dst[k] != nullptr) {
+      std::copy(src.begin() + off, src.begin() + off + len, dst[k]);
+    }
+  };
+  for (int k = 0; k < count_; ++k) {
+    const BatchInstance& I = inst_[static_cast<size_t>(k)];
+    put(dl_dc, k, dc, I.col, I.n);
+    put(dl_dl, k, dl, I.col, I.n);
+    put(dl_du, k, du, I.col, I.n);
+    put(dl_drl, k, drl, I.row, I.m);
+    put(dl_dru, k, dru, I.row, I.m);
+    if (info != nullptr) {
+      const AdjointOutcome& o = out[static_cast<size_t>(k)];
+      info[k].status = o.status;
+      info[k].basic_cols = o.basic_cols;
+      info[k].active_rows = o.active_rows;
+      info[k].iterations[0] = o.iterations[0];
+      info[k].iterations[1] = o.iterations[1];
+      info[k].residual[0] = o.residual[0];
+      info[k].residual[1] = o.residual[1];
+    }
+  }
+}
+
+void BatchEngine::polish(sankhya_gb300_batch_item* items, sankhya_gb300_adjoint_info* info) {
+  require_loaded();
+  if (!solved_) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no solve has run"};
+  SGB_CUDA(cudaSetDevice(device_));
+  cudaStream_t s = stream_;
+  ensure_adjoint_buffers();
+  AdjointBuffers a = adjoint_buffers();
+  SGB_CUDA(cudaMemsetAsync(d_queue_.ptr + 3, 0, sizeof(unsigned int), s));
+  const int grid = std::max(1, std::min(count_, num_sms_ * batch_blocks_per_sm()));
+  launch_batch_polish(buffers_, a, grid, s);
+  SGB_CUDA(cudaGetLastError());
+  std::vector<BatchOutcome> out(static_cast<size_t>(count_));
+  std::vector<AdjointOutcome> pol(static_cast<size_t>(count_));
+  SGB_CUDA(cudaMemcpyAsync(out.data(), outcome_.ptr, out.size() * sizeof(BatchOutcome),
+                           cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaMemcpyAsync(pol.data(), a_out_.ptr, pol.size() * sizeof(AdjointOutcome),
+                           cudaMemcpyDeviceToHost, s));
+  SGB_CUDA(cudaStreamSynchronize(s));
+  for (int k = 0; k < count_; ++k) {
+    const BatchOutcome& o = out[static_cast<size_t>(k)];
+    if (items != nullptr) {
+      sankhya_gb300_batch_item& it = items[k];
+      it.status = o.status;
+      it.objective = o.objective;
+      it.dual_bound = o.dual_bound;
+      const Residuals& f = o.final_residuals;
+      it.final_residuals = sankhya_gb300_residuals{f.primal,          f.dual,           f.gap,
+                                                   f.primal_objective, f.dual_objective,
+                                                   f.absolute_primal,  f.absolute_dual,
+                                                   f.gap_as_verified,  f.complementarity};
+    }
+    if (info != nullptr) {
+      const AdjointOutcome& p = pol[static_cast<size_t>(k)];
+      info[k].status = p.status;
+      info[k].basic_cols = p.basic_cols;
+      info[k].active_rows = p.active_rows;
+      info[k].iterations[0] = p.iterations[0];
+      info[k].iterations[1] = p.iterations[1];
+      info[k].residual[0] = p.residual[0];
+      info[k].residual[1] = p.residual[1];
+    }
   }
 }
 

@@ -12,6 +12,10 @@
 // their bounds): the matrix is stored, scaled and its norm estimated once, by a first
 // persistent launch over the distinct matrices, and the LPs keep only their own vectors.
 //
+// With precision MIXED each block runs the mixed method of the single-LP engine on its LP: FP32
+// PDHG on the correction problem around an FP64 anchor, the anchor moved at every inner
+// restart, and the exact FP64 evaluation deciding convergence (mixed.cuh).
+//
 // An LP whose iterates drift along a dual ray is reported infeasible: at every evaluation
 // the change of the dual iterate since the restart anchor, d, is tested as a Farkas
 // certificate of the unscaled problem (min over the box of (A^T d)'x minus the support of
@@ -78,14 +82,48 @@ struct BatchBuffers {
   double *y0, *y1, *y_sum, *y_rst, *yu0, *yu1, *best_y;
   double* ray;  // the unscaled dual change tested as a Farkas certificate (m per LP)
   BatchOutcome* outcome;
+  // Mixed precision (FP32 inner loop on FP64 refinement rounds; see k_batch_solve_mixed).
+  float *csc_f, *csr_f;                                   // scaled values in FP32 (per matrix)
+  float *u0, *u1, *u_sum, *u_rst, *cf, *lf, *uf, *uc0, *uc1, *u_best;  // n per LP
+  float2* ud;                                             // (2u' - u, u' - u), n per LP
+  float *v0, *v1, *v_sum, *v_rst, *gu, *gl, *yhat, *vc0, *vc1, *v_best;  // m per LP
+  long long* refinements;                                 // rounds per LP
   // Options.
   double tolerance;
   long long iteration_limit;
   int use_restarts, stop_at_request, stop_rule, detect_infeasibility;
 };
 
+// The adjoint of a solved batch (batch_kernels.cu, k_batch_adjoint): per LP, upstream
+// gradients g_x = dL/dx* (n), g_y = dL/dy* (m, y* the row multipliers as reported, dL/db = y*
+// for f*) and g_f = dL/df*, and the gradients of L with respect to the cost, the row bounds
+// and the column bounds.
+struct AdjointOutcome {
+  int basic_cols, active_rows;  // |B| and |R|: equal for a nondegenerate optimum
+  int iterations[2];            // conjugate-gradient iterations of the two solves
+  double residual[2];           // their final relative residuals
+  int status;  // 0 ok, 1 degenerate (|B| != |R|), 2 not converged, 3 maximisation (unsupported)
+};
+
+struct AdjointBuffers {
+  const double *gx, *gy, *gf;                      // upstream (gx, gy per LP slices; gf per LP)
+  double *dc, *dl, *du, *drl, *dru;                // results
+  double *cn0, *cn1, *cn2, *cn3, *cn4, *cn5;       // n-sized scratch per LP
+  double *rm0, *rm1, *rm2, *rm3, *rm4, *rm5;       // m-sized scratch per LP
+  signed char *col_state, *row_state;              // active sets
+  AdjointOutcome* outcome;
+  int max_iterations;
+  double cg_tolerance;
+};
+
 void launch_batch_scaling(const BatchBuffers& b, int grid, cudaStream_t s);
+void launch_batch_adjoint(const BatchBuffers& b, const AdjointBuffers& a, int grid,
+                          cudaStream_t s);
+void launch_batch_polish(const BatchBuffers& b, const AdjointBuffers& a, int grid,
+                         cudaStream_t s);
 void launch_batch_solve(const BatchBuffers& b, int grid, cudaStream_t s);
+void launch_batch_solve_mixed(const BatchBuffers& b, int grid, cudaStream_t s);
+int batch_mixed_blocks_per_sm();
 int batch_blocks_per_sm();
 
 }  // namespace sgb

@@ -19,11 +19,22 @@ class BatchEngine {
   void solve(const sankhya_gb300_params& params, sankhya_gb300_batch_item* items,
              double* device_seconds);
   void solution(int index, double* col_value, double* col_dual, double* row_dual);
+  void adjoint(const double* const* dl_dx, const double* const* dl_dy, const double* dl_df,
+               double* const* dl_dc, double* const* dl_drl, double* const* dl_dru,
+               double* const* dl_dl, double* const* dl_du, sankhya_gb300_adjoint_info* info);
+  // Refines every converged, nondegenerate LP's reported point by its active-set solve;
+  // items (load order) receive the new statuses, objectives and residuals.
+  void polish(sankhya_gb300_batch_item* items, sankhya_gb300_adjoint_info* info);
   int count() const { return count_; }
   int distinct_matrices() const { return static_cast<int>(mats_.size()); }
 
  private:
   void require_loaded() const;
+  void ensure_adjoint_buffers();
+  AdjointBuffers adjoint_buffers();
+  void finish_adjoint(double* const* dl_dc, double* const* dl_drl, double* const* dl_dru,
+                      double* const* dl_dl, double* const* dl_du,
+                      sankhya_gb300_adjoint_info* info);
 
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
@@ -47,6 +58,20 @@ class BatchEngine {
   DeviceArray<double2> xd_;
   DeviceArray<double> y0_, y1_, y_sum_, y_rst_, yu0_, yu1_, best_y_, ray_;
   DeviceArray<BatchOutcome> outcome_;
+  // Mixed precision (allocated on the first mixed solve).
+  bool mixed_ready_ = false;
+  DeviceArray<float> csc_f_, csr_f_;
+  DeviceArray<float> u0_, u1_, u_sum_, u_rst_, cf_, lf_, uf_, uc0_, uc1_, u_best_;
+  DeviceArray<float2> ud_;
+  DeviceArray<float> v0_, v1_, v_sum_, v_rst_, gu_, gl_, yhat_, vc0_, vc1_, v_best_;
+  DeviceArray<long long> refinements_;
+  BatchBuffers buffers_{};  // of the last solve
+  // Adjoint (allocated on first use).
+  bool adjoint_ready_ = false;
+  DeviceArray<double> a_gx_, a_gy_, a_gf_, a_dc_, a_dl_, a_du_, a_drl_, a_dru_;
+  DeviceArray<double> a_cn_[6], a_rm_[6];
+  DeviceArray<signed char> a_cs_, a_rs_;
+  DeviceArray<AdjointOutcome> a_out_;
   long long total_n_ = 0, total_m_ = 0, mat_n_ = 0, mat_m_ = 0;
 };
 

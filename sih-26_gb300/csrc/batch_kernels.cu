@@ -138,6 +138,10 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_scale(BatchBuffers b) {
       const double a = fabs(cv[k]);
       mx[0] = dmax(mx[0], a);
       mx[1] = dmax(mx[1], -a);
+      if (b.csc_f != nullptr) {  // the mixed method's FP32 copies
+        b.csc_f[M.nz + k] = static_cast<float>(cv[k]);
+        b.csr_f[M.nz + k] = static_cast<float>(rv[k]);
+      }
     }
     double mo[2];
     block_max<2>(mx, scratch, mo);
@@ -439,13 +443,23 @@ __device__ void b_evaluate(const LpView& v, Ctl* c, double* scratch, bool fin) {
 // value > 0 proves the primal infeasible (for a feasible x0, r'x0 = d'(A x0) <= the support
 // term, so value <= 0). A term whose bound is absent with a nonzero coefficient makes the
 // value -inf (not a certificate). Returns value / (sum of |terms|), or -1 (thread 0).
+__device__ double b_farkas_ray(const LpView& v, double* scratch);
+
 __device__ double b_farkas(const LpView& v, Ctl* c, double* scratch) {
-  const int T = blockDim.x, t = threadIdx.x;
   const int cur = c->cur;
+  for (int i = threadIdx.x; i < v.m; i += blockDim.x) {
+    v.ray[i] = (v.y[cur][i] - v.y_rst[i]) * v.dr[i];
+  }
+  __syncthreads();
+  return b_farkas_ray(v, scratch);
+}
+
+// The same test of the direction already in v.ray.
+__device__ double b_farkas_ray(const LpView& v, double* scratch) {
+  const int T = blockDim.x, t = threadIdx.x;
   double acc[3] = {0.0, 0.0, 0.0};  // value, magnitude, absent-bound flags
   for (int i = t; i < v.m; i += T) {
-    const double d = (v.y[cur][i] - v.y_rst[i]) * v.dr[i];
-    v.ray[i] = d;
+    const double d = v.ray[i];
     const double rl = v.rl[i], ru = v.ru[i];
     if (d > 0.0) {
       if (finite_bound(ru)) {
@@ -638,7 +652,954 @@ __global__ void __launch_bounds__(kBatchThreads, 4) k_batch_solve(BatchBuffers b
   }
 }
 
+// ---- Mixed precision, one LP per block ----------------------------------------------------
+// The single-LP engine's mixed method (mixed.cuh, Engine::solve_mixed) restated for a block:
+// FP32 PDHG on the correction problem u = Dp (x - xbar), v = Dd (y - ybar) around an FP64
+// anchor, FP64 step size / primal weight / restart decisions and correction-form KKT
+// estimates; a round ends at each inner restart (the anchor moves to the current iterate)
+// or when the estimate meets the round's target (the anchor moves to the best candidate),
+// and the exact FP64 evaluation of the anchor decides convergence. The anchor lives in the
+// FP64 iterate arrays (x[0] = xbar, y[0] = ybar, y[1] = A xbar, x[1] = A' ybar).
+struct MixView {
+  float *u[2], *u_sum, *u_rst, *cf, *lf, *uf, *uc[2], *u_best;
+  float2* ud;
+  float *v[2], *v_sum, *v_rst, *gu, *gl, *yhat, *vc[2], *v_best;
+  const float *csf, *rsf;
+};
+
+__device__ MixView make_mix_view(const BatchBuffers& b, const BatchInstance& I,
+                                 const BatchMatrix& M) {
+  MixView f;
+  const long long c = I.col, r = I.row;
+  f.u[0] = b.u0 + c;
+  f.u[1] = b.u1 + c;
+  f.u_sum = b.u_sum + c;
+  f.u_rst = b.u_rst + c;
+  f.cf = b.cf + c;
+  f.lf = b.lf + c;
+  f.uf = b.uf + c;
+  f.uc[0] = b.uc0 + c;
+  f.uc[1] = b.uc1 + c;
+  f.u_best = b.u_best + c;
+  f.ud = b.ud + c;
+  f.v[0] = b.v0 + r;
+  f.v[1] = b.v1 + r;
+  f.v_sum = b.v_sum + r;
+  f.v_rst = b.v_rst + r;
+  f.gu = b.gu + r;
+  f.gl = b.gl + r;
+  f.yhat = b.yhat + r;
+  f.vc[0] = b.vc0 + r;
+  f.vc[1] = b.vc1 + r;
+  f.v_best = b.v_best + r;
+  f.csf = b.csc_f + M.nz;
+  f.rsf = b.csr_f + M.nz;
+  return f;
+}
+
+__device__ bool batch_round_stop(const Ctl* c, const Residuals& r) {
+  return worst(r) <= c->round_target;
+}
+
+// The FP32 column pass (k_primal_f's arithmetic).
+__device__ void bm_primal(const LpView& v, const MixView& f, Ctl* c, double* scratch) {
+  const int T = blockDim.x;
+  const int cur = c->cur;
+  const float* u = f.u[cur];
+  float* un = f.u[cur ^ 1];
+  const float* vv = f.v[cur];
+  const double omega = c->omega;
+  const float tau = static_cast<float>(c->eta / omega);
+  const bool add = c->pending_add != 0;
+  float mvf = 0.0f;
+  for (int j = threadIdx.x; j < v.n; j += T) {
+    float acc = 0.0f;
+    for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) acc = fmaf(f.csf[k], vv[v.ci[k]], acc);
+    const float uj = u[j];
+    if (add) f.u_sum[j] += uj;
+    const float g = f.cf[j] + acc;
+    const float unj = clamp_box(fmaf(-tau, g, uj), f.lf[j], f.uf[j]);
+    un[j] = unj;
+    const float d = unj - uj;
+    f.ud[j] = make_float2(fmaf(2.0f, unj, -uj), d);
+    mvf = fmaf(d, d, mvf);
+  }
+  double mv[1] = {static_cast<double>(mvf)}, out[1];
+  block_sum<1>(mv, scratch, out);
+  if (threadIdx.x == 0) c->mv_primal = 0.5 * omega * out[0];
+  __syncthreads();
+}
+
+// The FP32 row pass with the correction-form prox (k_dual_f's arithmetic) and the decision.
+__device__ void bm_dual(const LpView& v, const MixView& f, Ctl* c, double* scratch) {
+  const int T = blockDim.x;
+  const int cur = c->cur;
+  const float* vv = f.v[cur];
+  float* vn = f.v[cur ^ 1];
+  const double omega = c->omega;
+  const float sigma = static_cast<float>(c->eta * omega);
+  const float inv_sigma = 1.0f / sigma;
+  const bool add = c->pending_add != 0;
+  float a0 = 0.0f, a1 = 0.0f;
+  for (int i = threadIdx.x; i < v.m; i += T) {
+    float s0 = 0.0f, s1 = 0.0f;
+    for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
+      const float2 p = f.ud[v.ri[k]];
+      s0 = fmaf(f.rsf[k], p.x, s0);
+      s1 = fmaf(f.rsf[k], p.y, s1);
+    }
+    const float vi = vv[i];
+    if (add) f.v_sum[i] += vi;
+    const float gu = f.gu[i], gl = f.gl[i];
+    float vni;
+    if (gu == gl) {
+      vni = fmaf(sigma, gu + s0, vi);
+    } else {
+      const float yh = f.yhat[i];
+      const float tt = fmaf(yh + vi, inv_sigma, s0);
+      if (tt + gu > 0.0f) vni = fmaf(sigma, gu + s0, vi);
+      else if (tt + gl < 0.0f) vni = fmaf(sigma, gl + s0, vi);
+      else vni = -yh;
+    }
+    vn[i] = vni;
+    const float d = vni - vi;
+    a0 = fmaf(d, d, a0);
+    a1 = fmaf(d, s1, a1);
+  }
+  double acc[2] = {static_cast<double>(a0), static_cast<double>(a1)}, tot[2];
+  block_sum<2>(acc, scratch, tot);
+  if (threadIdx.x == 0 && c->done == kRunning) {
+    const double movement = c->mv_primal + (0.5 * tot[0]) / omega;
+    step_decision(c, movement, fabs(tot[1]));
+  }
+  __syncthreads();
+}
+
+// The inner evaluation in correction form (k_evalf_rows0 / cols / rows1) and its decisions.
+__device__ void bm_evaluate(const LpView& v, const MixView& f, Ctl* c, double* scratch) {
+  const int T = blockDim.x, t = threadIdx.x;
+  const int cur = c->cur;
+  const bool avg = c->averaged > 0;
+  const bool pend = c->pending_add != 0;
+  const float count = static_cast<float>(c->averaged);
+  const int nc = avg ? 2 : 1;
+  // s: [0] pviol0 [1] gapr0 [2] pviol1 [3] gapr1 [4] rviol0 [5] rviol1 [6] dv^2
+  //    [7] cviol0 [8] gapc0 [9] cviol1 [10] gapc1 [11] du^2 [12] c'u0 [13] c'u1
+  double s[14];
+#pragma unroll
+  for (int q = 0; q < 14; ++q) s[q] = 0.0;
+  for (int i = t; i < v.m; i += T) {
+    const float vcur = f.v[cur][i];
+    float cand[2] = {vcur, 0.0f};
+    if (avg) cand[1] = (pend ? f.v_sum[i] + vcur : f.v_sum[i]) / count;
+    const float gu = f.gu[i], gl = f.gl[i], yh = f.yhat[i];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (q >= nc) break;
+      f.vc[q][i] = cand[q];
+      const double yc = static_cast<double>(yh) + static_cast<double>(cand[q]);
+      if ((yc > 0.0 && isinf(gu)) || (yc < 0.0 && isinf(gl))) s[4 + q] += yc * yc;
+    }
+    const double d = static_cast<double>(vcur) - static_cast<double>(f.v_rst[i]);
+    s[6] += d * d;
+  }
+  __syncthreads();
+  for (int j = t; j < v.n; j += T) {
+    float sq[2] = {0.0f, 0.0f};
+    for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) {
+      const int row = v.ci[k];
+      sq[0] = fmaf(f.csf[k], f.vc[0][row], sq[0]);
+      if (avg) sq[1] = fmaf(f.csf[k], f.vc[1][row], sq[1]);
+    }
+    const float ucur = f.u[cur][j];
+    float cand[2] = {ucur, 0.0f};
+    if (avg) cand[1] = (pend ? f.u_sum[j] + ucur : f.u_sum[j]) / count;
+    const float lf = f.lf[j], uf = f.uf[j], cf = f.cf[j];
+    const double cj = v.cs[j];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (q >= nc) break;
+      f.uc[q][j] = cand[q];
+      const double d = static_cast<double>(cf) + static_cast<double>(sq[q]);
+      const double uq = static_cast<double>(cand[q]);
+      if (d > 0.0) {
+        if (isinf(lf)) s[7 + 2 * q] += d * d; else s[8 + 2 * q] += d * (uq - lf);
+      } else if (d < 0.0) {
+        if (isinf(uf)) s[7 + 2 * q] += d * d; else s[8 + 2 * q] += d * (uq - uf);
+      }
+      s[12 + q] += cj * uq;
+    }
+    const double d = static_cast<double>(ucur) - static_cast<double>(f.u_rst[j]);
+    s[11] += d * d;
+  }
+  __syncthreads();
+  for (int i = t; i < v.m; i += T) {
+    float a[2] = {0.0f, 0.0f};
+    for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
+      const int col = v.ri[k];
+      a[0] = fmaf(f.rsf[k], f.uc[0][col], a[0]);
+      if (avg) a[1] = fmaf(f.rsf[k], f.uc[1][col], a[1]);
+    }
+    const double gu = f.gu[i], gl = f.gl[i], yh = f.yhat[i];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (q >= nc) break;
+      const double aq = a[q];
+      const double eu = gu + aq;
+      const double el = -(gl + aq);
+      const double viol = dmax(0.0, dmax(eu, el));
+      s[2 * q] += viol * viol;
+      const double yc = yh + static_cast<double>(f.vc[q][i]);
+      if (yc > 0.0 && !isinf(gu)) s[2 * q + 1] += yc * eu;
+      else if (yc < 0.0 && !isinf(gl)) s[2 * q + 1] += yc * (gl + aq);
+    }
+  }
+  double tt[14];
+  block_sum<14>(s, scratch, tt);
+  if (t == 0) {
+    const double dp = c->dp, dd = c->dd;
+    auto assemble = [&](double pv, double gr, double rv, double cv, double gc, double cu) {
+      Residuals r;
+      r.absolute_primal = sqrt(pv) / dp;
+      r.primal = r.absolute_primal / (1.0 + c->bound_norm_s);
+      r.absolute_dual = sqrt(cv + rv) / dd;
+      r.dual = r.absolute_dual / (1.0 + c->cost_norm_s);
+      const double gap = (gc - gr) / (dp * dd);
+      r.primal_objective = c->pobj0 + cu / dp;
+      r.dual_objective = r.primal_objective - gap;
+      r.gap = fabs(gap) / (1.0 + fabs(r.primal_objective) + fabs(r.dual_objective));
+      r.gap_as_verified = fabs(gap) / dmax(1.0, fabs(r.primal_objective));
+      r.complementarity = 0.0;
+      return r;
+    };
+    const Residuals rc = assemble(tt[0], tt[1], tt[4], tt[7], tt[8], tt[12]);
+    Residuals ra;
+    if (avg) ra = assemble(tt[2], tt[3], tt[5], tt[9], tt[10], tt[13]);
+    tick_decisions(c, rc, avg ? &ra : nullptr, batch_round_stop, tt[11], tt[6], 1e-10, 1e10);
+  }
+  __syncthreads();
+  // The vector half of the decisions (k_evalf_apply).
+  const int copy = c->copy_best;
+  const bool restart = c->do_restart != 0;
+  if (copy != 0 || restart) {
+    const int cc = c->cur;
+    for (int j = t; j < v.n; j += T) {
+      if (copy) f.u_best[j] = f.uc[copy - 1][j];
+      if (restart) {
+        f.u_rst[j] = f.u[cc][j];
+        f.u_sum[j] = 0.0f;
+      }
+    }
+    for (int i = t; i < v.m; i += T) {
+      if (copy) f.v_best[i] = f.vc[copy - 1][i];
+      if (restart) {
+        f.v_rst[i] = f.v[cc][i];
+        f.v_sum[i] = 0.0f;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Four blocks per SM, as k_batch_solve.
+__global__ void __launch_bounds__(kBatchThreads, 4) k_batch_solve_mixed(BatchBuffers b) {
+  __shared__ double scratch[kBScratch];
+  __shared__ int s_item;
+  __shared__ Ctl s_ctl;  // the inner loop's control block
+  __shared__ Ctl s_fin;  // the exact evaluation's
+  __shared__ LpView s_view;
+  __shared__ MixView s_mix;
+  __shared__ double s_r[8];  // round scalars: [0] dp [1] dd [2] target [3..5] measures
+  __shared__ int s_flags[4];  // [0] converged [1] stop [2] infeasible [3] round source
+  const int T = blockDim.x, t = threadIdx.x;
+  Ctl* c = &s_ctl;
+  for (int w = next_item(&b.queue[1], b.ninstances, &s_item); w >= 0;
+       w = next_item(&b.queue[1], b.ninstances, &s_item)) {
+    const int li = b.order[w];
+    const BatchInstance I = b.instances[li];
+    const BatchMatrix M = b.matrices_out[I.matrix];
+    if (t == 0) {
+      s_view = make_view(b, I, M);
+      s_mix = make_mix_view(b, I, M);
+    }
+    __syncthreads();
+    const LpView& v = s_view;
+    const MixView& f = s_mix;
+    // Scaled problem, anchor at the start point, and the scaled problem's norms.
+    double nrm[2] = {0.0, 0.0};  // sum b_i^2 (scaled rows), sum c_j^2 (scaled cost)
+    for (int j = t; j < v.n; j += T) {
+      const double d = v.dc[j];
+      v.cs[j] = v.cost[j] * d;
+      const double inv = 1.0 / d;
+      const double lj = finite_bound(v.l[j]) ? v.l[j] * inv : -HUGE_VAL;
+      const double uj = finite_bound(v.u[j]) ? v.u[j] * inv : HUGE_VAL;
+      v.ls[j] = lj;
+      v.us[j] = uj;
+      const double x0 = clamp_box(0.0, lj, uj);
+      v.x[0][j] = x0;
+      v.best_x[j] = x0;
+      nrm[1] += v.cs[j] * v.cs[j];
+    }
+    for (int i = t; i < v.m; i += T) {
+      const double d = v.dr[i];
+      const double rl = finite_bound(v.rl[i]) ? v.rl[i] * d : -HUGE_VAL;
+      const double ru = finite_bound(v.ru[i]) ? v.ru[i] * d : HUGE_VAL;
+      v.rls[i] = rl;
+      v.rus[i] = ru;
+      v.y[0][i] = 0.0;
+      v.best_y[i] = 0.0;
+      const double bb = !isinf(rl) ? rl : (!isinf(ru) ? ru : 0.0);
+      nrm[0] += bb * bb;
+    }
+    double nout[2];
+    block_sum<2>(nrm, scratch, nout);
+    for (Ctl* z : {&s_ctl, &s_fin}) {
+      unsigned long long* words = reinterpret_cast<unsigned long long*>(z);
+      for (int k = t; k < static_cast<int>(sizeof(Ctl) / sizeof(unsigned long long)); k += T) {
+        words[k] = 0ull;
+      }
+    }
+    __syncthreads();
+    if (t == 0) {
+      const double norm = M.spectral_norm;
+      c->eta = norm > 0.0 ? 1.0 / norm : 1.0;
+      c->omega = 1.0;
+      c->spectral_norm = norm;
+      c->eta_ceiling = 1.0e3 / dmax(norm, 1e-12);
+      c->restart_kkt = HUGE_VAL;
+      c->tolerance = b.tolerance;
+      c->iteration_limit = b.iteration_limit;
+      c->use_restarts = b.use_restarts;
+      c->inner_mode = 1;
+      c->bound_norm_s = sqrt(nout[0]);
+      c->cost_norm_s = sqrt(nout[1]);
+      s_fin.tolerance = b.tolerance;
+      s_fin.stop_rule = b.stop_rule;
+      s_fin.stop_at_request = b.stop_at_request;
+      s_r[0] = 1.0;
+      s_r[1] = 1.0;
+      s_r[2] = 0.5 * b.tolerance;
+      s_flags[0] = s_flags[1] = s_flags[2] = 0;
+    }
+    __syncthreads();
+    long long rounds = 0;
+    int farkas_hits = 0;
+    for (;; ++rounds) {
+      // Anchor measures in FP64 on the scaled problem (k_round_measure).
+      for (int i = t; i < v.m; i += T) {
+        double acc = 0.0;
+        for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) acc = fma(v.rsv[k], v.x[0][v.ri[k]], acc);
+        v.y[1][i] = acc;
+      }
+      for (int j = t; j < v.n; j += T) {
+        double acc = 0.0;
+        for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) acc = fma(v.csv[k], v.y[0][v.ci[k]], acc);
+        v.x[1][j] = acc;
+      }
+      __syncthreads();
+      double mx[2] = {0.0, 0.0}, ob[1] = {0.0};
+      for (int i = t; i < v.m; i += T) {
+        const double a = v.y[1][i], rl = v.rls[i], ru = v.rus[i], y = v.y[0][i];
+        mx[0] = dmax(mx[0], dmax(rl - a, a - ru));
+        if (rl != ru) {
+          if (y > 0.0 && a < ru) mx[1] = dmax(mx[1], y);
+          if (y < 0.0 && a > rl) mx[1] = dmax(mx[1], -y);
+        }
+      }
+      for (int j = t; j < v.n; j += T) {
+        const double d = v.cs[j] + v.x[1][j], x = v.x[0][j], l = v.ls[j], u = v.us[j];
+        double res;
+        if (l == u) res = 0.0;
+        else if (x <= l) res = d < 0.0 ? -d : 0.0;
+        else if (x >= u) res = d > 0.0 ? d : 0.0;
+        else res = fabs(d);
+        mx[1] = dmax(mx[1], res);
+        ob[0] = fma(v.cs[j], x, ob[0]);
+      }
+      double m2[2], o1[1];
+      block_max<2>(mx, scratch, m2);
+      block_sum<1>(ob, scratch, o1);
+      if (t == 0) {
+        // Scales of this round's correction (Engine::solve_mixed): 1 / residual, at least
+        // 1, at most 1e3 times the last and 1e15 overall.
+        const double dp = s_r[0], dd = s_r[1];
+        const auto scale = [&](double residual, double prev) {
+          if (rounds == 0) return 1.0;
+          const double want = 1.0 / dmax(residual, 1e-300);
+          return dmax(1.0, dmin(dmin(want, prev * 1e3), 1e15));
+        };
+        const double dpn = scale(m2[0], dp), ddn = scale(m2[1], dd);
+        c->omega = dmin(dmax(c->omega * (ddn / dd) / (dpn / dp), 1e-10), 1e10);
+        s_r[0] = dpn;
+        s_r[1] = ddn;
+        c->dp = dpn;
+        c->dd = ddn;
+        c->pobj0 = o1[0];
+        c->round_target = s_r[2];
+        c->cur = 0;
+        c->averaged = 0;
+        c->pending_add = 0;
+        c->done = kRunning;
+        c->eval_now = c->copy_best = c->do_restart = 0;
+        c->best.primal = c->best.dual = c->best.gap = HUGE_VAL;
+      }
+      __syncthreads();
+      // The correction problem (k_round_build) and its zero start.
+      {
+        const double dp = s_r[0], dd = s_r[1];
+        for (int j = t; j < v.n; j += T) {
+          const double x = v.x[0][j];
+          f.cf[j] = static_cast<float>(dd * (v.cs[j] + v.x[1][j]));
+          f.lf[j] = static_cast<float>(dp * (v.ls[j] - x));
+          f.uf[j] = static_cast<float>(dp * (v.us[j] - x));
+          f.u[0][j] = 0.0f;
+          f.u_sum[j] = 0.0f;
+          f.u_rst[j] = 0.0f;
+          f.u_best[j] = 0.0f;
+        }
+        for (int i = t; i < v.m; i += T) {
+          const double a = v.y[1][i];
+          f.gu[i] = static_cast<float>(dp * (a - v.rus[i]));
+          f.gl[i] = static_cast<float>(dp * (a - v.rls[i]));
+          f.yhat[i] = static_cast<float>(dd * v.y[0][i]);
+          f.v[0][i] = 0.0f;
+          f.v_sum[i] = 0.0f;
+          f.v_rst[i] = 0.0f;
+          f.v_best[i] = 0.0f;
+        }
+      }
+      __syncthreads();
+      for (;;) {
+        if (t == 0) {
+          c->eval_now = 0;
+          c->copy_best = 0;
+          c->do_restart = 0;
+          if (c->iteration >= c->iteration_limit) c->done = kIterationLimit;
+        }
+        __syncthreads();
+        if (c->done != kRunning) break;
+        bm_primal(v, f, c, scratch);
+        bm_dual(v, f, c, scratch);
+        if (c->eval_now && c->done == kRunning) bm_evaluate(v, f, c, scratch);
+      }
+      // Move the anchor: to the current iterate at a restart, else to the best candidate.
+      {
+        const bool restart = c->done == kRestartRound;
+        const int cc = c->cur;
+        const float* us = restart ? f.u[cc] : f.u_best;
+        const float* vs = restart ? f.v[cc] : f.v_best;
+        const double dp = s_r[0], dd = s_r[1];
+        for (int j = t; j < v.n; j += T) {
+          const double x = clamp_box(v.x[0][j] + static_cast<double>(us[j]) / dp, v.ls[j], v.us[j]);
+          v.x[0][j] = x;
+          v.best_x[j] = x * v.dc[j];
+        }
+        for (int i = t; i < v.m; i += T) {
+          const double step = static_cast<double>(vs[i]) / dd;
+          v.y[0][i] += step;
+          v.best_y[i] = v.y[0][i] * v.dr[i];
+          v.ray[i] = step * v.dr[i];
+        }
+      }
+      __syncthreads();
+      b_evaluate(v, &s_fin, scratch, true);
+      if (t == 0) {
+        const Residuals& fr = s_fin.final_residuals;
+        s_flags[0] = batch_stop_test(&s_fin, fr) ? 1 : 0;
+        s_flags[1] = s_flags[0] || c->done == kIterationLimit ||
+                     c->iteration >= c->iteration_limit;
+        if (!s_flags[1] && c->done == kConverged) s_r[2] *= 0.3;
+      }
+      __syncthreads();
+      if (s_flags[1]) break;
+      if (b.detect_infeasibility) {
+        const double share = b_farkas_ray(v, scratch);
+        if (t == 0) {
+          farkas_hits = share > kFarkasShare ? farkas_hits + 1 : 0;
+          if (farkas_hits >= 2) s_flags[2] = 1;
+        }
+        __syncthreads();
+        if (s_flags[2]) break;
+      }
+    }
+    if (t == 0) {
+      BatchOutcome o;
+      const Residuals& fr = s_fin.final_residuals;
+      const bool infeasible = s_flags[2] != 0;
+      const bool converged = s_flags[0] != 0 && !infeasible;
+      const bool verifiable = converged && meets_project_standard(fr);
+      o.status = infeasible ? SANKHYA_GB300_INFEASIBLE
+                            : (verifiable ? SANKHYA_GB300_OPTIMAL
+                                          : (converged ? SANKHYA_GB300_FEASIBLE
+                                                       : SANKHYA_GB300_ITERATION_LIMIT));
+      o.converged = converged;
+      o.iterations = c->iteration;
+      o.attempts = c->attempts;
+      o.restarts = c->restarts;
+      o.evaluations = c->evaluations;
+      o.final_residuals = fr;
+      o.objective = I.offset + s_fin.model_objective;
+      o.dual_bound = verifiable ? I.sense * fr.dual_objective + I.offset
+                                : (I.sense < 0.0 ? HUGE_VAL : -HUGE_VAL);
+      o.farkas_value = 0.0;
+      o.error = 0;
+      b.outcome[li] = o;
+      if (b.refinements != nullptr) b.refinements[li] = rounds + 1;
+    }
+  }
+}
+
+// ---- The adjoint ---------------------------------------------------------------------------
+// At a nondegenerate optimum with basic columns B (strictly inside their bounds), nonbasic
+// columns N at a bound and active rows R (equality rows, and inequality rows whose multiplier
+// is nonzero), the optimum moves, for small changes of the data, along
+//     A_RB dx_B = db_R - A_RN dbound_N,    A_RB' dy_R = dc_B,    dx_N = dbound_N,
+// (y the row multipliers as reported, so dy*/db = 0 and df*/db_R = y_R, df*/dc = x*,
+// df*/dbound_N = d_N, d = c - A'y the reduced costs). For L with upstream gradients g_x, g_y,
+// g_f, with p solving A_RB' p = g_x[B] and q solving A_RB q = g_y[R]:
+//     dL/dc = g_f x* + q (on B),   dL/db_R = p + g_f y_R,
+//     dL/dbound_N = g_x[N] - A_RN' p + g_f d_N,
+// and zero for inactive rows and basic columns' bounds. The two square solves run as
+// Jacobi-preconditioned conjugate gradients on the normal equations, whose operator is a
+// pair of SpMVs with A masked to R x B -- the transposed products of the PDHG step restricted
+// by the projection's Jacobian (1 on B, 0 on N).
+struct AdjView {
+  const double *gx, *gy;
+  double gf;
+  double *dc, *dl, *du, *drl, *dru;
+  double *cn[6], *rm[6];
+  signed char *cs, *rs;
+};
+
+__device__ AdjView make_adj_view(const AdjointBuffers& a, const BatchInstance& I, int li) {
+  AdjView w;
+  const long long c = I.col, r = I.row;
+  w.gx = a.gx + c;
+  w.gy = a.gy + r;
+  w.gf = a.gf[li];
+  w.dc = a.dc + c;
+  w.dl = a.dl + c;
+  w.du = a.du + c;
+  w.drl = a.drl + r;
+  w.dru = a.dru + r;
+  double* const cn[6] = {a.cn0, a.cn1, a.cn2, a.cn3, a.cn4, a.cn5};
+  double* const rm[6] = {a.rm0, a.rm1, a.rm2, a.rm3, a.rm4, a.rm5};
+  for (int k = 0; k < 6; ++k) {
+    w.cn[k] = cn[k] + c;
+    w.rm[k] = rm[k] + r;
+  }
+  w.cs = a.col_state + c;
+  w.rs = a.row_state + r;
+  return w;
+}
+
+// t (n) = M' z: t_j = sum over active rows i of A_ij z_i for basic j, 0 elsewhere.
+__device__ void masked_at(const LpView& v, const AdjView& w, const double* z, double* t) {
+  for (int j = threadIdx.x; j < v.n; j += blockDim.x) {
+    double acc = 0.0;
+    if (w.cs[j] == 0) {
+      for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) {
+        const int i = v.ci[k];
+        if (w.rs[i] != 0) acc = fma(v.craw[k], z[i], acc);
+      }
+    }
+    t[j] = acc;
+  }
+  __syncthreads();
+}
+
+// o (m) = M t: o_i = sum over basic columns j of A_ij t_j for active i, 0 elsewhere.
+__device__ void masked_a(const LpView& v, const AdjView& w, const double* t, double* o) {
+  for (int i = threadIdx.x; i < v.m; i += blockDim.x) {
+    double acc = 0.0;
+    if (w.rs[i] != 0) {
+      for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
+        const int j = v.ri[k];
+        if (w.cs[j] == 0) acc = fma(v.rraw[k], t[j], acc);
+      }
+    }
+    o[i] = acc;
+  }
+  __syncthreads();
+}
+
+// sum over k < count of a[k] b[k] (mask: entries whose state is nonzero == on), to every thread.
+__device__ double b_dot(const double* a, const double* b, int count, double* scratch) {
+  double acc[1] = {0.0}, out[1];
+  for (int k = threadIdx.x; k < count; k += blockDim.x) acc[0] = fma(a[k], b[k], acc[0]);
+  block_sum<1>(acc, scratch, out);
+  __shared__ double s_dot;
+  if (threadIdx.x == 0) s_dot = out[0];
+  __syncthreads();
+  const double r = s_dot;
+  __syncthreads();
+  return r;
+}
+
+// Preconditioned CG on K x = rhs, K = M M' (ROWS: over the rows, dimension m, entries of
+// inactive rows held at 0) or M' M (over the columns, nonbasic entries held at 0). x, r, z, p,
+// kp and prec have the system's dimension; tmp the other one. prec holds the diagonal of K.
+template <bool ROWS>
+__device__ void b_pcg(const LpView& v, const AdjView& w, const double* rhs, double* x, double* r,
+                      double* z, double* p, double* kp, const double* prec, double* tmp,
+                      double* scratch, int max_it, double tol, int* iterations, double* resid) {
+  const int dim = ROWS ? v.m : v.n;
+  const int T = blockDim.x, t = threadIdx.x;
+  for (int k = t; k < dim; k += T) {
+    const bool on = ROWS ? w.rs[k] != 0 : w.cs[k] == 0;
+    x[k] = 0.0;
+    r[k] = on ? rhs[k] : 0.0;
+    z[k] = r[k] / prec[k];
+    p[k] = z[k];
+  }
+  __syncthreads();
+  const double bnorm = sqrt(b_dot(r, r, dim, scratch));
+  double rz = b_dot(r, z, dim, scratch);
+  int it = 0;
+  double rnorm = bnorm;
+  while (bnorm > 0.0 && rnorm > tol * bnorm && it < max_it) {
+    if (ROWS) {
+      masked_at(v, w, p, tmp);
+      masked_a(v, w, tmp, kp);
+    } else {
+      masked_a(v, w, p, tmp);
+      masked_at(v, w, tmp, kp);
+    }
+    const double pkp = b_dot(p, kp, dim, scratch);
+    if (!(pkp > 0.0)) break;
+    const double alpha = rz / pkp;
+    for (int k = t; k < dim; k += T) {
+      x[k] = fma(alpha, p[k], x[k]);
+      r[k] = fma(-alpha, kp[k], r[k]);
+      z[k] = r[k] / prec[k];
+    }
+    __syncthreads();
+    rnorm = sqrt(b_dot(r, r, dim, scratch));
+    const double rz_new = b_dot(r, z, dim, scratch);
+    const double beta = rz_new / rz;
+    rz = rz_new;
+    for (int k = t; k < dim; k += T) p[k] = fma(beta, p[k], z[k]);
+    __syncthreads();
+    ++it;
+  }
+  *iterations = it;
+  *resid = bnorm > 0.0 ? rnorm / bnorm : 0.0;
+}
+
+// The active sets of a reported point (best_x, reduced costs, best_y): column states 0 basic,
+// 1 at its lower bound (also a fixed column), 2 at its upper; row states 0 inactive, 1 held at
+// row_lower, 2 at row_upper (an equality row is active, on the side its multiplier's sign
+// names). A column is nonbasic when its reduced cost exceeds 1e-6 of the largest cost, a row
+// active when its multiplier exceeds 1e-6 of the largest multiplier. Returns |B| and |R| (all
+// threads).
+__device__ void b_active_sets(const LpView& v, const AdjView& w, double* scratch, int* nb,
+                              int* nr) {
+  const int T = blockDim.x, t = threadIdx.x;
+  double mx[2] = {0.0, 0.0};
+  for (int j = t; j < v.n; j += T) mx[0] = dmax(mx[0], fabs(v.cost[j]));
+  for (int i = t; i < v.m; i += T) mx[1] = dmax(mx[1], fabs(v.best_y[i]));
+  double mo[2];
+  block_max<2>(mx, scratch, mo);
+  __shared__ double s_tau[2];
+  if (t == 0) {
+    s_tau[0] = 1e-6 * dmax(1.0, mo[0]);
+    s_tau[1] = 1e-6 * dmax(1.0, mo[1]);
+  }
+  __syncthreads();
+  double counts[2] = {0.0, 0.0};
+  for (int j = t; j < v.n; j += T) {
+    const double d = v.reduced[j];
+    signed char st = 0;
+    if (v.l[j] == v.u[j]) st = 1;
+    else if (fabs(d) > s_tau[0]) st = d > 0.0 ? 1 : 2;
+    w.cs[j] = st;
+    if (st == 0) counts[0] += 1.0;
+  }
+  for (int i = t; i < v.m; i += T) {
+    const double y = v.best_y[i];  // the solver's sign: y > 0 holds the row at its upper side
+    signed char st = 0;
+    if (v.rl[i] == v.ru[i]) st = y > 0.0 ? 2 : 1;
+    else if (fabs(y) > s_tau[1]) st = y > 0.0 ? 2 : 1;
+    w.rs[i] = st;
+    if (st != 0) counts[1] += 1.0;
+  }
+  double cnt[2];
+  block_sum<2>(counts, scratch, cnt);
+  __shared__ int s_counts[2];
+  if (t == 0) {
+    s_counts[0] = static_cast<int>(cnt[0]);
+    s_counts[1] = static_cast<int>(cnt[1]);
+  }
+  __syncthreads();
+  *nb = s_counts[0];
+  *nr = s_counts[1];
+  __syncthreads();
+}
+
+// Jacobi diagonals of the two normal-equation operators: M M' (rows) into rm[5], M' M
+// (columns) into cn[0].
+__device__ void b_jacobi(const LpView& v, const AdjView& w) {
+  const int T = blockDim.x, t = threadIdx.x;
+  for (int i = t; i < v.m; i += T) {
+    double acc = 0.0;
+    if (w.rs[i] != 0) {
+      for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
+        if (w.cs[v.ri[k]] == 0) acc = fma(v.rraw[k], v.rraw[k], acc);
+      }
+    }
+    w.rm[5][i] = acc > 0.0 ? acc : 1.0;
+  }
+  for (int j = t; j < v.n; j += T) {
+    double acc = 0.0;
+    if (w.cs[j] == 0) {
+      for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) {
+        if (w.rs[v.ci[k]] != 0) acc = fma(v.craw[k], v.craw[k], acc);
+      }
+    }
+    w.cn[0][j] = acc > 0.0 ? acc : 1.0;
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(kBatchThreads) k_batch_adjoint(BatchBuffers b, AdjointBuffers a) {
+  __shared__ double scratch[kBScratch];
+  __shared__ int s_item;
+  __shared__ LpView s_view;
+  __shared__ AdjView s_adj;
+  const int T = blockDim.x, t = threadIdx.x;
+  for (int wk = next_item(&b.queue[2], b.ninstances, &s_item); wk >= 0;
+       wk = next_item(&b.queue[2], b.ninstances, &s_item)) {
+    const int li = b.order[wk];
+    const BatchInstance I = b.instances[li];
+    const BatchMatrix M = b.matrices_out[I.matrix];
+    if (t == 0) {
+      s_view = make_view(b, I, M);
+      s_adj = make_adj_view(a, I, li);
+    }
+    __syncthreads();
+    const LpView& v = s_view;
+    const AdjView& w = s_adj;
+    int nb = 0, nr = 0;
+    b_active_sets(v, w, scratch, &nb, &nr);
+    b_jacobi(v, w);
+    // The reported multipliers are -y (minimisation) and satisfy A_RB' y_R = c_B, so
+    // q = A_RB^-1 g_y. Solve 1: (M M') z = g_y[R] over the rows, q = M' z.
+    int it1 = 0, it2 = 0;
+    double res1 = 0.0, res2 = 0.0;
+    b_pcg<true>(v, w, w.gy, w.rm[0], w.rm[1], w.rm[2], w.rm[3], w.rm[4], w.rm[5], w.cn[1],
+                scratch, a.max_iterations, a.cg_tolerance, &it1, &res1);
+    masked_at(v, w, w.rm[0], w.cn[1]);  // q (on B)
+    for (int j = t; j < v.n; j += T) {
+      const double x = v.best_x[j];
+      w.dc[j] = fma(w.gf, x, w.cs[j] == 0 ? w.cn[1][j] : 0.0);
+    }
+    __syncthreads();
+    // Solve 2: (M' M) z' = g_x[B] over the columns, p = M z'.
+    b_pcg<false>(v, w, w.gx, w.cn[1], w.cn[2], w.cn[3], w.cn[4], w.cn[5], w.cn[0], w.rm[1],
+                 scratch, a.max_iterations, a.cg_tolerance, &it2, &res2);
+    masked_a(v, w, w.cn[1], w.rm[2]);  // p (on R)
+    for (int i = t; i < v.m; i += T) {
+      const signed char st = w.rs[i];
+      const double yrep = -v.best_y[i];  // the reported multiplier
+      const double g = st != 0 ? w.rm[2][i] + w.gf * yrep : 0.0;
+      w.drl[i] = st == 1 ? g : 0.0;
+      w.dru[i] = st == 2 ? g : 0.0;
+    }
+    for (int j = t; j < v.n; j += T) {
+      const signed char st = w.cs[j];
+      double g = 0.0;
+      if (st != 0) {
+        double atp = 0.0;
+        for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) {
+          const int i = v.ci[k];
+          if (w.rs[i] != 0) atp = fma(v.craw[k], w.rm[2][i], atp);
+        }
+        g = w.gx[j] - atp + w.gf * v.reduced[j];
+      }
+      w.dl[j] = st == 1 ? g : 0.0;
+      w.du[j] = st == 2 ? g : 0.0;
+    }
+    if (t == 0) {
+      AdjointOutcome o;
+      o.basic_cols = nb;
+      o.active_rows = nr;
+      o.iterations[0] = it1;
+      o.iterations[1] = it2;
+      o.residual[0] = res1;
+      o.residual[1] = res2;
+      o.status = I.sense < 0.0 ? 3
+                 : nb != nr
+                     ? 1
+                     : ((res1 > 100.0 * a.cg_tolerance || res2 > 100.0 * a.cg_tolerance) ? 2
+                                                                                        : 0);
+      a.outcome[li] = o;
+    }
+  }
+}
+
+// Active-set polish of a batch solve (the PDHG -> basis hand-off): at the reported point's
+// active sets, x_B solves A_RB x_B = b_R - A_RN x_N (x_N at its bounds) and the multipliers
+// solve A_RB' y_R = c_B (y = 0 off R), both by the masked conjugate gradients above. The
+// polished point replaces the reported one when the optimum is nondegenerate (|B| = |R|) and
+// the point is primal and dual feasible within 1e-9 (relative); the final evaluation then
+// runs on it and the outcome's residuals, objective and status are rewritten.
+// AdjointOutcome.status: 0 polished, 1 degenerate, 2 CG not converged, 3 maximisation,
+// 4 not a converged solve, 5 the polished point failed the feasibility checks.
+__global__ void __launch_bounds__(kBatchThreads) k_batch_polish(BatchBuffers b, AdjointBuffers a) {
+  __shared__ double scratch[kBScratch];
+  __shared__ int s_item;
+  __shared__ LpView s_view;
+  __shared__ AdjView s_adj;
+  __shared__ Ctl s_ctl;
+  const int T = blockDim.x, t = threadIdx.x;
+  for (int wk = next_item(&b.queue[3], b.ninstances, &s_item); wk >= 0;
+       wk = next_item(&b.queue[3], b.ninstances, &s_item)) {
+    const int li = b.order[wk];
+    const BatchInstance I = b.instances[li];
+    const BatchMatrix M = b.matrices_out[I.matrix];
+    if (t == 0) {
+      s_view = make_view(b, I, M);
+      s_adj = make_adj_view(a, I, li);
+    }
+    __syncthreads();
+    const LpView& v = s_view;
+    const AdjView& w = s_adj;
+    const BatchOutcome before = b.outcome[li];
+    int nb = 0, nr = 0;
+    b_active_sets(v, w, scratch, &nb, &nr);
+    AdjointOutcome o{};
+    o.basic_cols = nb;
+    o.active_rows = nr;
+    const bool solved = before.status == SANKHYA_GB300_OPTIMAL ||
+                        before.status == SANKHYA_GB300_FEASIBLE;
+    if (I.sense < 0.0 || nb != nr || !solved) {
+      if (t == 0) {
+        o.status = I.sense < 0.0 ? 3 : (!solved ? 4 : 1);
+        a.outcome[li] = o;
+      }
+      continue;
+    }
+    b_jacobi(v, w);
+    // Right-hand sides: rm[4] = b_R - A_RN x_N over the rows; cn[2] = c_B over the columns.
+    for (int i = t; i < v.m; i += T) {
+      const signed char st = w.rs[i];
+      double r = 0.0;
+      if (st != 0) {
+        r = st == 1 ? v.rl[i] : v.ru[i];
+        for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
+          const signed char cj = w.cs[v.ri[k]];
+          if (cj != 0) r -= v.rraw[k] * (cj == 1 ? v.l[v.ri[k]] : v.u[v.ri[k]]);
+        }
+      }
+      w.rm[4][i] = r;
+    }
+    for (int j = t; j < v.n; j += T) w.cn[2][j] = w.cs[j] == 0 ? v.cost[j] : 0.0;
+    __syncthreads();
+    int it1 = 0, it2 = 0;
+    double res1 = 0.0, res2 = 0.0;
+    // x_B = M' z, (M M') z = rhs. The right-hand side doubles as the operator's output
+    // buffer: b_pcg reads it only before the first product.
+    b_pcg<true>(v, w, w.rm[4], w.rm[0], w.rm[1], w.rm[2], w.rm[3], w.rm[4], w.rm[5], w.cn[1],
+                scratch, a.max_iterations, a.cg_tolerance, &it1, &res1);
+    masked_at(v, w, w.rm[0], v.xu[1]);  // x_B (0 off B)
+    // y_R = M z', (M' M) z' = c_B.
+    b_pcg<false>(v, w, w.cn[2], w.cn[1], w.cn[3], w.cn[4], w.cn[5], w.cn[2], w.cn[0], w.rm[1],
+                 scratch, a.max_iterations, a.cg_tolerance, &it2, &res2);
+    masked_a(v, w, w.cn[1], w.rm[2]);  // the reported multipliers y_R (0 off R)
+    // The polished point into xu[1] (columns) and yu[1] (the solver's sign: -y), then checks.
+    double bad[1] = {0.0};
+    double cmax[1] = {0.0};
+    for (int j = t; j < v.n; j += T) cmax[0] = dmax(cmax[0], fabs(v.cost[j]));
+    double cm[1];
+    block_max<1>(cmax, scratch, cm);
+    __shared__ double s_cmax;
+    if (t == 0) s_cmax = dmax(1.0, cm[0]);
+    __syncthreads();
+    for (int j = t; j < v.n; j += T) {
+      const signed char st = w.cs[j];
+      const double lj = v.l[j], uj = v.u[j];
+      double x = st == 0 ? v.xu[1][j] : (st == 1 ? lj : uj);
+      if (st == 0) {
+        const double tol = 1e-9 * dmax(1.0, dmax(fabs(lj), fabs(uj)));
+        if ((finite_bound(lj) && x < lj - tol) || (finite_bound(uj) && x > uj + tol)) {
+          bad[0] += 1.0;
+        }
+        x = clamp_box(x, finite_bound(lj) ? lj : -HUGE_VAL, finite_bound(uj) ? uj : HUGE_VAL);
+      } else {
+        double aty = 0.0;
+        for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) aty = fma(v.craw[k], w.rm[2][v.ci[k]], aty);
+        const double d = v.cost[j] - aty;
+        const double tol = 1e-9 * s_cmax;
+        if (lj != uj && ((st == 1 && d < -tol) || (st == 2 && d > tol))) bad[0] += 1.0;
+      }
+      v.xu[1][j] = x;
+    }
+    for (int i = t; i < v.m; i += T) v.yu[1][i] = -w.rm[2][i];
+    __syncthreads();
+    for (int i = t; i < v.m; i += T) {
+      if (w.rs[i] != 0 || v.rl[i] == v.ru[i]) continue;
+      double ax = 0.0;
+      for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) ax = fma(v.rraw[k], v.xu[1][v.ri[k]], ax);
+      const double rl = v.rl[i], ru = v.ru[i];
+      const double tol = 1e-9 * dmax(1.0, dmax(finite_bound(rl) ? fabs(rl) : 0.0,
+                                               finite_bound(ru) ? fabs(ru) : 0.0));
+      if ((finite_bound(rl) && ax < rl - tol) || (finite_bound(ru) && ax > ru + tol)) {
+        bad[0] += 1.0;
+      }
+    }
+    double nbad[1];
+    block_sum<1>(bad, scratch, nbad);
+    __shared__ int s_accept;
+    if (t == 0) {
+      const bool converged = res1 <= 100.0 * a.cg_tolerance && res2 <= 100.0 * a.cg_tolerance;
+      s_accept = converged && nbad[0] == 0.0;
+      o.status = !converged ? 2 : (nbad[0] != 0.0 ? 5 : 0);
+    }
+    __syncthreads();
+    if (s_accept) {
+      for (int j = t; j < v.n; j += T) v.best_x[j] = v.xu[1][j];
+      for (int i = t; i < v.m; i += T) v.best_y[i] = v.yu[1][i];
+      {
+        unsigned long long* words = reinterpret_cast<unsigned long long*>(&s_ctl);
+        for (int k = t; k < static_cast<int>(sizeof(Ctl) / sizeof(unsigned long long)); k += T) {
+          words[k] = 0ull;
+        }
+      }
+      __syncthreads();
+      b_evaluate(v, &s_ctl, scratch, true);
+      if (t == 0) {
+        BatchOutcome out = before;
+        const Residuals& f = s_ctl.final_residuals;
+        const bool verifiable = meets_project_standard(f);
+        out.status = verifiable ? SANKHYA_GB300_OPTIMAL : SANKHYA_GB300_FEASIBLE;
+        out.final_residuals = f;
+        out.objective = I.offset + s_ctl.model_objective;
+        out.dual_bound = verifiable ? I.sense * f.dual_objective + I.offset : -HUGE_VAL;
+        b.outcome[li] = out;
+      }
+    }
+    if (t == 0) {
+      o.iterations[0] = it1;
+      o.iterations[1] = it2;
+      o.residual[0] = res1;
+      o.residual[1] = res2;
+      a.outcome[li] = o;
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace
+
+void launch_batch_adjoint(const BatchBuffers& b, const AdjointBuffers& a, int grid,
+                          cudaStream_t s) {
+  k_batch_adjoint<<<grid, kBatchThreads, 0, s>>>(b, a);
+}
+
+void launch_batch_polish(const BatchBuffers& b, const AdjointBuffers& a, int grid,
+                         cudaStream_t s) {
+  k_batch_polish<<<grid, kBatchThreads, 0, s>>>(b, a);
+}
 
 int batch_blocks_per_sm() {
   int per_sm = 0;
@@ -652,6 +1613,16 @@ void launch_batch_scaling(const BatchBuffers& b, int grid, cudaStream_t s) {
 
 void launch_batch_solve(const BatchBuffers& b, int grid, cudaStream_t s) {
   k_batch_solve<<<grid, kBatchThreads, 0, s>>>(b);
+}
+
+void launch_batch_solve_mixed(const BatchBuffers& b, int grid, cudaStream_t s) {
+  k_batch_solve_mixed<<<grid, kBatchThreads, 0, s>>>(b);
+}
+
+int batch_mixed_blocks_per_sm() {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_solve_mixed, kBatchThreads, 0);
+  return per_sm > 0 ? per_sm : 1;
 }
 
 }  // namespace sgb

@@ -222,4 +222,23 @@ SGB_API int sankhya_gb300_batch_solution(sankhya_gb300_batch* batch, int32_t ind
   return guarded([&] { batch->engine->solution(index, col_value, col_dual, row_dual); });
 }
 
+SGB_API int sankhya_gb300_batch_adjoint(sankhya_gb300_batch* batch,
+                                        const double* const* dl_dx, const double* const* dl_dy,
+                                        const double* dl_df, double* const* dl_dc,
+                                        double* const* dl_drl, double* const* dl_dru,
+                                        double* const* dl_dl, double* const* dl_du,
+                                        sankhya_gb300_adjoint_info* info) {
+  if (batch == nullptr) return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null batch");
+  return guarded([&] {
+    batch->engine->adjoint(dl_dx, dl_dy, dl_df, dl_dc, dl_drl, dl_dru, dl_dl, dl_du, info);
+  });
+}
+
+SGB_API int sankhya_gb300_batch_polish(sankhya_gb300_batch* batch,
+                                       sankhya_gb300_batch_item* items,
+                                       sankhya_gb300_adjoint_info* info) {
+  if (batch == nullptr) return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null batch");
+  return guarded([&] { batch->engine->polish(items, info); });
+}
+
 }  // extern "C"

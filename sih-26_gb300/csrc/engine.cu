@@ -81,6 +81,9 @@ template struct DeviceArray<Ctl>;
 template struct DeviceArray<BatchMatrix>;
 template struct DeviceArray<BatchInstance>;
 template struct DeviceArray<BatchOutcome>;
+template struct DeviceArray<AdjointOutcome>;
+template struct DeviceArray<signed char>;
+template struct DeviceArray<long long>;
 
 namespace {
 

@@ -81,13 +81,19 @@ class CResult(ctypes.Structure):
                 ("message", ctypes.c_char * 512)]
 
 
+class CAdjointInfo(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("basic_cols", ctypes.c_int32),
+                ("active_rows", ctypes.c_int32), ("iterations", ctypes.c_int32 * 2),
+                ("residual", ctypes.c_double * 2)]
+
+
 class CBatchItem(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("converged", ctypes.c_int32),
                 ("iterations", ctypes.c_int64), ("attempts", ctypes.c_int64),
                 ("restarts", ctypes.c_int64), ("evaluations", ctypes.c_int64),
                 ("objective", ctypes.c_double), ("dual_bound", ctypes.c_double),
                 ("final_residuals", CResiduals), ("spectral_norm", ctypes.c_double),
-                ("farkas_value", ctypes.c_double)]
+                ("farkas_value", ctypes.c_double), ("refinements", ctypes.c_int64)]
 
 
 EXPORTS = [
@@ -98,7 +104,7 @@ EXPORTS = [
     "sankhya_gb300_pdhg_scaling", "sankhya_gb300_pdhg_spmv", "sankhya_gb300_pdhg_time_kernels",
     "sankhya_gb300_pdhg_spmv_noalloc", "sankhya_gb300_batch_create",
     "sankhya_gb300_batch_destroy", "sankhya_gb300_batch_load", "sankhya_gb300_batch_solve",
-    "sankhya_gb300_batch_solution",
+    "sankhya_gb300_batch_solution", "sankhya_gb300_batch_adjoint", "sankhya_gb300_batch_polish",
 ]
 
 _lib = None
@@ -145,6 +151,11 @@ def load_library():
                                                   ctypes.POINTER(CBatchItem), _D]
         lib.sankhya_gb300_batch_solution.argtypes = [ctypes.c_void_p, ctypes.c_int32, _D, _D,
                                                      _D]
+        _PP = ctypes.POINTER(ctypes.POINTER(ctypes.c_double))
+        lib.sankhya_gb300_batch_adjoint.argtypes = [ctypes.c_void_p, _PP, _PP, _D, _PP, _PP, _PP,
+                                                    _PP, _PP, ctypes.POINTER(CAdjointInfo)]
+        lib.sankhya_gb300_batch_polish.argtypes = [ctypes.c_void_p, ctypes.POINTER(CBatchItem),
+                                                   ctypes.POINTER(CAdjointInfo)]
         lib.sankhya_gb300_pdhg_spmv_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int32,
                                                         ctypes.c_int32, ctypes.c_void_p,
                                                         ctypes.c_void_p, ctypes.c_void_p]
@@ -320,6 +331,7 @@ class BatchItem:
     residuals: dict
     spectral_norm: float
     farkas_value: float
+    refinements: int = 0
 
 
 class BatchEngine:
@@ -364,10 +376,10 @@ class BatchEngine:
 
     def solve(self, tolerance: float = 1e-4, iteration_limit: int = -1, restart: bool = True,
               stop_at_request: bool = False, random_seed: int = 0,
-              stop_rule: str = "standard"):
+              stop_rule: str = "standard", precision: str = "fp64"):
         """Returns ([BatchItem] in load order, device seconds of the solve)."""
         params = CParams(tolerance, iteration_limit, 1e308, int(restart), int(stop_at_request),
-                         random_seed, PRECISIONS["fp64"], 0, STOP_RULES[stop_rule], 0,
+                         random_seed, PRECISIONS[precision], 0, STOP_RULES[stop_rule], 0,
                          ctypes.POINTER(ctypes.c_int32)(), LOG_FN(), None, POLL_FN(), None)
         items = (CBatchItem * len(self._lps))()
         sec = np.zeros(1)
@@ -379,7 +391,7 @@ class BatchEngine:
                                  bool(it.converged), it.iterations, it.attempts, it.restarts,
                                  it.evaluations, it.objective, it.dual_bound,
                                  it.final_residuals.as_dict(), it.spectral_norm,
-                                 it.farkas_value))
+                                 it.farkas_value, it.refinements))
         return out, float(sec[0])
 
     def solution(self, index: int):
@@ -389,6 +401,61 @@ class BatchEngine:
         y = np.zeros(lp.rows)
         _check(self._lib.sankhya_gb300_batch_solution(self._h, index, _ptr(x), _ptr(d), _ptr(y)))
         return x, d, y
+
+    def polish(self):
+        """Active-set polish of the last solve (sankhya_gb300_batch_polish). Returns
+        ([BatchItem] with the polished statuses / objectives / residuals, [info dict])."""
+        n = len(self._lps)
+        items = (CBatchItem * n)()
+        info = (CAdjointInfo * n)()
+        _check(self._lib.sankhya_gb300_batch_polish(self._h, items, info))
+        out = [BatchItem(it.status, STATUS_NAMES.get(it.status, str(it.status)), True, 0, 0, 0,
+                         0, it.objective, it.dual_bound, it.final_residuals.as_dict(), 0.0, 0.0)
+               for it in items]
+        return out, [dict(status=i.status, basic_cols=i.basic_cols, active_rows=i.active_rows,
+                          iterations=tuple(i.iterations), residual=tuple(i.residual))
+                     for i in info]
+
+    def adjoint(self, dl_dx=None, dl_dy=None, dl_df=None):
+        """Gradients through the last solve (sankhya_gb300_batch_adjoint). dl_dx / dl_dy are
+        lists (one array per LP, or None) of upstream gradients with respect to col_value and
+        row_dual; dl_df a sequence of upstream gradients with respect to the objective.
+        Returns a list of dicts with dc, drl, dru, dl, du and the solve info."""
+        n = len(self._lps)
+        keep = []
+
+        def ins(arrs, size_of):
+            ptrs = (ctypes.POINTER(ctypes.c_double) * n)()
+            for k in range(n):
+                a = None if arrs is None else arrs[k]
+                if a is not None:
+                    a = np.ascontiguousarray(a, dtype=np.float64)
+                    assert a.shape == (size_of(self._lps[k]),)
+                    keep.append(a)
+                    ptrs[k] = _ptr(a)
+            return ptrs
+
+        def outs(size_of):
+            arrs = [np.zeros(size_of(lp)) for lp in self._lps]
+            ptrs = (ctypes.POINTER(ctypes.c_double) * n)(*[_ptr(a) for a in arrs])
+            return arrs, ptrs
+
+        px = ins(dl_dx, lambda lp: lp.cols)
+        py = ins(dl_dy, lambda lp: lp.rows)
+        gf = np.zeros(n) if dl_df is None else np.ascontiguousarray(dl_df, dtype=np.float64)
+        dc, pdc = outs(lambda lp: lp.cols)
+        dl, pdl = outs(lambda lp: lp.cols)
+        du, pdu = outs(lambda lp: lp.cols)
+        drl, pdrl = outs(lambda lp: lp.rows)
+        dru, pdru = outs(lambda lp: lp.rows)
+        info = (CAdjointInfo * n)()
+        _check(self._lib.sankhya_gb300_batch_adjoint(self._h, px, py, _ptr(gf), pdc, pdrl, pdru,
+                                                     pdl, pdu, info))
+        return [dict(dc=dc[k], drl=drl[k], dru=dru[k], dl=dl[k], du=du[k],
+                     status=info[k].status, basic_cols=info[k].basic_cols,
+                     active_rows=info[k].active_rows,
+                     iterations=tuple(info[k].iterations), residual=tuple(info[k].residual))
+                for k in range(n)]
 
 
 @dataclass

@@ -143,3 +143,37 @@ def test_batch_rejects_bad_lps():
         eng.load([lp])
         items, _ = eng.solve(tolerance=1e-6)
         assert items[0].status_name in ("optimal", "feasible")
+
+
+@pytest.mark.parametrize("rule", ["relative", "standard"])
+def test_batch_mixed_precision_matches_oracle(oracle, rule):
+    """The mixed method per LP (FP32 iterations on FP64 refinement rounds) reaches the
+    requested relative KKT on the FP64 evaluation, with the oracle's objective."""
+    lps = _mixed_batch()
+    tol = 1e-8
+    with capi.BatchEngine(0) as eng:
+        eng.load(lps)
+        items, _ = eng.solve(tolerance=tol, iteration_limit=400000, precision="mixed",
+                             stop_rule=rule)
+        for k, (lp, it) in enumerate(zip(lps, items)):
+            ref = oracle.solve(lp, tolerance=tol, iteration_limit=400000)
+            print(f"{k}: {it.status_name} {it.iterations} it {it.refinements} rounds; obj "
+                  f"{it.objective!r} vs {ref.objective!r}")
+            assert it.status_name in ("optimal", "feasible"), (k, it)
+            if rule == "standard":
+                assert it.status_name == "optimal", (k, it)
+            assert rel(it.objective, ref.objective) <= 1e-6
+            x, d, y = eng.solution(k)
+            res, _, red = oracle.evaluate(lp, x, -lp.sense * y)
+            assert max(res["primal"], res["dual"], res["gap"]) <= tol, (k, res)
+
+
+def test_batch_mixed_reports_infeasible_lps():
+    bad = [from_dense([[1, 1]], [5], [5], [1, 1], col_upper=[1, 1])]
+    good = [lpgen.planted_uniform(50, 100, 5, seed=8)]
+    with capi.BatchEngine(0) as eng:
+        eng.load(bad + good)
+        items, _ = eng.solve(tolerance=1e-6, iteration_limit=200000, precision="mixed",
+                             stop_rule="relative")
+    assert items[0].status_name == "infeasible"
+    assert items[1].status_name in ("optimal", "feasible")
