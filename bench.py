@@ -16,6 +16,11 @@ Also reported: each step kernel's achieved HBM GB/s against the measured copy ba
 (roofline), an end-to-end solve through the C ABI from host buffers (copies included), the
 kernels launched, clocks sampled during the timed region, and the reference algorithm (the CPU
 oracle on this host's cores) on a bounded sample, extrapolated to the FP64 iteration count.
+Two further sections: `batched` -- LPs/s of the batched engine on 4,096 independent planted
+LPs and on 1,024 branch-and-bound node relaxations of one 10,000 x 20,000 LP, against the
+same LPs solved one at a time; `adjoint` -- 256 nondegenerate 5,000 x 10,000 LPs solved,
+polished and differentiated, with the gradients checked against basis solves and finite
+differences.
 
 Multi-GPU: the path does not shard (one LP per device); N ranks run N independent replicas.
 """
@@ -225,37 +230,54 @@ def batched_section(device):
 
 
 # Differentiation: 256 planted LPs of 5,000 x 10,000 with 5 nonzeros per column and a unique,
-# nondegenerate optimum (the differentiable form of the planted generator), solved in FP64 to
-# relative KKT 1e-7 in one batch and polished at their active sets; L = w'x* + v'y* + f* with
-# w, v ~ N(0,1).
+# nondegenerate optimum (the differentiable form of the planted generator), solved in one
+# batch (mixed precision) and polished at their active sets, which puts x*, y* on the vertex
+# in FP64; L = w'x* + v'y* + f* with w, v ~ N(0,1).
 ADJOINT_LPS = 256
 ADJOINT_SHAPE = (5000, 10000)
+# The active sets of these LPs are settled long before PDHG's tail: the batch stops at this
+# relative KKT and the polish puts x*, y* on the vertex (every LP is checked afterwards).
+ADJOINT_FORWARD_TOLERANCE = 1e-4
 
 
-def adjoint_section(device, lps_count=ADJOINT_LPS, shape=ADJOINT_SHAPE, fd_lps=2, fd_coords=8):
-    """Forward + adjoint times, and the gradients' agreement with (a) the basis solves of the
-    planted optimum (every LP, every coordinate, sparse LU on the host) and (b) central finite
-    differences through SciPy's HiGHS (a sample of coordinates)."""
+def adjoint_section(device, lps_count=ADJOINT_LPS, shape=ADJOINT_SHAPE, ref_lps=16, fd_lps=2,
+                    fd_coords=4):
+    """Forward + polish + adjoint times for the whole batch, and the gradients' agreement with
+    (a) the basis solves of the planted optimum (sparse LU on the host, `ref_lps` LPs, every
+    coordinate) and (b) central finite differences of L (step 1e-6) through re-solves of the
+    perturbed LPs on the device (solve + polish, which land on the exact perturbed vertex), on
+    `fd_coords` cost coordinates of `fd_lps` LPs."""
     import numpy as np
     from sankhya_gb300 import capi, lpgen
+    from sankhya_gb300.model import LP
 
     m, n = shape
     lps = [lpgen.planted_nondegenerate(m, n, 5, seed=5000 + k) for k in range(lps_count)]
     rng = np.random.default_rng(4)
     gx = [rng.standard_normal(n) for _ in lps]
     gy = [rng.standard_normal(m) for _ in lps]
+    solve_kw = dict(tolerance=ADJOINT_FORWARD_TOLERANCE, stop_rule="relative",
+                    iteration_limit=2000000, precision="mixed")
     with capi.BatchEngine(device) as eng:
         eng.load(lps)
-        items, fwd_s = eng.solve(tolerance=1e-7, stop_rule="relative", iteration_limit=2000000)
+        items, fwd_s = eng.solve(**solve_kw)
         t0 = time.perf_counter()
         items, polish_info = eng.polish()
         polish_s = time.perf_counter() - t0
         t0 = time.perf_counter()
         res = eng.adjoint(gx, gy, np.ones(len(lps)))
         adj_s = time.perf_counter() - t0
-    out = {"lps": len(lps), "shape": [m, n], "forward_device_s": fwd_s, "polish_s": polish_s,
+        vertex_err = 0.0
+        for k in range(min(ref_lps, len(lps))):
+            x, _, y = eng.solution(k)
+            vertex_err = max(vertex_err, float(np.abs(x - lps[k].x0).max()),
+                             float(np.abs(y - lps[k].lam).max()))
+    out = {"lps": len(lps), "shape": [m, n], "forward_tolerance": ADJOINT_FORWARD_TOLERANCE,
+           "forward_device_s": fwd_s, "polish_s": polish_s,
+           "forward_iterations_mean": sum(it.iterations for it in items) / len(items),
            "adjoint_s": adj_s, "statuses": {}, "adjoint_status": {}, "cg_iterations_max": 0,
-           "polished": sum(1 for p in polish_info if p["status"] == 0)}
+           "polished": sum(1 for p in polish_info if p["status"] == 0),
+           "vertex_max_abs_err": vertex_err}
     for it, r in zip(items, res):
         out["statuses"][it.status_name] = out["statuses"].get(it.status_name, 0) + 1
         out["adjoint_status"][str(r["status"])] = out["adjoint_status"].get(str(r["status"]), 0) + 1
@@ -263,47 +285,57 @@ def adjoint_section(device, lps_count=ADJOINT_LPS, shape=ADJOINT_SHAPE, fd_lps=2
     try:
         import scipy.sparse as sp
         import scipy.sparse.linalg as spl
-        import scipy.optimize as so
     except ImportError:
-        out["reference"] = "scipy unavailable"
-        return out
-    worst = 0.0
-    for lp, g_x, g_y, r in zip(lps, gx, gy, res):
-        A = sp.csc_matrix((lp.values, lp.row_index, lp.col_starts), shape=(m, n))
-        B = (lp.x0 > lp.col_lower) & (lp.x0 < lp.col_upper)
-        lu = spl.splu(A[:, B].tocsc())
-        p = lu.solve(g_x[B], trans="T")
-        q = lu.solve(g_y)
-        d = lp.col_cost - A.T @ lp.lam
-        dc = lp.x0.copy()
-        dc[B] += q
-        db = p + lp.lam
-        dbound = g_x - A.T @ p + d
-        dl = np.where(~B & (lp.x0 <= lp.col_lower), dbound, 0.0)
-        du = np.where(~B & (lp.x0 >= lp.col_upper), dbound, 0.0)
-        for got, want in ((r["dc"], dc), (r["drl"] + r["dru"], db), (r["dl"], dl),
-                          (r["du"], du)):
-            worst = max(worst, float(np.max(np.abs(got - want) / np.maximum(1.0, np.abs(want)))))
-    out["max_rel_err_vs_basis_solves"] = worst
-    fd_worst = 0.0
+        out["basis_reference"] = "scipy unavailable"
+    else:
+        worst = 0.0
+        for lp, g_x, g_y, r in list(zip(lps, gx, gy, res))[:ref_lps]:
+            A = sp.csc_matrix((lp.values, lp.row_index, lp.col_starts), shape=(m, n))
+            B = (lp.x0 > lp.col_lower) & (lp.x0 < lp.col_upper)
+            lu = spl.splu(A[:, B].tocsc())
+            p = lu.solve(g_x[B], trans="T")
+            q = lu.solve(g_y)
+            d = lp.col_cost - A.T @ lp.lam
+            dc = lp.x0.copy()
+            dc[B] += q
+            db = p + lp.lam
+            dbound = g_x - A.T @ p + d
+            dl = np.where(~B & (lp.x0 <= lp.col_lower), dbound, 0.0)
+            du = np.where(~B & (lp.x0 >= lp.col_upper), dbound, 0.0)
+            for got, want in ((r["dc"], dc), (r["drl"] + r["dru"], db), (r["dl"], dl),
+                              (r["du"], du)):
+                worst = max(worst,
+                            float(np.max(np.abs(got - want) / np.maximum(1.0, np.abs(want)))))
+        out["max_rel_err_vs_basis_solves"] = worst
+        out["basis_reference_lps"] = min(ref_lps, len(lps))
+    # Finite differences: perturbed copies (sharing each LP's matrix) re-solved in one batch.
+    h = 1e-6
+    pert, meta = [], []
     for k in range(min(fd_lps, len(lps))):
-        lp, r = lps[k], res[k]
-        A = sp.csc_matrix((lp.values, lp.row_index, lp.col_starts), shape=(m, n))
-
-        def loss(c, b, lo, up):
-            h = so.linprog(c, A_eq=A, b_eq=b, bounds=np.column_stack([lo, up]), method="highs")
-            return gx[k] @ h.x + gy[k] @ h.eqlin.marginals + h.fun
-
+        lp = lps[k]
         for j in rng.choice(n, fd_coords, replace=False):
-            h = 1e-6
-            cp, cm = lp.col_cost.copy(), lp.col_cost.copy()
-            cp[j] += h
-            cm[j] -= h
-            fd = (loss(cp, lp.row_lower, lp.col_lower, lp.col_upper)
-                  - loss(cm, lp.row_lower, lp.col_lower, lp.col_upper)) / (2 * h)
-            fd_worst = max(fd_worst, abs(r["dc"][j] - fd) / max(1.0, abs(fd)))
+            for sign in (1.0, -1.0):
+                c = lp.col_cost.copy()
+                c[j] += sign * h
+                pert.append(LP(m, n, lp.col_starts, lp.row_index, lp.values, c, lp.col_lower,
+                               lp.col_upper, lp.row_lower, lp.row_upper))
+                meta.append((k, int(j), sign))
+    with capi.BatchEngine(device) as eng:
+        eng.load(pert)
+        eng.solve(**solve_kw)
+        fitems, _ = eng.polish()
+        losses = []
+        for q, (k, j, sign) in enumerate(meta):
+            x, _, y = eng.solution(q)
+            losses.append(gx[k] @ x + gy[k] @ y + fitems[q].objective)
+    fd_worst = 0.0
+    for q in range(0, len(meta), 2):
+        k, j, _ = meta[q]
+        fd = (losses[q] - losses[q + 1]) / (2 * h)
+        fd_worst = max(fd_worst, abs(res[k]["dc"][j] - fd) / max(1.0, abs(fd)))
     out["fd_max_rel_err"] = fd_worst
-    out["fd_sample"] = f"{min(fd_lps, len(lps))} LPs x {fd_coords} cost coordinates, step 1e-6"
+    out["fd_sample"] = (f"{min(fd_lps, len(lps))} LPs x {fd_coords} cost coordinates, central "
+                        f"differences with step {h}, perturbed LPs re-solved and polished")
     return out
 
 

@@ -1289,37 +1289,41 @@ __device__ void b_pcg(const LpView& v, const AdjView& w, const double* rhs, doub
 // The active sets of a reported point (best_x, reduced costs, best_y): column states 0 basic,
 // 1 at its lower bound (also a fixed column), 2 at its upper; row states 0 inactive, 1 held at
 // row_lower, 2 at row_upper (an equality row is active, on the side its multiplier's sign
-// names). A column is nonbasic when its reduced cost exceeds 1e-6 of the largest cost, a row
-// active when its multiplier exceeds 1e-6 of the largest multiplier. Returns |B| and |R| (all
+// names). Strict complementarity decides, so the rule holds at a moderately accurate point:
+// a column is nonbasic when its reduced cost is larger than its distance to the bound that
+// cost pushes it against (a basic column has a small reduced cost and room on both sides, a
+// nonbasic one the reverse), and an inequality row is active when its multiplier is larger
+// than its activity's distance to the side the multiplier names. Returns |B| and |R| (all
 // threads).
 __device__ void b_active_sets(const LpView& v, const AdjView& w, double* scratch, int* nb,
                               int* nr) {
   const int T = blockDim.x, t = threadIdx.x;
-  double mx[2] = {0.0, 0.0};
-  for (int j = t; j < v.n; j += T) mx[0] = dmax(mx[0], fabs(v.cost[j]));
-  for (int i = t; i < v.m; i += T) mx[1] = dmax(mx[1], fabs(v.best_y[i]));
-  double mo[2];
-  block_max<2>(mx, scratch, mo);
-  __shared__ double s_tau[2];
-  if (t == 0) {
-    s_tau[0] = 1e-6 * dmax(1.0, mo[0]);
-    s_tau[1] = 1e-6 * dmax(1.0, mo[1]);
-  }
-  __syncthreads();
   double counts[2] = {0.0, 0.0};
   for (int j = t; j < v.n; j += T) {
-    const double d = v.reduced[j];
+    const double d = v.reduced[j], x = v.best_x[j], lj = v.l[j], uj = v.u[j];
     signed char st = 0;
-    if (v.l[j] == v.u[j]) st = 1;
-    else if (fabs(d) > s_tau[0]) st = d > 0.0 ? 1 : 2;
+    if (lj == uj) {
+      st = 1;
+    } else if (d > 0.0 && finite_bound(lj) && d > x - lj) {
+      st = 1;
+    } else if (d < 0.0 && finite_bound(uj) && -d > uj - x) {
+      st = 2;
+    }
     w.cs[j] = st;
     if (st == 0) counts[0] += 1.0;
   }
   for (int i = t; i < v.m; i += T) {
     const double y = v.best_y[i];  // the solver's sign: y > 0 holds the row at its upper side
+    const double rl = v.rl[i], ru = v.ru[i];
     signed char st = 0;
-    if (v.rl[i] == v.ru[i]) st = y > 0.0 ? 2 : 1;
-    else if (fabs(y) > s_tau[1]) st = y > 0.0 ? 2 : 1;
+    if (rl == ru) {
+      st = y > 0.0 ? 2 : 1;
+    } else {
+      double a = 0.0;
+      for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) a = fma(v.rraw[k], v.best_x[v.ri[k]], a);
+      if (y > 0.0 && finite_bound(ru) && y > ru - a) st = 2;
+      else if (y < 0.0 && finite_bound(rl) && -y > a - rl) st = 1;
+    }
     w.rs[i] = st;
     if (st != 0) counts[1] += 1.0;
   }

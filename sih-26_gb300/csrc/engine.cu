@@ -274,7 +274,6 @@ Engine::Engine(int device) : device_(device) {
   }
   SGB_CUDA(cudaSetDevice(device));
   SGB_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
-  SGB_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
   SGB_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device));
   SGB_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&snapshot_), 2 * sizeof(Ctl),
                          cudaHostAllocDefault));
@@ -301,7 +300,6 @@ Engine::~Engine() {
   }
   if (snapshot_ != nullptr) cudaFreeHost(snapshot_);
   if (snapshot_mixed_ != nullptr) cudaFreeHost(snapshot_mixed_);
-  if (capture_stream_ != nullptr) cudaStreamDestroy(capture_stream_);
   if (stream_ != nullptr) cudaStreamDestroy(stream_);
 }
 
@@ -409,11 +407,8 @@ void Engine::build_mixed_graphs(int steps) {
     cudaGraph_t graph = nullptr;
     SGB_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < steps; ++k) {
-      MixedBuffers mb = mixed_;
-      mb.cond = step_condition();
-      mb.use_cond = 1;
-      launch_mixed_step(mb, stream_);
-      capture_if(mb.cond, [&](cudaStream_t cs) { launch_mixed_evaluation(mixed_, cs); });
+      launch_mixed_step(mixed_, stream_);
+      launch_mixed_evaluation(mixed_, stream_);
     }
     cudaMemcpyAsync(snapshot_mixed_ + slot, ctl_mixed_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost,
                     stream_);
@@ -890,46 +885,6 @@ void Engine::init_iterates(const sankhya_gb300_params& p) {
   (void)p;
 }
 
-// During a capture on stream_: creates the conditional handle of the next step (its value
-// is 0 at every graph launch unless the step's last block sets it).
-cudaGraphConditionalHandle Engine::step_condition() {
-  cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
-  cudaGraph_t graph = nullptr;
-  SGB_CUDA(cudaStreamGetCaptureInfo(stream_, &status, nullptr, &graph, nullptr, nullptr,
-                                    nullptr));
-  cudaGraphConditionalHandle h = 0;
-  SGB_CUDA(cudaGraphConditionalHandleCreate(&h, graph, 0, cudaGraphCondAssignDefault));
-  return h;
-}
-
-// During a capture on stream_: appends an IF node on `h` after the work captured so far,
-// whose body -- captured on a second stream -- is what `body` launches, and makes the node
-// the dependency of what is captured next.
-template <typename F>
-void Engine::capture_if(cudaGraphConditionalHandle h, F body) {
-  cudaStreamCaptureStatus status = cudaStreamCaptureStatusNone;
-  cudaGraph_t graph = nullptr;
-  const cudaGraphNode_t* deps = nullptr;
-  size_t ndeps = 0;
-  SGB_CUDA(cudaStreamGetCaptureInfo(stream_, &status, nullptr, &graph, &deps, nullptr, &ndeps));
-  std::vector<cudaGraphNode_t> dep_list(deps, deps + ndeps);
-  cudaGraphNodeParams params{};
-  params.type = cudaGraphNodeTypeConditional;
-  params.conditional.handle = h;
-  params.conditional.type = cudaGraphCondTypeIf;
-  params.conditional.size = 1;
-  cudaGraphNode_t node = nullptr;
-  SGB_CUDA(cudaGraphAddNode(&node, graph, dep_list.data(), nullptr, dep_list.size(), &params));
-  cudaGraph_t inner = params.conditional.phGraph_out[0];
-  SGB_CUDA(cudaStreamBeginCaptureToGraph(capture_stream_, inner, nullptr, nullptr, 0,
-                                         cudaStreamCaptureModeRelaxed));
-  body(capture_stream_);
-  cudaGraph_t captured = nullptr;
-  SGB_CUDA(cudaStreamEndCapture(capture_stream_, &captured));
-  SGB_CUDA(cudaStreamUpdateCaptureDependencies(stream_, &node, nullptr, 1,
-                                               cudaStreamSetCaptureDependencies));
-}
-
 void Engine::build_graphs(int steps) {
   if (graph_steps_ == steps && graph_exec_[0] != nullptr) return;
   destroy_graphs();
@@ -937,11 +892,8 @@ void Engine::build_graphs(int steps) {
     cudaGraph_t graph = nullptr;
     SGB_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < steps; ++k) {
-      StepBuffers sb = step_;
-      sb.cond = step_condition();
-      sb.use_cond = 1;
-      launch_pdhg_step(sb, stream_);
-      capture_if(sb.cond, [&](cudaStream_t cs) { launch_evaluation(eval_, cs); });
+      launch_pdhg_step(step_, stream_);
+      launch_evaluation(eval_, stream_);
     }
     cudaMemcpyAsync(snapshot_ + slot, ctl_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_);
     const cudaError_t end = cudaStreamEndCapture(stream_, &graph);
@@ -1133,8 +1085,7 @@ void Engine::solve_fp64(const sankhya_gb300_params& p, sankhya_gb300_result* r, 
   SGB_CUDA(cudaEventElapsedTime(&device_ms, timing_[0], timing_[1]));
   r->device_seconds = 1e-3 * device_ms;
   launches_ = launches_setup + (kernel_launch_count() - count_after_capture) +
-              graphs_launched_ * static_cast<long long>(graph_steps_) * kStepKernels +
-              c.evaluations * kEvalKernels;
+              graphs_launched_ * static_cast<long long>(graph_steps_) * kKernelsPerStep;
   r->kernel_launches = launches_;
   r->staged_fraction[0] = step_csc_.staged;
   r->staged_fraction[1] = step_csr_.staged;
@@ -1353,8 +1304,7 @@ void Engine::solve_mixed(const sankhya_gb300_params& p, sankhya_gb300_result* r,
   SGB_CUDA(cudaEventElapsedTime(&device_ms, timing_[0], timing_[1]));
   r->device_seconds = 1e-3 * device_ms;
   launches_ = launches_setup + extra_launches_ +
-              graphs_launched_ * static_cast<long long>(mgraph_steps_) * kStepKernels +
-              c.evaluations * kEvalKernels;
+              graphs_launched_ * static_cast<long long>(mgraph_steps_) * kKernelsPerStep;
   r->kernel_launches = launches_;
   r->staged_fraction[0] = step_csc_f_.staged;
   r->staged_fraction[1] = step_csr_f_.staged;

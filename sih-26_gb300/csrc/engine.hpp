@@ -61,9 +61,6 @@ class Engine {
   void precondition(long long seed);
   double power_iteration(long long seed);
   void init_iterates(const sankhya_gb300_params& p);
-  cudaGraphConditionalHandle step_condition();
-  template <typename F>
-  void capture_if(cudaGraphConditionalHandle h, F body);
   void build_graphs(int steps);
   void build_mixed_graphs(int steps);
   void destroy_graphs();
@@ -83,7 +80,6 @@ class Engine {
 
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
-  cudaStream_t capture_stream_ = nullptr;  // captures the bodies of conditional graph nodes
   int num_sms_ = 0;
   bool loaded_ = false;
   bool solved_ = false;

@@ -108,10 +108,6 @@ struct StepBuffers {
   double* chunk_dual;    // [csr.nchunks * 2]
   int grid_primal, grid_dual;
   int smem_primal, smem_dual;  // dynamic shared memory: pipeline + staged window
-  // Inside a CUDA graph, k_dual's last block sets `cond` to 1 when the step's evaluation
-  // must run: the evaluation kernels sit in a conditional node and are skipped otherwise.
-  cudaGraphConditionalHandle cond;
-  int use_cond;
 };
 
 struct EvalBuffers {
@@ -145,8 +141,8 @@ void launch_pdhg_step(const StepBuffers& b, cudaStream_t s);
 void launch_primal_pass(const StepBuffers& b, cudaStream_t s);
 void launch_dual_pass(const StepBuffers& b, cudaStream_t s);
 // Kernels launched per attempted step inside a graph (2 step + 4 evaluation kernels).
-constexpr int kStepKernels = 2;  // k_primal, k_dual (every attempted step)
-constexpr int kEvalKernels = 4;  // the evaluation kernels (evaluation ticks only)
+constexpr int kKernelsPerStep = 6;  // k_primal, k_dual and the four evaluation kernels (which
+                                    // return at once off an evaluation tick)
 // Running count of kernel launches issued by the launchers of this file (host side).
 long long kernel_launch_count();
 // The evaluation tick (no-op on the device unless ctl->eval_now or ctl->final_mode).

@@ -60,8 +60,6 @@ struct MixedBuffers {
   int grid_primal, grid_dual;     // evaluation passes
   int grid_step_primal, grid_step_dual;  // step passes (one block per SM when staging)
   int smem_primal, smem_dual;     // step passes' dynamic shared memory
-  cudaGraphConditionalHandle cond;  // as StepBuffers::cond, set by k_dual_f
-  int use_cond;
   int m, n;
 };
 

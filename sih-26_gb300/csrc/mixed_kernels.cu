@@ -166,9 +166,6 @@ __global__ void __launch_bounds__(kWideBlockThreads) k_dual_f(MixedBuffers b) {
       const double movement = ctl->mv_primal + (0.5 * (total[0] + longs[0])) / omega;
       step_decision(ctl, movement, fabs(total[1] + longs[1]));
     }
-    if (b.use_cond) {
-      cudaGraphSetConditional(b.cond, ctl->eval_now != 0 && ctl->done == kRunning ? 1u : 0u);
-    }
   }
 }
 
