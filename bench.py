@@ -145,11 +145,30 @@ def dist_setup():
     return rank, world, local, None
 
 
-def make_workload():
+def make_workload(blocks=None):
     from sankhya_gb300 import lpgen
 
-    return lpgen.planted_blocks(WORKLOAD["blocks"], WORKLOAD["rows_per_block"],
+    return lpgen.planted_blocks(blocks or WORKLOAD["blocks"], WORKLOAD["rows_per_block"],
                                 WORKLOAD["cols_per_block"], WORKLOAD["k"], WORKLOAD["seed"])
+
+
+def profile_case(blocks, precision, iterations):
+    """The small case the kernel captures run on: the same generator with fewer periods
+    (16 periods: 250,000 x 500,000, about 5M nonzeros, matrix copies of 40-120 MB), solved for
+    a fixed number of accepted iterations. Prints one line and returns."""
+    from sankhya_gb300 import build, capi
+
+    build.build_lpgen()
+    build.build_engine()
+    lp = make_workload(blocks)
+    eng = capi.PdhgEngine(0)
+    eng.load(lp)
+    r = eng.solve(tolerance=TOLERANCE, stop_rule="relative", precision=precision,
+                  iteration_limit=iterations, steps_per_poll=8)
+    print(json.dumps({"profile_case": f"{lp.rows} x {lp.cols}, {lp.nnz} nnz",
+                      "precision": precision, "status": r.status_name,
+                      "iterations": r.iterations, "staged_share": list(r.staged_fraction)}))
+    eng.close()
 
 
 # Batched workloads: 4,096 independent planted LPs (m log-uniform in [50, 2,000], n = 2m,
@@ -394,7 +413,13 @@ def main():
     ap.add_argument("--cpu-iterations", type=int, default=20)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-LP section")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint section")
+    ap.add_argument("--profile-case", type=int, metavar="PERIODS", default=0,
+                    help="run only the small kernel-capture case with this many periods")
+    ap.add_argument("--profile-iterations", type=int, default=40)
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args.profile_case, args.precision, args.profile_iterations)
+        return
     rank, world, local, dist = dist_setup()
     threads = os.cpu_count() or 1
 

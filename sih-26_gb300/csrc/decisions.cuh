@@ -7,6 +7,24 @@
 
 namespace sgb {
 
+// Called by every block of an evaluation's last kernel once it has read the flags: the last
+// block to arrive clears them (and its ticket), after which the next step runs.
+__device__ inline void clear_evaluation_flags(Ctl* c) {
+  __shared__ bool s_last_apply;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last_apply = atomicAdd(&c->ticket[kTicketApply], 1u) == gridDim.x - 1;
+    if (s_last_apply) {
+      c->eval_now = 0;
+      c->copy_best = 0;
+      c->do_restart = 0;
+      c->ticket[kTicketApply] = 0;
+      __threadfence();
+    }
+  }
+}
+
 // Adaptive step, src/pdhg/pdhg.cpp:252-335: accept iff eta <= movement / interaction, then
 // eta <- clamp(min(shrink * limit, grow * eta), 1e-12, ceiling) unless the step carried no
 // information; an accepted step flips the current buffer and counts an iteration.

@@ -4,10 +4,11 @@
 //   setup     device Ruiz x10 + Pock-Chambolle (src/la/scaling.cpp:111-159) on both the CSC
 //             and the CSR copy, power iteration (src/la/scaling.cpp:161-194) from the same
 //             std::mt19937 start, x0 = proj(0), y0 = 0 (src/pdhg/pdhg.cpp:140-147);
-//   loop      CUDA graphs of `steps_per_poll` attempted steps, each step = k_primal + k_dual
-//             + the evaluation kernels (which return at once off the evaluation tick); the
-//             host launches graph k+1 before it reads the status snapshot graph k copied
-//             out, so the device never waits on the host;
+//   loop      CUDA graphs of `steps_per_poll` attempted steps, each step = k_primal + k_dual,
+//             with the evaluation kernels after every kEvalStride steps (a step that falls
+//             due for an evaluation holds the steps after it until the evaluation has run);
+//             the host launches graph k+1 before it reads the status snapshot graph k
+//             copied out, so the device never waits on the host;
 //   report    one final evaluation of (best_x, best_y) on the device
 //             (src/pdhg/pdhg.cpp:487-567), status and message assembled here.
 // The reference checks the clock at every step; this engine checks it, and the
@@ -326,7 +327,7 @@ void Engine::allocate_mixed() {
   csr_f_.allocate_padded(z, kPad, s);
   // kPad elements of padding, as for the FP64 vectors (staged slices and windows).
   for (DeviceArray<float>* a : {&u0f_, &u1f_, &usumf_, &urstf_, &cf_, &lf_, &uf_, &uc0_, &uc1_,
-                                &ubest_, &csf_, &ubarf_}) {
+                                &ubest_, &csf_, &duf_}) {
     a->allocate(n + kPad);
   }
   for (DeviceArray<float>* a : {&v0f_, &v1f_, &vsumf_, &vrstf_, &gu_, &gl_, &yhat_, &vc0_, &vc1_,
@@ -356,7 +357,7 @@ void Engine::fill_mixed_buffers() {
   b.v_sum = vsumf_.ptr;
   b.u_rst = urstf_.ptr;
   b.v_rst = vrstf_.ptr;
-  b.ubar = ubarf_.ptr;
+  b.du = duf_.ptr;
   b.au[0] = auf0_.ptr;
   b.au[1] = auf1_.ptr;
   b.cf = cf_.ptr;
@@ -408,7 +409,7 @@ void Engine::build_mixed_graphs(int steps) {
     SGB_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < steps; ++k) {
       launch_mixed_step(mixed_, stream_);
-      launch_mixed_evaluation(mixed_, stream_);
+      if ((k + 1) % kEvalStride == 0 || k + 1 == steps) launch_mixed_evaluation(mixed_, stream_);
     }
     cudaMemcpyAsync(snapshot_mixed_ + slot, ctl_mixed_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost,
                     stream_);
@@ -514,8 +515,8 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   int unused_chunks = 0;
   lanes_csc_ = 1;
   lanes_csr_ = 1;
-  lanes_csc_f_ = choose_lanes(n > 0 ? static_cast<double>(nnz) / n : 1.0, kWideThreads);
-  lanes_csr_f_ = choose_lanes(m > 0 ? static_cast<double>(nnz) / m : 1.0, kWideThreads);
+  lanes_csc_f_ = wide_lanes(n > 0 ? static_cast<double>(nnz) / n : 1.0, kWideThreads);
+  lanes_csr_f_ = wide_lanes(m > 0 ? static_cast<double>(nnz) / m : 1.0, kWideThreads);
   build_tiles(cptr, n, lanes_csc_, kTileThreads, &ctiles, &clongs, &nchunks_csc_);
   build_tiles(rptr, m, lanes_csr_, kTileThreads, &rtiles, &rlongs, &nchunks_csr_);
   {
@@ -893,7 +894,7 @@ void Engine::build_graphs(int steps) {
     SGB_CUDA(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     for (int k = 0; k < steps; ++k) {
       launch_pdhg_step(step_, stream_);
-      launch_evaluation(eval_, stream_);
+      if ((k + 1) % kEvalStride == 0 || k + 1 == steps) launch_evaluation(eval_, stream_);
     }
     cudaMemcpyAsync(snapshot_ + slot, ctl_.ptr, sizeof(Ctl), cudaMemcpyDeviceToHost, stream_);
     const cudaError_t end = cudaStreamEndCapture(stream_, &graph);
@@ -1085,7 +1086,7 @@ void Engine::solve_fp64(const sankhya_gb300_params& p, sankhya_gb300_result* r, 
   SGB_CUDA(cudaEventElapsedTime(&device_ms, timing_[0], timing_[1]));
   r->device_seconds = 1e-3 * device_ms;
   launches_ = launches_setup + (kernel_launch_count() - count_after_capture) +
-              graphs_launched_ * static_cast<long long>(graph_steps_) * kKernelsPerStep;
+              graphs_launched_ * graph_kernel_launches(graph_steps_);
   r->kernel_launches = launches_;
   r->staged_fraction[0] = step_csc_.staged;
   r->staged_fraction[1] = step_csr_.staged;
@@ -1304,7 +1305,7 @@ void Engine::solve_mixed(const sankhya_gb300_params& p, sankhya_gb300_result* r,
   SGB_CUDA(cudaEventElapsedTime(&device_ms, timing_[0], timing_[1]));
   r->device_seconds = 1e-3 * device_ms;
   launches_ = launches_setup + extra_launches_ +
-              graphs_launched_ * static_cast<long long>(mgraph_steps_) * kKernelsPerStep;
+              graphs_launched_ * graph_kernel_launches(mgraph_steps_);
   r->kernel_launches = launches_;
   r->staged_fraction[0] = step_csc_f_.staged;
   r->staged_fraction[1] = step_csr_f_.staged;
@@ -1331,6 +1332,7 @@ void Engine::time_kernels(int reps, double* ms) {
   Ctl run = saved;
   run.done = kRunning;
   run.final_mode = 0;
+  run.eval_now = 0;
   run.iteration_limit = std::numeric_limits<long long>::max();
   SGB_CUDA(cudaMemcpyAsync(ctl, &run, sizeof(Ctl), cudaMemcpyHostToDevice, s));
   std::vector<cudaEvent_t> ev(3 * static_cast<size_t>(reps));

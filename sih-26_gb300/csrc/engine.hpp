@@ -154,7 +154,7 @@ class Engine {
   DeviceArray<float> u0f_, u1f_, v0f_, v1f_, usumf_, vsumf_, urstf_, vrstf_;
   DeviceArray<float> cf_, lf_, uf_, gu_, gl_, yhat_, uc0_, uc1_, vc0_, vc1_, ubest_, vbest_;
   DeviceArray<float> csf_;   // scaled cost in FP32
-  DeviceArray<float> ubarf_;         // 2u' - u per column
+  DeviceArray<float> duf_;           // u' - u per column
   DeviceArray<float> auf0_, auf1_;   // A u per row, double-buffered with u
   DeviceArray<double> anchor_x_, anchor_y_, ax64_, aty64_;
   DeviceArray<Ctl> ctl_mixed_;

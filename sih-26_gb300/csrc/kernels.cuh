@@ -56,7 +56,7 @@ struct EvalRecord {
 
 // Ticket slots (last-block counters), one per reducing kernel.
 enum Ticket : int { kTicketDual = 0, kTicketEvalRows = 1, kTicketPrimal = 2, kTicketEvalCols = 3,
-                    kTicketCount = 4 };
+                    kTicketApply = 4, kTicketCount = 5 };
 
 struct Ctl {
   // Step size and primal weight, src/pdhg/pdhg.cpp:181-186.
@@ -65,7 +65,8 @@ struct Ctl {
   long long iteration_limit;
   int cur;          // which of the two x / y buffers holds the current iterate
   int pending_add;  // the last step was accepted and its iterate is not yet in the sums
-  int eval_now;     // the evaluation tick falls after this step
+  int eval_now;     // an evaluation is due: set by the step decision, cleared by the
+                    // evaluation's last kernel; steps do nothing while it is set
   int done;         // DoneCode
   int use_restarts, stop_at_request, no_information, accepted;
   int copy_best;    // 0: nothing; 1: the current candidate; 2: the average candidate
@@ -141,8 +142,17 @@ void launch_pdhg_step(const StepBuffers& b, cudaStream_t s);
 void launch_primal_pass(const StepBuffers& b, cudaStream_t s);
 void launch_dual_pass(const StepBuffers& b, cudaStream_t s);
 // Kernels launched per attempted step inside a graph (2 step + 4 evaluation kernels).
-constexpr int kKernelsPerStep = 6;  // k_primal, k_dual and the four evaluation kernels (which
-                                    // return at once off an evaluation tick)
+// A step graph holds `steps` attempted steps (k_primal + k_dual) and, after every
+// kEvalStride of them, the four evaluation kernels. A step that falls due for an evaluation
+// sets ctl->eval_now; the steps after it in the graph return at once until the evaluation
+// kernels have run and cleared the flag, so the iterates, step sizes and evaluation points
+// are those of one evaluation after every due step. The stride divides the 40-step
+// evaluation cadence, so on accepted steps the due step ends a stride and nothing is
+// skipped. Off a due step the four evaluation kernels return at once.
+constexpr int kEvalStride = 8;
+inline long long graph_kernel_launches(int steps) {
+  return 2LL * steps + 4LL * ((steps + kEvalStride - 1) / kEvalStride);
+}
 // Running count of kernel launches issued by the launchers of this file (host side).
 long long kernel_launch_count();
 // The evaluation tick (no-op on the device unless ctl->eval_now or ctl->final_mode).

@@ -36,10 +36,11 @@ struct MixedBuffers {
   float* v_sum;
   float* u_rst;
   float* v_rst;
-  float* ubar;                 // 2u' - u per column, gathered by the row pass
-  // A u of the iterate, double-buffered with u: the row pass forms A(u' - u) = (A ubar - A u)
-  // / 2 and A u' = (A ubar + A u) / 2 from the one product it gathers (u = 0, so A u = 0, at
-  // the start of every round).
+  float* du;                   // u' - u per column, gathered by the row pass
+  // A u of the iterate, double-buffered with u. The row pass gathers only du and forms
+  // A ubar = A u + 2 A du and A u' = A u + A du. The rounding that the carried sum picks up
+  // cannot build up: every evaluation (at most 40 accepted steps apart) stores A u computed
+  // afresh from u, and u = 0, so A u = 0, at the start of every round.
   float* au[2];
   const float *cf, *lf, *uf;   // correction cost and box (n)
   const float* cs;             // scaled cost c-hat (n): the objective of the correction

@@ -3,10 +3,12 @@
 // The step kernels mirror k_primal / k_dual with FP32 values, iterates and FP32-accumulated
 // products; the movement and interaction partials are promoted to FP64 at the block level,
 // and the step-size decision, restarts and primal weight (decisions.cuh) are FP64. The column
-// pass writes ubar = 2u' - u per column; the row pass gathers only ubar (4 bytes per
-// nonzero, measured markedly faster on GB300 than an 8-byte (ubar, du) gather) and gets
-// A(u' - u) from the identity A ubar = 2 A u' - A u, with A u carried per row
-// (MixedBuffers::au).
+// pass writes du = u' - u per column; the row pass gathers only du (4 bytes per nonzero,
+// measured markedly faster on GB300 than an 8-byte (ubar, du) gather) and forms
+// A ubar = A u + 2 A du with A u carried per row (MixedBuffers::au). A du comes straight
+// from the gather, so the interaction term of the step-size rule keeps FP32's relative
+// accuracy however small the step is; forming it as a difference of two large products
+// instead measured about 16% more iterations.
 #include "common.cuh"
 #include "decisions.cuh"
 #include "kernels.cuh"
@@ -42,12 +44,7 @@ __global__ void __launch_bounds__(kWideBlockThreads) k_primal_f(MixedBuffers b) 
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kScratch];
   Ctl* ctl = b.ctl;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    ctl->eval_now = 0;
-    ctl->copy_best = 0;
-    ctl->do_restart = 0;
-  }
-  if (ctl->done != kRunning) return;
+  if (ctl->done != kRunning || ctl->eval_now != 0) return;
   if (ctl->iteration >= ctl->iteration_limit) {
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->done = kIterationLimit;
     return;
@@ -76,7 +73,7 @@ __global__ void __launch_bounds__(kWideBlockThreads) k_primal_f(MixedBuffers b) 
     const float unj = clamp_box(fmaf(-tau, g, uj), pipe.row(2, j), pipe.row(3, j));
     un[j] = unj;
     const float d = unj - uj;
-    b.ubar[j] = fmaf(2.0f, unj, -uj);
+    b.du[j] = d;
     mvf = fmaf(d, d, mvf);
   };
   if (!run_tiles<1, float>(pipe, b.csc, win, b.chunk_primal, gather, epi) &&
@@ -101,7 +98,7 @@ __global__ void __launch_bounds__(kWideBlockThreads) k_dual_f(MixedBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kScratch];
   Ctl* ctl = b.ctl;
-  if (ctl->done != kRunning) return;
+  if (ctl->done != kRunning || ctl->eval_now != 0) return;
   const int cur = ctl->cur;
   float* __restrict__ vn = b.v[cur ^ 1];
   float* __restrict__ aun = b.au[cur ^ 1];
@@ -119,25 +116,26 @@ __global__ void __launch_bounds__(kWideBlockThreads) k_dual_f(MixedBuffers b) {
   pipe.rsrc[4] = b.v_sum;
   pipe.rsrc[5] = b.au[cur];
   Window<float> win;
-  win.setup(b.ubar, pipe, dsmem);
+  win.setup(b.du, pipe, dsmem);
   auto gather = [&](int col, float a, float* acc) { acc[0] = fmaf(a, win.get(col), acc[0]); };
   auto epi = [&](int i, const float* s) {
     const float vi = pipe.row(0, i);
     if (add) b.v_sum[i] = pipe.row(4, i) + vi;
     const float gu = pipe.row(1, i), gl = pipe.row(2, i);
     const float au = pipe.row(5, i);
-    const float adu = 0.5f * (s[0] - au);
-    aun[i] = 0.5f * (s[0] + au);
+    const float adu = s[0];
+    aun[i] = au + adu;
+    const float abar = fmaf(2.0f, adu, au);  // A ubar
     float vni;
     if (gu == gl) {
-      vni = fmaf(sigma, gu + s[0], vi);
+      vni = fmaf(sigma, gu + abar, vi);
     } else {
       const float yhat = pipe.row(3, i);
-      const float t = fmaf(yhat + vi, inv_sigma, s[0]);
+      const float t = fmaf(yhat + vi, inv_sigma, abar);
       if (t + gu > 0.0f) {
-        vni = fmaf(sigma, gu + s[0], vi);
+        vni = fmaf(sigma, gu + abar, vi);
       } else if (t + gl < 0.0f) {
-        vni = fmaf(sigma, gl + s[0], vi);
+        vni = fmaf(sigma, gl + abar, vi);
       } else {
         vni = -yhat;
       }
@@ -281,7 +279,8 @@ __device__ bool round_stop_test(const Ctl* c, const Residuals& r) {
 }
 
 // Rows over the FP32 CSR: A u_c, the primal violation and the row half of the gap; the last
-// block assembles the scaled-problem KKT of xbar + u/dp, ybar + v/dd and decides.
+// block assembles the scaled-problem KKT of xbar + u/dp, ybar + v/dd and decides. A u of the
+// current iterate (candidate 0) replaces the step passes' carried A u.
 __global__ void __launch_bounds__(kWideBlockThreads) k_evalf_rows1(MixedBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kScratch];
@@ -290,12 +289,14 @@ __global__ void __launch_bounds__(kWideBlockThreads) k_evalf_rows1(MixedBuffers 
   const bool avg = c->averaged > 0;
   const float* __restrict__ uc0 = b.uc[0];
   const float* __restrict__ uc1 = b.uc[1];
+  float* __restrict__ au = b.au[c->cur];
   double acc[4] = {0.0, 0.0, 0.0, 0.0};  // pviol0, gapr0, pviol1, gapr1
   auto gather = [&](int col, float a, float* s) {
     s[0] = fmaf(a, uc0[col], s[0]);
     if (avg) s[1] = fmaf(a, uc1[col], s[1]);
   };
   auto epi = [&](int i, const float* s) {
+    au[i] = s[0];
     const double gu = b.gu[i], gl = b.gl[i], yh = b.yhat[i];
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
@@ -369,14 +370,14 @@ __global__ void __launch_bounds__(kWideBlockThreads) k_evalf_rows1(MixedBuffers 
   tick_decisions(c, cur, avg ? &av : nullptr, round_stop_test, t[11], t[6], 1e-10, 1e10);
 }
 
+// The vector half of the decisions; the last block to finish clears the evaluation flags.
 __global__ void k_evalf_apply(MixedBuffers b) {
-  const Ctl* c = b.ctl;
+  Ctl* c = b.ctl;
   if (c->eval_now == 0) return;
   const int copy = c->copy_best;
   const bool restart = c->do_restart != 0;
-  if (copy == 0 && !restart) return;
   const int cur = c->cur;
-  const int total = b.m > b.n ? b.m : b.n;
+  const int total = (copy == 0 && !restart) ? 0 : (b.m > b.n ? b.m : b.n);
   for (int k = grid_stride_begin(); k < total; k += gridDim.x * blockDim.x) {
     if (k < b.n) {
       if (copy) b.u_best[k] = b.uc[copy - 1][k];
@@ -393,6 +394,7 @@ __global__ void k_evalf_apply(MixedBuffers b) {
       }
     }
   }
+  clear_evaluation_flags(c);
 }
 
 // ---- Refinement rounds (FP64) --------------------------------------------------------------

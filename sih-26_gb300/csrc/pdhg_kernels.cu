@@ -58,14 +58,7 @@ __global__ void __launch_bounds__(kBlockThreads) k_primal(StepBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kScratch];
   Ctl* ctl = b.ctl;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    // The evaluation flags of the previous step are consumed; no kernel of this step reads
-    // them before the step decision sets them again.
-    ctl->eval_now = 0;
-    ctl->copy_best = 0;
-    ctl->do_restart = 0;
-  }
-  if (ctl->done != kRunning) return;
+  if (ctl->done != kRunning || ctl->eval_now != 0) return;
   if (ctl->iteration >= ctl->iteration_limit) {  // src/pdhg/pdhg.cpp:206
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->done = kIterationLimit;
     return;
@@ -122,7 +115,7 @@ __global__ void __launch_bounds__(kBlockThreads) k_dual(StepBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kScratch];
   Ctl* ctl = b.ctl;
-  if (ctl->done != kRunning) return;
+  if (ctl->done != kRunning || ctl->eval_now != 0) return;
   const int cur = ctl->cur;
   const double* __restrict__ y = b.y[cur];
   double* __restrict__ yn = b.y[cur ^ 1];
@@ -439,15 +432,15 @@ __global__ void __launch_bounds__(kBlockThreads) k_eval_rows1(EvalBuffers e) {
   tick_decisions(c, cur, avg ? &av : nullptr, fp64_stop_test, t15[13], t15[4], 1e-6, 1e6);
 }
 
-// E4: the vector half of the decisions: best point copy, restart anchors, zeroed sums.
+// E4: the vector half of the decisions: best point copy, restart anchors, zeroed sums. The
+// last block to finish clears the evaluation flags, which lets the next step run.
 __global__ void k_eval_apply(EvalBuffers e) {
-  const Ctl* c = e.ctl;
+  Ctl* c = e.ctl;
   if (c->eval_now == 0 || c->final_mode != 0) return;
   const int copy = c->copy_best;
   const bool restart = c->do_restart != 0;
-  if (copy == 0 && !restart) return;
   const int cur = c->cur;
-  const int total = e.m > e.n ? e.m : e.n;
+  const int total = (copy == 0 && !restart) ? 0 : (e.m > e.n ? e.m : e.n);
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < total; k += gridDim.x * blockDim.x) {
     if (k < e.n) {
       if (copy) e.best_x[k] = e.xu[copy - 1][k];
@@ -464,6 +457,7 @@ __global__ void k_eval_apply(EvalBuffers e) {
       }
     }
   }
+  clear_evaluation_flags(c);
 }
 
 // ---- Setup kernels (src/la/scaling.cpp) ----------------------------------------------------

@@ -84,12 +84,18 @@ __device__ __forceinline__ void block_tile_range(int ntiles, int& first, int& la
   last = static_cast<int>(((b + 1) * T) / G);
 }
 
-// Lanes per row for a pattern with `avg` entries per row, for blocks of `threads` consumer
-// threads: the smallest power of two for which threads / lanes rows of average length fill
-// one buffer (so every thread has entries to sum) and a tile has at most kMaxTileRows rows.
-inline int choose_lanes(double avg, int threads) {
+// Lanes per row for the FP32 layouts (the FP64 layouts use one lane per row, which sums
+// each row in the reference's order): the smallest power of two for which a tile has at
+// most kMaxTileRows rows and threads / lanes rows of average length fill at most two
+// buffers. The tile is then cut at kCap entries with at least half of the threads busy.
+// Asking instead that the rows fill only one buffer (every thread busy) gives tiles half as
+// long, and on the 1M x 2M block-angular LP the column pass (avg 10 entries: 2 lanes against
+// 4) measured 27% slower and the row pass (avg 20: 4 lanes against 8) 14% slower that way:
+// each bulk copy in flight carries less of the matrix. One lane fewer again (2 for the
+// rows) measured slower too.
+inline int wide_lanes(double avg, int threads) {
   int lanes = 1;
-  while (lanes < 32 && ((static_cast<double>(threads) / lanes) * avg > kCap ||
+  while (lanes < 32 && ((static_cast<double>(threads) / lanes) * avg > 2.0 * kCap ||
                         threads / lanes > kMaxTileRows)) {
     lanes *= 2;
   }
