@@ -260,12 +260,12 @@ ADJOINT_FORWARD_TOLERANCE = 1e-4
 
 
 def adjoint_section(device, lps_count=ADJOINT_LPS, shape=ADJOINT_SHAPE, ref_lps=16, fd_lps=2,
-                    fd_coords=4):
+                    fd_coords=64):
     """Forward + polish + adjoint times for the whole batch, and the gradients' agreement with
     (a) the basis solves of the planted optimum (sparse LU on the host, `ref_lps` LPs, every
     coordinate) and (b) central finite differences of L (step 1e-6) through re-solves of the
     perturbed LPs on the device (solve + polish, which land on the exact perturbed vertex), on
-    `fd_coords` cost coordinates of `fd_lps` LPs."""
+    `fd_coords` coordinates of `fd_lps` LPs spread over costs, right-hand sides and bounds."""
     import numpy as np
     from sankhya_gb300 import capi, lpgen
     from sankhya_gb300.model import LP
@@ -327,34 +327,66 @@ def adjoint_section(device, lps_count=ADJOINT_LPS, shape=ADJOINT_SHAPE, ref_lps=
                             float(np.max(np.abs(got - want) / np.maximum(1.0, np.abs(want)))))
         out["max_rel_err_vs_basis_solves"] = worst
         out["basis_reference_lps"] = min(ref_lps, len(lps))
-    # Finite differences: perturbed copies (sharing each LP's matrix) re-solved in one batch.
+    # Finite differences: perturbed copies (sharing each LP's matrix) re-solved in one batch,
+    # 64 coordinates per LP: 16 costs, 16 right-hand sides, 16 lower bounds of columns at
+    # their lower bound and 16 upper bounds of columns at their upper bound (the bounds that
+    # move the optimum). The loss difference is summed from the solutions' differences, so
+    # the two nearly equal losses are never subtracted.
     h = 1e-6
+    per_family = fd_coords // 4
     pert, meta = [], []
     for k in range(min(fd_lps, len(lps))):
         lp = lps[k]
-        for j in rng.choice(n, fd_coords, replace=False):
+        at_l = np.flatnonzero(lp.x0 <= lp.col_lower)
+        at_u = np.flatnonzero(lp.x0 >= lp.col_upper)
+        picks = ([("c", int(j)) for j in rng.choice(n, per_family, replace=False)] +
+                 [("b", int(i)) for i in rng.choice(m, per_family, replace=False)] +
+                 [("l", int(j)) for j in rng.choice(at_l, min(per_family, at_l.size), replace=False)] +
+                 [("u", int(j)) for j in rng.choice(at_u, min(per_family, at_u.size), replace=False)])
+        for fam, j in picks:
             for sign in (1.0, -1.0):
-                c = lp.col_cost.copy()
-                c[j] += sign * h
-                pert.append(LP(m, n, lp.col_starts, lp.row_index, lp.values, c, lp.col_lower,
-                               lp.col_upper, lp.row_lower, lp.row_upper))
-                meta.append((k, int(j), sign))
+                c, lo, up = lp.col_cost.copy(), lp.col_lower.copy(), lp.col_upper.copy()
+                rl, ru = lp.row_lower.copy(), lp.row_upper.copy()
+                if fam == "c":
+                    c[j] += sign * h
+                elif fam == "b":
+                    rl[j] += sign * h
+                    ru[j] += sign * h
+                elif fam == "l":
+                    lo[j] += sign * h
+                else:
+                    up[j] += sign * h
+                pert.append(LP(m, n, lp.col_starts, lp.row_index, lp.values, c, lo, up, rl, ru))
+                meta.append((k, fam, j, sign))
     with capi.BatchEngine(device) as eng:
         eng.load(pert)
         eng.solve(**solve_kw)
-        fitems, _ = eng.polish()
-        losses = []
-        for q, (k, j, sign) in enumerate(meta):
-            x, _, y = eng.solution(q)
-            losses.append(gx[k] @ x + gy[k] @ y + fitems[q].objective)
-    fd_worst = 0.0
+        fitems, finfo = eng.polish()
+        sols = [eng.solution(q) for q in range(len(meta))]
+    fd_worst, fam_worst, fd_count = 0.0, {}, 0
     for q in range(0, len(meta), 2):
-        k, j, _ = meta[q]
-        fd = (losses[q] - losses[q + 1]) / (2 * h)
-        fd_worst = max(fd_worst, abs(res[k]["dc"][j] - fd) / max(1.0, abs(fd)))
+        k, fam, j, _ = meta[q]
+        lp = lps[k]
+        (xp, _, yp), (xm, _, ym) = sols[q], sols[q + 1]
+        dx, dy = xp - xm, yp - ym
+        dl = (gx[k] + lp.col_cost) @ dx + gy[k] @ dy
+        if fam == "c":
+            dl += h * (xp[j] + xm[j])
+        fd = dl / (2 * h)
+        r = res[k]
+        got = {"c": r["dc"][j], "b": r["drl"][j] + r["dru"][j], "l": r["dl"][j],
+               "u": r["du"][j]}[fam]
+        err = abs(got - fd) / max(1.0, abs(fd))
+        fd_worst = max(fd_worst, err)
+        fam_worst[fam] = max(fam_worst.get(fam, 0.0), err)
+        fd_count += 1
     out["fd_max_rel_err"] = fd_worst
-    out["fd_sample"] = (f"{min(fd_lps, len(lps))} LPs x {fd_coords} cost coordinates, central "
-                        f"differences with step {h}, perturbed LPs re-solved and polished")
+    out["fd_max_rel_err_by_family"] = fam_worst
+    out["fd_polished"] = sum(1 for p in finfo if p["status"] == 0)
+    out["fd_sample"] = (f"{min(fd_lps, len(lps))} LPs x {fd_count // max(1, min(fd_lps, len(lps)))} "
+                        f"coordinates (costs, right-hand sides, active lower and upper bounds), "
+                        f"central differences with step {h}; the {len(meta)} perturbed LPs "
+                        f"re-solved and polished in one batch")
     return out
 
 

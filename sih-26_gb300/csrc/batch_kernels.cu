@@ -1485,31 +1485,63 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_polish(BatchBuffers b, 
     }
     b_jacobi(v, w);
     // Right-hand sides: rm[4] = b_R - A_RN x_N over the rows; cn[2] = c_B over the columns.
-    for (int i = t; i < v.m; i += T) {
-      const signed char st = w.rs[i];
-      double r = 0.0;
-      if (st != 0) {
-        r = st == 1 ? v.rl[i] : v.ru[i];
-        for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
-          const signed char cj = w.cs[v.ri[k]];
-          if (cj != 0) r -= v.rraw[k] * (cj == 1 ? v.l[v.ri[k]] : v.u[v.ri[k]]);
+    const auto row_rhs = [&]() {
+      for (int i = t; i < v.m; i += T) {
+        const signed char st = w.rs[i];
+        double r = 0.0;
+        if (st != 0) {
+          r = st == 1 ? v.rl[i] : v.ru[i];
+          for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
+            const signed char cj = w.cs[v.ri[k]];
+            if (cj != 0) r -= v.rraw[k] * (cj == 1 ? v.l[v.ri[k]] : v.u[v.ri[k]]);
+          }
         }
+        w.rm[4][i] = r;
       }
-      w.rm[4][i] = r;
-    }
-    for (int j = t; j < v.n; j += T) w.cn[2][j] = w.cs[j] == 0 ? v.cost[j] : 0.0;
+    };
+    const auto col_rhs = [&]() {
+      for (int j = t; j < v.n; j += T) w.cn[2][j] = w.cs[j] == 0 ? v.cost[j] : 0.0;
+    };
+    row_rhs();
+    col_rhs();
     __syncthreads();
-    int it1 = 0, it2 = 0;
-    double res1 = 0.0, res2 = 0.0;
+    int it1 = 0, it2 = 0, itr = 0;
+    double res1 = 0.0, res2 = 0.0, resr = 0.0;
     // x_B = M' z, (M M') z = rhs. The right-hand side doubles as the operator's output
     // buffer: b_pcg reads it only before the first product.
     b_pcg<true>(v, w, w.rm[4], w.rm[0], w.rm[1], w.rm[2], w.rm[3], w.rm[4], w.rm[5], w.cn[1],
                 scratch, a.max_iterations, a.cg_tolerance, &it1, &res1);
     masked_at(v, w, w.rm[0], v.xu[1]);  // x_B (0 off B)
+    // One pass of iterative refinement: the residual of M x_B = rhs, formed in FP64 against
+    // the rebuilt right-hand side, solved the same way and added. The normal equations square
+    // the basis's condition number, so the first solve alone leaves x_B with an error of
+    // about cond(M)^2 times the CG tolerance; the pass takes that down to the rounding of the
+    // residual itself.
+    row_rhs();
+    masked_a(v, w, v.xu[1], w.rm[1]);
+    for (int i = t; i < v.m; i += T) w.rm[4][i] -= w.rm[1][i];
+    __syncthreads();
+    b_pcg<true>(v, w, w.rm[4], w.rm[0], w.rm[1], w.rm[2], w.rm[3], w.rm[4], w.rm[5], w.cn[1],
+                scratch, a.max_iterations, a.cg_tolerance, &itr, &resr);
+    masked_at(v, w, w.rm[0], w.cn[1]);
+    for (int j = t; j < v.n; j += T) v.xu[1][j] += w.cn[1][j];
+    __syncthreads();
+    it1 += itr;
     // y_R = M z', (M' M) z' = c_B.
     b_pcg<false>(v, w, w.cn[2], w.cn[1], w.cn[3], w.cn[4], w.cn[5], w.cn[2], w.cn[0], w.rm[1],
                  scratch, a.max_iterations, a.cg_tolerance, &it2, &res2);
     masked_a(v, w, w.cn[1], w.rm[2]);  // the reported multipliers y_R (0 off R)
+    // The same refinement pass for y_R against c_B.
+    col_rhs();
+    masked_at(v, w, w.rm[2], w.cn[3]);
+    for (int j = t; j < v.n; j += T) w.cn[2][j] -= w.cn[3][j];
+    __syncthreads();
+    b_pcg<false>(v, w, w.cn[2], w.cn[1], w.cn[3], w.cn[4], w.cn[5], w.cn[2], w.cn[0], w.rm[1],
+                 scratch, a.max_iterations, a.cg_tolerance, &itr, &resr);
+    masked_a(v, w, w.cn[1], w.rm[1]);
+    for (int i = t; i < v.m; i += T) w.rm[2][i] += w.rm[1][i];
+    __syncthreads();
+    it2 += itr;
     // The polished point into xu[1] (columns) and yu[1] (the solver's sign: -y), then checks.
     double bad[1] = {0.0};
     double cmax[1] = {0.0};
