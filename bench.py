@@ -280,6 +280,7 @@ def adjoint_section(device, lps_count=ADJOINT_LPS, shape=ADJOINT_SHAPE, ref_lps=
     with capi.BatchEngine(device) as eng:
         eng.load(lps)
         items, fwd_s = eng.solve(**solve_kw)
+        fwd_iterations = sum(it.iterations for it in items) / len(items)
         t0 = time.perf_counter()
         items, polish_info = eng.polish()
         polish_s = time.perf_counter() - t0
@@ -293,7 +294,7 @@ def adjoint_section(device, lps_count=ADJOINT_LPS, shape=ADJOINT_SHAPE, ref_lps=
                              float(np.abs(y - lps[k].lam).max()))
     out = {"lps": len(lps), "shape": [m, n], "forward_tolerance": ADJOINT_FORWARD_TOLERANCE,
            "forward_device_s": fwd_s, "polish_s": polish_s,
-           "forward_iterations_mean": sum(it.iterations for it in items) / len(items),
+           "forward_iterations_mean": fwd_iterations,
            "adjoint_s": adj_s, "statuses": {}, "adjoint_status": {}, "cg_iterations_max": 0,
            "polished": sum(1 for p in polish_info if p["status"] == 0),
            "vertex_max_abs_err": vertex_err}
