@@ -1,0 +1,199 @@
+// layout_check.cu -- host-only checks of the tile and window layouts the kernels rely on.
+//
+// Built by tests/test_host_layout.py against the engine's objects and run on the CPU (no
+// CUDA call is made). For random and banded sparsity patterns, every lane count and both
+// block sizes, it checks that:
+//   * the tiles cover the lines in order, short tiles within min(kMaxTileRows, threads /
+//     lanes) rows and kCap entries, rows longer than kCap as consecutive chunk tiles;
+//   * every bulk copy a tile issues (entries widened to 4-element bounds, row pointers, the
+//     rows' operand slices) fits its shared-memory buffer and stays inside the padded arrays;
+//   * every window starts and ends on a 4-element bound, holds at most wmax elements, lies
+//     inside the padded gathered vector, and the staged count build_windows returns is the
+//     number of entries that fall inside their tile's window;
+// plus the FP32 lane rule and the step graph's launch count.
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+#include <vector>
+
+#include "engine.hpp"
+#include "kernels.cuh"
+#include "tiles.cuh"
+
+using namespace sgb;
+
+namespace {
+
+int g_failures = 0;
+
+void fail(const char* what, long long a, long long b) {
+  if (g_failures < 20) std::printf("FAIL: %s (%lld, %lld)\n", what, a, b);
+  ++g_failures;
+}
+
+struct Pattern {
+  int lines = 0;
+  int extent = 0;
+  std::vector<int> ptr;
+  std::vector<int> idx;
+};
+
+// Row lengths: mostly short, some empty, a few around and far beyond kCap.
+Pattern make_pattern(unsigned seed, int lines, int extent, bool banded) {
+  std::mt19937 rng(seed);
+  Pattern p;
+  p.lines = lines;
+  p.extent = extent;
+  p.ptr.push_back(0);
+  for (int r = 0; r < lines; ++r) {
+    int len;
+    const unsigned kind = rng() % 1000;
+    if (kind < 20) {
+      len = 0;
+    } else if (kind < 23) {
+      const int specials[] = {kCap, kCap + 1, 3 * kCap + 17};
+      len = specials[rng() % 3];
+    } else {
+      len = 1 + static_cast<int>(rng() % 40);
+    }
+    for (int k = 0; k < len; ++k) {
+      int c;
+      if (banded) {
+        const long long centre = static_cast<long long>(r) * extent / lines;
+        const int spread = 600;
+        c = static_cast<int>((centre + static_cast<int>(rng() % (2 * spread)) - spread +
+                              extent) % extent);
+        if (rng() % 10 == 0) c = static_cast<int>(rng() % extent);  // a far link
+      } else {
+        c = static_cast<int>(rng() % extent);
+      }
+      p.idx.push_back(c);
+    }
+    p.ptr.push_back(static_cast<int>(p.idx.size()));
+  }
+  return p;
+}
+
+void check_tiles(const Pattern& p, int lanes, int threads, const std::vector<Tile>& tiles,
+                 const std::vector<LongRow>& longs, int nchunks) {
+  const int max_rows = std::min(kMaxTileRows, threads / lanes);
+  const long long nnz = p.ptr[p.lines];
+  int row = 0;
+  int chunk = 0;
+  size_t li = 0;
+  for (size_t t = 0; t < tiles.size(); ++t) {
+    const Tile& tile = tiles[t];
+    if (tile.k1 - tile.k0 > kCap) fail("tile entries > kCap", tile.k0, tile.k1);
+    if (tile.k0 < 0 || tile.k1 > nnz || tile.k0 > tile.k1) fail("tile entry range", tile.k0, tile.k1);
+    // The entry copy: widened to 4-element bounds, within the buffer and the padded arrays.
+    const int a0 = tile.k0 & ~3, a1 = (tile.k1 + 3) & ~3;
+    if (a1 - a0 > kCap + kSlack) fail("entry copy exceeds the buffer", a0, a1);
+    if (a1 > nnz + kPad) fail("entry copy beyond the padded arrays", a1, nnz);
+    if (tile.r1 < 0) {
+      // A chunk tile of the long row `row`.
+      if (li >= longs.size() || longs[li].row != tile.r0) fail("chunk tile without its long row", tile.r0, static_cast<long long>(li));
+      if (-tile.r1 - 1 != chunk) fail("chunk slot order", -tile.r1 - 1, chunk);
+      if (tile.r0 != row) fail("chunk tile row", tile.r0, row);
+      const bool last = tile.k1 == p.ptr[row + 1];
+      ++chunk;
+      if (last) {
+        if (li < longs.size() && longs[li].chunk0 + longs[li].nchunks != chunk) {
+          fail("long row chunk count", longs[li].nchunks, chunk);
+        }
+        ++li;
+        ++row;
+      }
+      continue;
+    }
+    if (tile.r0 != row) fail("tiles out of order", tile.r0, row);
+    if (tile.r1 <= tile.r0) fail("empty tile", tile.r0, tile.r1);
+    if (tile.r1 - tile.r0 > max_rows) fail("tile rows > limit", tile.r1 - tile.r0, max_rows);
+    if (tile.k0 != p.ptr[tile.r0] || tile.k1 != p.ptr[tile.r1]) fail("tile entries do not match its rows", tile.k0, tile.k1);
+    for (int r = tile.r0; r < tile.r1; ++r) {
+      if (p.ptr[r + 1] - p.ptr[r] > kCap) fail("long row inside a short tile", r, p.ptr[r + 1] - p.ptr[r]);
+    }
+    // Row pointer and row operand copies.
+    const int w0 = tile.r0 & ~3;
+    const int bp = ((tile.r1 + 1 + 3) & ~3) - w0;
+    const int br = ((tile.r1 + 3) & ~3) - w0;
+    if (bp > kRowStride) fail("row pointer copy exceeds the buffer", bp, kRowStride);
+    if (br > kRowStride) fail("row operand copy exceeds the buffer", br, kRowStride);
+    if (w0 + bp > p.lines + 1 + kPad) fail("row pointer copy beyond the padded array", w0 + bp, p.lines);
+    if (w0 + br > p.lines + kPad) fail("row operand copy beyond the padded vectors", w0 + br, p.lines);
+    row = tile.r1;
+  }
+  if (row != p.lines) fail("tiles do not cover every line", row, p.lines);
+  if (chunk != nchunks) fail("chunk count", chunk, nchunks);
+  if (li != longs.size()) fail("long rows", static_cast<long long>(li), static_cast<long long>(longs.size()));
+}
+
+void check_windows(const Pattern& p, const std::vector<Tile>& tiles, int wmax) {
+  std::vector<int> tile_win;
+  std::vector<int2> windows;
+  const long long covered = build_windows(tiles, p.idx.data(), p.extent, wmax, &tile_win, &windows);
+  if (tile_win.size() != tiles.size()) fail("one window id per tile", static_cast<long long>(tile_win.size()), static_cast<long long>(tiles.size()));
+  const int ext4 = (p.extent + 3) & ~3;
+  for (const int2& w : windows) {
+    if (w.x % 4 != 0 || w.y % 4 != 0) fail("window not on 4-element bounds", w.x, w.y);
+    if (w.y <= 0 || w.y > wmax) fail("window length", w.y, wmax);
+    if (w.x < 0 || w.x + w.y > ext4) fail("window beyond the padded vector", w.x, w.y);
+  }
+  long long count = 0;
+  for (size_t t = 0; t < tiles.size(); ++t) {
+    const int id = tile_win[t];
+    if (id < -1 || id >= static_cast<int>(windows.size())) {
+      fail("window id", id, static_cast<long long>(windows.size()));
+      continue;
+    }
+    if (id < 0) continue;
+    const int2 w = windows[static_cast<size_t>(id)];
+    for (int k = tiles[t].k0; k < tiles[t].k1; ++k) {
+      if (p.idx[static_cast<size_t>(k)] >= w.x && p.idx[static_cast<size_t>(k)] < w.x + w.y) ++count;
+    }
+  }
+  if (wmax <= 0 && !windows.empty()) fail("windows without capacity", static_cast<long long>(windows.size()), wmax);
+  if (count != covered) fail("staged count", covered, count);
+}
+
+}  // namespace
+
+int main() {
+  // The FP32 lane rule: two lanes per 10-entry column, four per 20-entry row, and never more
+  // rows per tile than a tile can stage.
+  if (wide_lanes(10.0, kWideThreads) != 2) fail("wide_lanes(10)", wide_lanes(10.0, kWideThreads), 2);
+  if (wide_lanes(20.0, kWideThreads) != 4) fail("wide_lanes(20)", wide_lanes(20.0, kWideThreads), 4);
+  for (double avg = 0.5; avg < 5000.0; avg *= 1.37) {
+    const int lanes = wide_lanes(avg, kWideThreads);
+    if (lanes < 1 || lanes > 32 || (lanes & (lanes - 1)) != 0) fail("wide_lanes power of two", lanes, 0);
+    if (kWideThreads / lanes > kMaxTileRows) fail("wide_lanes rows", kWideThreads / lanes, kMaxTileRows);
+  }
+  // Step graphs: two kernels per step, four evaluation kernels after every kEvalStride steps
+  // and after the last.
+  if (graph_kernel_launches(1) != 6) fail("graph launches (1)", graph_kernel_launches(1), 6);
+  if (graph_kernel_launches(kEvalStride) != 2 * kEvalStride + 4) fail("graph launches (stride)", graph_kernel_launches(kEvalStride), 2 * kEvalStride + 4);
+  if (graph_kernel_launches(32) != 64 + 4 * ((32 + kEvalStride - 1) / kEvalStride)) fail("graph launches (32)", graph_kernel_launches(32), 0);
+
+  int layouts = 0;
+  for (unsigned seed = 1; seed <= 3; ++seed) {
+    for (int banded = 0; banded < 2; ++banded) {
+      const Pattern p = make_pattern(seed * 7919u + banded, 4000 + 37 * static_cast<int>(seed), 30001 + static_cast<int>(seed), banded != 0);
+      for (int threads : {kTileThreads, kWideThreads}) {
+        for (int lanes = 1; lanes <= 32; lanes *= 2) {
+          std::vector<Tile> tiles;
+          std::vector<LongRow> longs;
+          int nchunks = 0;
+          build_tiles(p.ptr, p.lines, lanes, threads, &tiles, &longs, &nchunks);
+          check_tiles(p, lanes, threads, tiles, longs, nchunks);
+          for (int wmax : {0, 1024, 8192, 40000}) check_windows(p, tiles, wmax);
+          ++layouts;
+        }
+      }
+    }
+  }
+  if (g_failures != 0) {
+    std::printf("%d failures\n", g_failures);
+    return 1;
+  }
+  std::printf("OK %d layouts\n", layouts);
+  return 0;
+}
