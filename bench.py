@@ -408,10 +408,15 @@ def cpu_reference(lp, iterations_sample, threads):
     """The reference algorithm on this host: the oracle (C restatement, OpenMP A^T y like the
     reference) -- setup alone, then setup + a few iterations; seconds to 1e-8 are
     setup + per-iteration x the FP64 iteration count."""
+    import ctypes
     import pyoracle
 
     pyoracle.build()
     os.environ["OMP_NUM_THREADS"] = str(threads)
+    try:  # the oracle's OpenMP runtime is shared with this process once loaded
+        ctypes.CDLL("libgomp.so.1").omp_set_num_threads(int(threads))
+    except OSError:
+        pass
     o = pyoracle.Oracle()
     t0 = time.perf_counter()
     o.solve(lp, tolerance=TOLERANCE, iteration_limit=0)
@@ -560,11 +565,15 @@ def main():
     if not args.no_cpu_baseline:
         setup, per_it, sample_s = cpu_reference(lp, args.cpu_iterations, threads)
         its = FP64_ITERATIONS_TO_1E8
+        setup1, per_it1, sample1 = cpu_reference(lp, max(2, args.cpu_iterations // 4), 1)
         cpu = {"value": setup + per_it * its, "unit": "s", "cores": threads, "kind": "port",
                "sample": f"oracle setup + {args.cpu_iterations} FP64 iterations on {threads} "
                          f"threads ({sample_s:.1f} s of CPU work), extrapolated to {its} "
                          f"iterations",
-               "setup_s": setup, "s_per_iteration": per_it}
+               "setup_s": setup, "s_per_iteration": per_it,
+               "single_thread": {"value": setup1 + per_it1 * its, "unit": "s", "cores": 1,
+                                 "setup_s": setup1, "s_per_iteration": per_it1,
+                                 "sample_s": sample1}}
 
     dominant = "k_dual" if roof["k_dual_ms"] >= roof["k_primal_ms"] else "k_primal"
     kname = {"k_dual": "row pass (A xbar, A dx, dual update)",
