@@ -42,12 +42,10 @@ SolveStatus to_status(int code) {
 }
 
 // An option row the registry may not carry in an older build: the default is used then.
+// Options' typed getters abort on a name the registry does not know (they treat it as a bug,
+// include/sankhya/options.hpp:82-86), so the row is looked up first.
 std::string string_option(const Options& options, const char* name, const char* fallback) {
-  try {
-    return options.get_string(name);
-  } catch (...) {
-    return fallback;
-  }
+  return Options::exists(name) ? options.get_string(name) : std::string(fallback);
 }
 
 struct Hooks {

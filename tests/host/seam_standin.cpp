@@ -1,0 +1,141 @@
+// seam_standin.cpp -- a CPU stand-in for the engine's C ABI, for the seam's behaviour test.
+//
+// Implements the five calls seam/pdhg_gpu.cpp makes (create, load, solve, solution,
+// last_error) by handing the LP to the REFERENCE's own CPU PDHG (sankhya::pdhg::solve_pdhg,
+// compiled from the reference's sources) with the options rebuilt from the params struct the
+// seam filled in. The seam is then checked against a direct call of the same reference
+// function: every option row it forwards, every field it fills and every status it maps must
+// come out the same. It also drives the seam's hooks: one iteration-table row through
+// params.log, the interrupt through params.poll, and a failing create on request
+// (standin_fail_create). Test infrastructure only; nothing here is part of the engine.
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <string>
+
+#include "sankhya/logging.hpp"
+#include "sankhya/model.hpp"
+#include "sankhya/options.hpp"
+#include "sankhya/pdhg.hpp"
+#include "sankhya_gb300.h"
+
+struct sankhya_gb300_pdhg {
+  sankhya::Model model;
+  sankhya::Solution solution;
+  bool solved = false;
+};
+
+namespace {
+
+thread_local std::string g_error;
+int g_fail_create = 0;
+
+int32_t to_code(sankhya::SolveStatus s) {
+  using S = sankhya::SolveStatus;
+  switch (s) {
+    case S::kOptimal: return SANKHYA_GB300_OPTIMAL;
+    case S::kFeasible: return SANKHYA_GB300_FEASIBLE;
+    case S::kInfeasible: return SANKHYA_GB300_INFEASIBLE;
+    case S::kIterationLimit: return SANKHYA_GB300_ITERATION_LIMIT;
+    case S::kTimeLimit: return SANKHYA_GB300_TIME_LIMIT;
+    case S::kInterrupted: return SANKHYA_GB300_INTERRUPTED;
+    case S::kModelError: return SANKHYA_GB300_MODEL_ERROR;
+    default: return SANKHYA_GB300_NUMERICAL_ERROR;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void standin_fail_create(int fail) { g_fail_create = fail; }
+
+const char* sankhya_gb300_last_error(void) { return g_error.c_str(); }
+
+int sankhya_gb300_pdhg_create(int32_t device, sankhya_gb300_pdhg** out) {
+  (void)device;
+  if (g_fail_create) {
+    g_error = "no usable CUDA device (stand-in)";
+    return SANKHYA_GB300_ERROR_DEVICE;
+  }
+  *out = new sankhya_gb300_pdhg();
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_pdhg_load(sankhya_gb300_pdhg* e, const sankhya_gb300_lp* lp) {
+  sankhya::Model& m = e->model;
+  m = sankhya::Model();
+  const auto n = static_cast<std::size_t>(lp->cols);
+  const auto rows = static_cast<std::size_t>(lp->rows);
+  m.sense = lp->sense < 0.0 ? sankhya::ObjSense::kMaximize : sankhya::ObjSense::kMinimize;
+  m.objective_offset = lp->objective_offset;
+  m.col_cost.assign(lp->col_cost, lp->col_cost + n);
+  m.col_lower.assign(lp->col_lower, lp->col_lower + n);
+  m.col_upper.assign(lp->col_upper, lp->col_upper + n);
+  m.col_type.assign(n, sankhya::VarType::kContinuous);
+  m.row_lower.assign(lp->row_lower, lp->row_lower + rows);
+  m.row_upper.assign(lp->row_upper, lp->row_upper + rows);
+  m.matrix.reset(lp->rows, lp->cols);
+  for (int32_t j = 0; j < lp->cols; ++j) {
+    for (int32_t k = lp->col_starts[j]; k < lp->col_starts[j + 1]; ++k) {
+      m.matrix.add_entry(lp->row_index[k], j, lp->values[k]);
+    }
+  }
+  m.matrix.finalize(0.0);
+  e->solved = false;
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_pdhg_solve(sankhya_gb300_pdhg* e, const sankhya_gb300_params* p,
+                             sankhya_gb300_result* r) {
+  std::memset(r, 0, sizeof(*r));
+  if (p->poll != nullptr && p->poll(p->poll_user, 0, 0.0) != 0) {
+    e->solution = sankhya::Solution();
+    e->solution.allocate_for(e->model);
+    e->solved = true;
+    r->status = SANKHYA_GB300_INTERRUPTED;
+    std::strncpy(r->message, "interrupted (stand-in)", sizeof(r->message) - 1);
+    return SANKHYA_GB300_OK;
+  }
+  if (p->precision != SANKHYA_GB300_FP64 || p->stop_rule != SANKHYA_GB300_STOP_STANDARD) {
+    g_error = "the stand-in runs the reference method only";
+    return SANKHYA_GB300_ERROR_OPTION;
+  }
+  sankhya::Options o;
+  o.set_double("pdhg_tolerance", p->tolerance);
+  o.set_int("iteration_limit", p->iteration_limit);
+  o.set_double("time_limit", p->time_limit);
+  o.set_bool("pdhg_restart", p->restart != 0);
+  o.set_bool("pdhg_stop_at_request", p->stop_at_request != 0);
+  o.set_int("random_seed", p->random_seed);
+  sankhya::Logger quiet(nullptr);
+  e->solution = sankhya::pdhg::solve_pdhg(e->model, o, quiet, nullptr);
+  e->solved = true;
+  if (p->log != nullptr) p->log(p->log_user, 40, e->solution.objective, 1e-3, 2e-3, 0.25);
+  r->status = to_code(e->solution.status);
+  r->iterations = e->solution.iterations;
+  r->objective = e->solution.objective;
+  r->dual_bound = e->solution.dual_bound;
+  r->solve_seconds = e->solution.solve_seconds;
+  std::strncpy(r->message, e->solution.message.c_str(), sizeof(r->message) - 1);
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_pdhg_solution(sankhya_gb300_pdhg* e, double* col_value, double* col_dual,
+                                double* row_dual) {
+  if (!e->solved) {
+    g_error = "no solve has run";
+    return SANKHYA_GB300_ERROR_ARGUMENT;
+  }
+  const auto& s = e->solution;
+  for (std::size_t j = 0; j < s.col_value.size(); ++j) {
+    if (col_value) col_value[j] = s.col_value[j];
+    if (col_dual) col_dual[j] = s.col_dual[j];
+  }
+  for (std::size_t i = 0; i < s.row_dual.size(); ++i) {
+    if (row_dual) row_dual[i] = s.row_dual[i];
+  }
+  return SANKHYA_GB300_OK;
+}
+
+}  // extern "C"
