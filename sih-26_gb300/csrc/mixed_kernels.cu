@@ -7,8 +7,9 @@
 // measured markedly faster on GB300 than an 8-byte (ubar, du) gather) and forms
 // A ubar = A u + 2 A du with A u carried per row (MixedBuffers::au). A du comes straight
 // from the gather, so the interaction term of the step-size rule keeps FP32's relative
-// accuracy however small the step is; forming it as a difference of two large products
-// instead measured about 16% more iterations.
+// accuracy however small the step is, rather than being the difference of two large
+// products. (On the 1M x 2M block-angular LP both forms took the same number of iterations
+// to relative KKT 1e-8.)
 #include "common.cuh"
 #include "decisions.cuh"
 #include "kernels.cuh"
