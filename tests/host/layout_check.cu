@@ -10,7 +10,8 @@
 //   * every window starts and ends on a 4-element bound, holds at most wmax elements, lies
 //     inside the padded gathered vector, and the staged count build_windows returns is the
 //     number of entries that fall inside their tile's window;
-// plus the FP32 lane rule and the step graph's launch count.
+// plus the FP32 lane rule and the step graph's launch count. Given a file, it checks the
+// layouts the engine builds for that pattern instead (read_pattern).
 #include <cstdio>
 #include <cstdlib>
 #include <random>
@@ -155,9 +156,59 @@ void check_windows(const Pattern& p, const std::vector<Tile>& tiles, int wmax) {
   if (count != covered) fail("staged count", covered, count);
 }
 
+// A pattern from a file: int32 lines, int32 extent, int32 ptr[lines + 1], int32 idx[nnz].
+bool read_pattern(const char* path, Pattern* p) {
+  std::FILE* f = std::fopen(path, "rb");
+  if (f == nullptr) return false;
+  int head[2];
+  bool ok = std::fread(head, sizeof(int), 2, f) == 2 && head[0] >= 0 && head[1] > 0;
+  if (ok) {
+    p->lines = head[0];
+    p->extent = head[1];
+    p->ptr.resize(static_cast<size_t>(p->lines) + 1);
+    ok = std::fread(p->ptr.data(), sizeof(int), p->ptr.size(), f) == p->ptr.size() &&
+         p->ptr[0] == 0 && p->ptr[static_cast<size_t>(p->lines)] >= 0;
+  }
+  if (ok) {
+    p->idx.resize(static_cast<size_t>(p->ptr[static_cast<size_t>(p->lines)]));
+    ok = std::fread(p->idx.data(), sizeof(int), p->idx.size(), f) == p->idx.size();
+  }
+  std::fclose(f);
+  return ok;
+}
+
+// The layouts the engine builds for a real pattern: lanes 1 with the FP64 block size and
+// the FP32 lane rule with the FP32 block size, at the window capacities of both.
+int check_file(const char* path) {
+  Pattern p;
+  if (!read_pattern(path, &p)) {
+    std::printf("FAIL: cannot read %s\n", path);
+    return 1;
+  }
+  const double avg = p.lines > 0 ? static_cast<double>(p.ptr[static_cast<size_t>(p.lines)]) / p.lines : 1.0;
+  const int layouts[2][2] = {{1, kTileThreads}, {wide_lanes(avg, kWideThreads), kWideThreads}};
+  long long chunks = 0;
+  for (const auto& l : layouts) {
+    std::vector<Tile> tiles;
+    std::vector<LongRow> longs;
+    int nchunks = 0;
+    build_tiles(p.ptr, p.lines, l[0], l[1], &tiles, &longs, &nchunks);
+    check_tiles(p, l[0], l[1], tiles, longs, nchunks);
+    for (int wmax : {0, 16384, 40960}) check_windows(p, tiles, wmax);
+    chunks += nchunks;
+  }
+  if (g_failures != 0) {
+    std::printf("%d failures\n", g_failures);
+    return 1;
+  }
+  std::printf("OK %d lines, %d nonzeros, %lld chunk tiles\n", p.lines, p.ptr[static_cast<size_t>(p.lines)], chunks);
+  return 0;
+}
+
 }  // namespace
 
-int main() {
+int main(int argc, char** argv) {
+  if (argc > 1) return check_file(argv[1]);
   // The FP32 lane rule: two lanes per 10-entry column, four per 20-entry row, and never more
   // rows per tile than a tile can stage.
   if (wide_lanes(10.0, kWideThreads) != 2) fail("wide_lanes(10)", wide_lanes(10.0, kWideThreads), 2);
