@@ -152,22 +152,35 @@ def make_workload(blocks=None):
                                 WORKLOAD["cols_per_block"], WORKLOAD["k"], WORKLOAD["seed"])
 
 
-def profile_case(blocks, precision, iterations):
+def profile_case(blocks, precision, iterations, zipf=False):
     """The small case the kernel captures run on: the same generator with fewer periods
     (16 periods: 250,000 x 500,000, about 5M nonzeros, matrix copies of 40-120 MB), solved for
-    a fixed number of accepted iterations. Prints one line and returns."""
-    from sankhya_gb300 import build, capi
+    a fixed number of accepted iterations. With `zipf`, the load-balance stress LP instead:
+    500,000 x 1,000,000, Zipf(1.5) row lengths, about 3e7 nonzeros, values of log-uniform
+    magnitude over [1e-3, 1e3]. Prints one line (with the step kernels' CUDA-event times
+    after the solve) and returns."""
+    from sankhya_gb300 import build, capi, lpgen
 
     build.build_lpgen()
     build.build_engine()
-    lp = make_workload(blocks)
+    lp = (lpgen.planted_zipf(500000, 1000000, 30000000, seed=3) if zipf
+          else make_workload(blocks))
     eng = capi.PdhgEngine(0)
     eng.load(lp)
     r = eng.solve(tolerance=TOLERANCE, stop_rule="relative", precision=precision,
                   iteration_limit=iterations, steps_per_poll=8)
+    ms_primal, ms_dual = eng.time_kernels(20)
+    v = 8 if precision == "fp64" else 4
+    b_col, b_row = algorithmic_bytes(lp.rows, lp.cols, lp.nnz, v, v)
     print(json.dumps({"profile_case": f"{lp.rows} x {lp.cols}, {lp.nnz} nnz",
                       "precision": precision, "status": r.status_name,
-                      "iterations": r.iterations, "staged_share": list(r.staged_fraction)}))
+                      "iterations": r.iterations, "staged_share": list(r.staged_fraction),
+                      "us_per_attempt": 1e6 * r.loop_seconds / max(1, r.attempts),
+                      "column_pass_us": 1e3 * ms_primal, "row_pass_us": 1e3 * ms_dual,
+                      "column_pass_gbs": b_col / (ms_primal * 1e-3) / 1e9,
+                      "row_pass_gbs": b_row / (ms_dual * 1e-3) / 1e9,
+                      "relative_kkt": max(r.residuals["primal"], r.residuals["dual"],
+                                          r.residuals["gap"])}))
     eng.close()
 
 
@@ -458,9 +471,12 @@ def main():
     ap.add_argument("--profile-case", type=int, metavar="PERIODS", default=0,
                     help="run only the small kernel-capture case with this many periods")
     ap.add_argument("--profile-iterations", type=int, default=40)
+    ap.add_argument("--profile-zipf", action="store_true",
+                    help="profile case on the 500,000 x 1,000,000 Zipf-row LP")
     args = ap.parse_args()
-    if args.profile_case:
-        profile_case(args.profile_case, args.precision, args.profile_iterations)
+    if args.profile_case or args.profile_zipf:
+        profile_case(args.profile_case, args.precision, args.profile_iterations,
+                     zipf=args.profile_zipf)
         return
     rank, world, local, dist = dist_setup()
     threads = os.cpu_count() or 1
