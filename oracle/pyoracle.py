@@ -224,3 +224,60 @@ class Oracle:
         out = np.zeros(count)
         self.lib.orc_power_start(seed, count, _ptr(out, ctypes.c_double))
         return out
+
+    # Reference-only helpers: Models built by the reference's own code.
+    def _model_from_handle(self, handle, name):
+        from sankhya_gb300.model import LP
+
+        lib = self.lib
+        rows, cols = ctypes.c_int32(), ctypes.c_int32()
+        nnz, optimum = ctypes.c_int64(), ctypes.c_int64()
+        sense, offset = ctypes.c_double(), ctypes.c_double()
+        lib.ref_model_shape(handle, ctypes.byref(rows), ctypes.byref(cols), ctypes.byref(nnz),
+                            ctypes.byref(sense), ctypes.byref(offset), ctypes.byref(optimum))
+        m, n, z = rows.value, cols.value, nnz.value
+        starts = np.zeros(n + 1, np.int32)
+        index = np.zeros(z, np.int32)
+        arrays = [np.zeros(k) for k in (z, n, n, n, m, m)]
+        lib.ref_model_arrays(handle, _ptr(starts, ctypes.c_int32), _ptr(index, ctypes.c_int32),
+                             *[_ptr(a, ctypes.c_double) for a in arrays])
+        lib.ref_model_free(handle)
+        values, cost, lower, upper, row_lower, row_upper = arrays
+        lp = LP(m, n, starts, index, values, cost, lower, upper, row_lower, row_upper,
+                sense=sense.value, objective_offset=offset.value, name=name)
+        return lp, optimum.value
+
+    def _model_api(self):
+        if not self.reference:
+            raise RuntimeError("only the reference library reads and generates Models")
+        lib = self.lib
+        lib.ref_model_read.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_int32]
+        lib.ref_model_read.restype = ctypes.c_void_p
+        lib.ref_model_kkt_lp.argtypes = [ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32,
+                                         ctypes.c_int32]
+        lib.ref_model_kkt_lp.restype = ctypes.c_void_p
+        lib.ref_model_shape.argtypes = [ctypes.c_void_p] + [ctypes.c_void_p] * 6
+        lib.ref_model_shape.restype = None
+        lib.ref_model_arrays.argtypes = [ctypes.c_void_p, _I, _I] + [_D] * 6
+        lib.ref_model_arrays.restype = None
+        lib.ref_model_free.argtypes = [ctypes.c_void_p]
+        lib.ref_model_free.restype = None
+        return lib
+
+    def read_model(self, path):
+        """The LP in an MPS or LP file, as the reference's reader builds it
+        (sankhya::io::read_model, src/io/lp_reader.cpp:650)."""
+        lib = self._model_api()
+        err = ctypes.create_string_buffer(1024)
+        handle = lib.ref_model_read(os.fsencode(path), err, 1024)
+        if not handle:
+            raise ValueError(f"{path}: {err.value.decode(errors='replace')}")
+        return self._model_from_handle(handle, os.path.basename(path))[0]
+
+    def kkt_lp(self, seed, trial, max_rows=8, max_cols=8):
+        """(LP, exact optimal objective): the trial-th instance of the reference's generator
+        of LPs with a known optimum (sankhya::oracle::kkt_lp, tests/oracles/lp_generator.cpp:122)
+        drawn from one mt19937_64(seed)."""
+        lib = self._model_api()
+        handle = lib.ref_model_kkt_lp(seed, trial, max_rows, max_cols)
+        return self._model_from_handle(handle, f"kkt_lp_{seed}_{trial}")

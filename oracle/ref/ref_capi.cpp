@@ -5,15 +5,25 @@
 // into oracle/_ref/libsankhya_ref.so. The functions mirror pdhg_oracle.h one for one so that a
 // test can run the restatement and the reference on identical inputs and compare the bits.
 // Nothing here is linked into the GPU engine.
+//
+// Two more groups hand Models that the reference's own code builds to the tests: one read by
+// its MPS/LP reader (sankhya::io::read_model, src/io/lp_reader.cpp:650), one made by its test
+// generator of LPs with an exact, analytically known optimum (sankhya::oracle::kkt_lp,
+// tests/oracles/lp_generator.cpp:122, turned into a Model by
+// tests/oracles/rational_simplex.cpp:252).
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <random>
 #include <string>
 #include <vector>
 
 #include "la/scaling.hpp"
+#include "oracles/lp_generator.hpp"
+#include "oracles/rational_simplex.hpp"
 #include "pdhg/pdhg_evaluate.hpp"
+#include "sankhya/io.hpp"
 #include "sankhya/logging.hpp"
 #include "sankhya/model.hpp"
 #include "sankhya/options.hpp"
@@ -176,5 +186,76 @@ orc_residuals ref_evaluate(const orc_lp* lp, const double* x, const double* y, d
   if (reduced != nullptr) std::memcpy(reduced, red.data(), n * sizeof(double));
   return to_c(r);
 }
+
+// ---- Models built by the reference's own code ------------------------------------------
+
+struct ref_model {
+  sankhya::Model model;
+  int64_t optimal_objective = 0;
+};
+
+// Reads an MPS or LP file with the reference's reader. Returns NULL (and the reader's message
+// in `error`) when the file does not parse or the Model does not validate.
+void* ref_model_read(const char* path, char* error, int32_t error_capacity) {
+  auto* h = new ref_model;
+  const sankhya::io::ReadResult r = sankhya::io::read_model(path, &h->model);
+  std::string message = r.ok ? h->model.validate() : r.error;
+  if (!r.ok || !message.empty()) {
+    if (error != nullptr && error_capacity > 0) {
+      std::snprintf(error, static_cast<std::size_t>(error_capacity), "%s", message.c_str());
+    }
+    delete h;
+    return nullptr;
+  }
+  return h;
+}
+
+// The `trial`-th instance (counting from 0) that kkt_lp draws from one mt19937_64 seeded with
+// `seed`, with the generator's default configuration except the row and column maxima, as
+// the reference's PDHG-against-simplex test draws them (tests/unit/test_pdhg.cpp:181-190).
+void* ref_model_kkt_lp(uint64_t seed, int32_t trial, int32_t max_rows, int32_t max_cols) {
+  std::mt19937_64 rng(seed);
+  sankhya::oracle::GeneratorConfig config;
+  config.max_rows = max_rows;
+  config.max_cols = max_cols;
+  sankhya::oracle::KktInstance instance;
+  for (int32_t t = 0; t <= trial; ++t) instance = sankhya::oracle::kkt_lp(rng, config);
+  auto* h = new ref_model;
+  h->model = sankhya::oracle::to_model(instance.lp);
+  h->optimal_objective = instance.optimal_objective;
+  return h;
+}
+
+void ref_model_shape(const void* handle, int32_t* rows, int32_t* cols, int64_t* nonzeros,
+                     double* sense, double* objective_offset, int64_t* optimal_objective) {
+  const auto* h = static_cast<const ref_model*>(handle);
+  *rows = h->model.num_rows();
+  *cols = h->model.num_cols();
+  *nonzeros = h->model.matrix.num_nonzeros();
+  *sense = h->model.sense == sankhya::ObjSense::kMaximize ? -1.0 : 1.0;
+  *objective_offset = h->model.objective_offset;
+  *optimal_objective = h->optimal_objective;
+}
+
+// Copies the Model into caller arrays sized by ref_model_shape (CSC, ascending rows).
+void ref_model_arrays(const void* handle, int32_t* col_starts, int32_t* row_index,
+                      double* values, double* col_cost, double* col_lower, double* col_upper,
+                      double* row_lower, double* row_upper) {
+  const auto* h = static_cast<const ref_model*>(handle);
+  const sankhya::Model& m = h->model;
+  const auto& starts = m.matrix.column_starts();
+  const auto& index = m.matrix.row_indices();
+  const auto& vals = m.matrix.values();
+  for (std::size_t k = 0; k < starts.size(); ++k) col_starts[k] = static_cast<int32_t>(starts[k]);
+  for (std::size_t k = 0; k < index.size(); ++k) row_index[k] = static_cast<int32_t>(index[k]);
+  std::memcpy(values, vals.data(), vals.size() * sizeof(double));
+  std::memcpy(col_cost, m.col_cost.data(), m.col_cost.size() * sizeof(double));
+  std::memcpy(col_lower, m.col_lower.data(), m.col_lower.size() * sizeof(double));
+  std::memcpy(col_upper, m.col_upper.data(), m.col_upper.size() * sizeof(double));
+  std::memcpy(row_lower, m.row_lower.data(), m.row_lower.size() * sizeof(double));
+  std::memcpy(row_upper, m.row_upper.data(), m.row_upper.size() * sizeof(double));
+}
+
+void ref_model_free(void* handle) { delete static_cast<ref_model*>(handle); }
 
 }  // extern "C"
