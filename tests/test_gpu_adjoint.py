@@ -9,7 +9,7 @@
 
 The forward solves stop at relative KKT 1e-7 and are then polished at their active sets
 (sankhya_gb300_batch_polish), which must land on the planted vertex. Bar: 1e-5 relative (the
-the benchmark spec's), measured against max(1, |gradient|).
+adjoint's accuracy target), measured against max(1, |gradient|).
 """
 import numpy as np
 import pytest

@@ -7,7 +7,7 @@ Bars (see each test):
 * sparse products on short rows: bit-identical to SparseMatrix::multiply /
   transpose_multiply (same summation order); on long rows, within 1e-13 relative;
 * solves: the same status, the objective within 1e-6 relative of the oracle's (the
-  spec bar; the achieved difference is printed), the reported point's relative KKT
+  engine's parity bar; the achieved difference is printed), the reported point's relative KKT
   (re-evaluated by the oracle's own evaluate) within the requested tolerance.
 """
 import numpy as np
@@ -18,7 +18,7 @@ from sankhya_gb300.model import LP, from_dense
 
 pytestmark = pytest.mark.gpu
 INF = np.inf
-OBJ_TOL = 1e-6  # relative objective agreement with the oracle (spec bar)
+OBJ_TOL = 1e-6  # relative objective agreement with the oracle (the engine's parity bar)
 
 
 def rel(a, b):
