@@ -7,8 +7,15 @@
 // function: every option row it forwards, every field it fills and every status it maps must
 // come out the same. It also drives the seam's hooks: one iteration-table row through
 // params.log, the interrupt through params.poll, and a failing create on request
-// (standin_fail_create). Test infrastructure only; nothing here is part of the engine.
+// (standin_fail_create).
+//
+// For the front-end test it also answers the device probes and the memory estimate that
+// seam/device.cpp and seam/gpu_memory.cpp forward to the C ABI, with a device the test sets
+// (standin_set_device), and counts the solves it ran (standin_solve_count), so a test can
+// tell whether SANKHYA's solve() reached the seam or took its own CPU path. Test
+// infrastructure only; nothing here is part of the engine.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -29,6 +36,18 @@ namespace {
 
 thread_local std::string g_error;
 int g_fail_create = 0;
+long long g_solves = 0;
+
+// The device the probes describe: a GB300 with 280 GiB free, unless a test says otherwise.
+struct Device {
+  int available = 1;
+  int major = 10;
+  int minor = 3;
+  unsigned long long free_bytes = 280ULL << 30;
+  unsigned long long total_bytes = 284ULL << 30;
+  unsigned long long estimate = 64ULL << 20;
+};
+Device g_device;
 
 int32_t to_code(sankhya::SolveStatus s) {
   using S = sankhya::SolveStatus;
@@ -49,6 +68,44 @@ int32_t to_code(sankhya::SolveStatus s) {
 extern "C" {
 
 void standin_fail_create(int fail) { g_fail_create = fail; }
+
+void standin_set_device(int available, int major, int minor, unsigned long long free_bytes,
+                        unsigned long long total_bytes, unsigned long long estimate) {
+  g_device = Device{available, major, minor, free_bytes, total_bytes, estimate};
+}
+
+long long standin_solve_count(void) { return g_solves; }
+
+int sankhya_gb300_device_available(char* description, int32_t capacity) {
+  if (description != nullptr && capacity > 0) {
+    std::snprintf(description, static_cast<std::size_t>(capacity), "%s",
+                  g_device.available ? "NVIDIA GB300 (stand-in)" : "no device (stand-in)");
+  }
+  return g_device.available ? SANKHYA_GB300_OK : SANKHYA_GB300_ERROR_DEVICE;
+}
+
+int sankhya_gb300_device_free_memory(size_t* free_bytes, size_t* total_bytes) {
+  if (!g_device.available) return SANKHYA_GB300_ERROR_DEVICE;
+  if (free_bytes != nullptr) *free_bytes = static_cast<size_t>(g_device.free_bytes);
+  if (total_bytes != nullptr) *total_bytes = static_cast<size_t>(g_device.total_bytes);
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_device_compute_capability(int32_t* major, int32_t* minor) {
+  if (!g_device.available) return SANKHYA_GB300_ERROR_DEVICE;
+  if (major != nullptr) *major = g_device.major;
+  if (minor != nullptr) *minor = g_device.minor;
+  return SANKHYA_GB300_OK;
+}
+
+size_t sankhya_gb300_estimate_memory(int32_t rows, int32_t cols, int64_t nonzeros,
+                                     int32_t precision) {
+  (void)rows;
+  (void)cols;
+  (void)nonzeros;
+  (void)precision;
+  return static_cast<size_t>(g_device.estimate);
+}
 
 const char* sankhya_gb300_last_error(void) { return g_error.c_str(); }
 
@@ -111,6 +168,7 @@ int sankhya_gb300_pdhg_solve(sankhya_gb300_pdhg* e, const sankhya_gb300_params* 
   sankhya::Logger quiet(nullptr);
   e->solution = sankhya::pdhg::solve_pdhg(e->model, o, quiet, nullptr);
   e->solved = true;
+  ++g_solves;
   if (p->log != nullptr) p->log(p->log_user, 40, e->solution.objective, 1e-3, 2e-3, 0.25);
   r->status = to_code(e->solution.status);
   r->iterations = e->solution.iterations;

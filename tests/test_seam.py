@@ -1,10 +1,14 @@
 """The drop-in C++ seam (sih-26_gb300/seam/) inside SANKHYA's tree: each file is checked
 against the reference's own headers (src/gpu/*.hpp, include/sankhya/*.hpp), which is how a
-maintainer builds it in place of src/gpu/*.cu, and the seam's behaviour is checked against
-the reference's own solve_pdhg (see the last test). Needs the reference tree and g++."""
+maintainer builds it in place of src/gpu/*.cu; the seam's behaviour is checked against the
+reference's own solve_pdhg; and the reference's front ends (solve(), its engine gates, the C
+API, the Python bindings) are checked to reach the engine through the seam. Needs the
+reference tree and g++; the engine's C ABI is a CPU stand-in (tests/host/seam_standin.cpp)."""
 import os
 import shutil
 import subprocess
+import sys
+import textwrap
 
 import pytest
 
@@ -58,3 +62,81 @@ def test_seam_solves_like_the_reference(tmp_path):
     run = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert run.returncode == 0, run.stdout[-2000:] + run.stderr[-2000:]
     assert run.stdout.strip().endswith("OK"), run.stdout
+
+
+def _core_link_args():
+    """Compiler arguments for the reference's whole core (oracle/_ref/libsankhya_core.a, built
+    by `make -C oracle ref-core` as a CUDA build compiles it), the four seam files in place of
+    src/gpu, the C-ABI stand-in and the checkpoint stub."""
+    if not os.path.isdir(os.path.join(REF, "src", "gpu")) or shutil.which("g++") is None:
+        pytest.skip("the reference tree (or g++) is not present here")
+    import torch
+
+    subprocess.run(["make", "-s", f"-j{os.cpu_count() or 4}", "-C",
+                    os.path.join(ROOT, "oracle"), "ref-core", f"REF={REF}"], check=True)
+    torch_inc = os.path.join(os.path.dirname(torch.__file__), "include")
+    flags = ["-std=c++20", "-O1", "-fPIC", "-DFMT_HEADER_ONLY", "-DSANKHYA_ENABLE_CUDA",
+             "-DSANKHYA_MIN_COMPUTE_ARCH=103", f"-I{REF}/include", f"-I{REF}/src",
+             f"-I{ROOT}/include", f"-I{ROOT}/oracle/ref/standin", "-isystem", torch_inc]
+    sources = [os.path.join(SEAM, f + ".cpp")
+               for f in ("pdhg_gpu", "pdhg_multi_gpu", "gpu_memory", "device")]
+    sources += [os.path.join(ROOT, "tests", "host", f)
+                for f in ("seam_standin.cpp", "checkpoint_stub.cpp")]
+    core = os.path.join(ROOT, "oracle", "_ref", "libsankhya_core.a")
+    return flags, sources, core
+
+
+def test_front_ends_reach_the_engine_through_the_seam(tmp_path):
+    """`tests/host/frontend_check.cpp` on afiro: SANKHYA's solve() with gpu=true (plain, with
+    the interior-point polish, and with two device ids), its gates (deterministic, compute
+    capability, free memory), algorithm=auto at 100,000 rows, and the C API all reach the
+    engine through the seam and give the CPU route's answer bit for bit; an engine that
+    cannot be created is an error status, not a CPU fallback."""
+    flags, sources, core = _core_link_args()
+    exe = str(tmp_path / "frontend_check")
+    cmd = (["g++"] + flags + sources + [os.path.join(ROOT, "tests", "host", "frontend_check.cpp"),
+                                        core, "-fopenmp", "-lz", "-o", exe])
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr[-2000:]
+    model = os.path.join(REF, "data", "netlib", "afiro.mps")
+    run = subprocess.run([exe, model], capture_output=True, text=True, timeout=600)
+    assert run.returncode == 0, run.stdout[-2000:] + run.stderr[-2000:]
+    assert run.stdout.strip().endswith("OK"), run.stdout
+
+
+def test_python_bindings_reach_the_engine_through_the_seam(tmp_path):
+    """The reference's own Python package (bindings/python/sankhya) loads a libsankhya.so
+    built from its core with the seam in place of src/gpu: Options(gpu=True,
+    algorithm="pdhg") reaches the engine once and returns what Options(gpu=False) returns."""
+    flags, sources, core = _core_link_args()
+    lib = str(tmp_path / "libsankhya.so")
+    cmd = (["g++", "-shared"] + flags + sources +
+           ["-Wl,--whole-archive", core, "-Wl,--no-whole-archive", "-Wl,--no-undefined",
+            "-fopenmp", "-lz", "-o", lib])
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr[-2000:]
+    script = textwrap.dedent(f"""
+        import ctypes, sys
+        sys.path.insert(0, {os.path.join(REF, "bindings", "python")!r})
+        import sankhya
+        model = sankhya.Model.read({os.path.join(REF, "data", "netlib", "afiro.mps")!r})
+        count = ctypes.CDLL({lib!r}).standin_solve_count
+        count.restype = ctypes.c_longlong
+        kw = dict(algorithm="pdhg", pdhg_polish=False, log_to_console=False)
+        before = count()
+        gpu = model.solve(sankhya.Options(gpu=True, **kw))
+        reached = count() - before
+        cpu = model.solve(sankhya.Options(gpu=False, **kw))
+        assert reached == 1 and count() - before == 1, ("seam calls", reached, count() - before)
+        assert gpu.status == cpu.status == "optimal", (gpu.status, cpu.status)
+        assert gpu.iterations == cpu.iterations, (gpu.iterations, cpu.iterations)
+        assert gpu.objective == cpu.objective, (gpu.objective, cpu.objective)
+        assert gpu.x == cpu.x and gpu.row_duals == cpu.row_duals
+        assert gpu.reduced_costs == cpu.reduced_costs
+        print("OK", gpu.objective, gpu.iterations)
+        """)
+    env = dict(os.environ, SANKHYA_LIBRARY=lib)
+    run = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True,
+                         timeout=600, env=env)
+    assert run.returncode == 0, run.stdout[-2000:] + run.stderr[-2000:]
+    assert run.stdout.startswith("OK"), run.stdout
