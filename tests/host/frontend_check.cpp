@@ -17,6 +17,11 @@
 //  5. algorithm=auto routes a model of 100,000 rows to the GPU when the device answers;
 //  6. the C API (sankhya_solve with the gpu option set) reaches the seam;
 //  7. the version banner names the device the seam reports.
+//
+// `frontend_check --write model.mps out.sol` instead solves the model once through solve()
+// with algorithm=pdhg, gpu=true (tolerance 1e-8, no polish) and writes the answer with the
+// reference's own writer (io::write_solution), for the reference's independent verifier
+// (tools/verify_solution.py). It fails if the solve did not go through the seam.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -103,9 +108,34 @@ sankhya::Model chain_model() {
 
 }  // namespace
 
+// Solve through the seam and write the reference's .sol file.
+int write_mode(const char* model_path, const char* sol_path) {
+  sankhya::Model model;
+  const sankhya::io::ReadResult read = sankhya::io::read_model(model_path, &model);
+  if (!read.ok) {
+    std::printf("cannot read %s: %s\n", model_path, read.error.c_str());
+    return 2;
+  }
+  sankhya::Options o = pdhg_options(true, false);
+  o.set_double("pdhg_tolerance", 1e-8);
+  o.set_int("iteration_limit", 1000000);
+  const Route route;
+  const sankhya::Solution s = sankhya::solve(model, o);
+  std::string error;
+  if (!sankhya::io::write_solution(sol_path, model, s, o, &error)) {
+    std::printf("cannot write %s: %s\n", sol_path, error.c_str());
+    return 2;
+  }
+  std::printf("%s: %s, %lld iterations, objective %.17g, algorithm %s\n", model_path,
+              sankhya::to_string(s.status), static_cast<long long>(s.iterations),
+              s.objective, s.algorithm.c_str());
+  return route.moved_by(1) ? 0 : 1;
+}
+
 int main(int argc, char** argv) {
+  if (argc == 4 && std::strcmp(argv[1], "--write") == 0) return write_mode(argv[2], argv[3]);
   if (argc < 2) {
-    std::printf("usage: frontend_check model.mps\n");
+    std::printf("usage: frontend_check model.mps | frontend_check --write model.mps out.sol\n");
     return 2;
   }
   sankhya::Model model;
