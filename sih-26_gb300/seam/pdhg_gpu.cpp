@@ -79,10 +79,15 @@ int poll(void* user, long long iteration, double objective) {
 }
 
 // One engine per process, created on first use (device memory is reused across solves).
+// SANKHYA's solve() may be called from several threads at once, and an engine holds one LP,
+// so a caller keeps `use` locked from its load until it has read its solution back: solves
+// from different threads run one after another on the one GPU. The lock is held while the
+// engine calls the caller's log and poll hooks, so a progress callback must not itself call
+// solve() with the GPU path on.
+std::mutex use;
+
 sankhya_gb300_pdhg* shared_engine(std::string* error) {
-  static std::mutex lock;
   static sankhya_gb300_pdhg* engine = nullptr;
-  std::lock_guard<std::mutex> guard(lock);
   if (engine == nullptr && sankhya_gb300_pdhg_create(0, &engine) != SANKHYA_GB300_OK) {
     *error = sankhya_gb300_last_error();
     engine = nullptr;
@@ -104,6 +109,7 @@ Solution solve_pdhg_gpu(const Model& model, const Options& options, Logger& logg
     return solution;
   }
   std::string error;
+  std::unique_lock<std::mutex> held(use);
   sankhya_gb300_pdhg* engine = shared_engine(&error);
   if (engine == nullptr) {
     solution.status = SolveStatus::kNumericalError;
@@ -160,6 +166,7 @@ Solution solve_pdhg_gpu(const Model& model, const Options& options, Logger& logg
     solution.message = std::string("GB300 PDHG: ") + sankhya_gb300_last_error();
     return solution;
   }
+  held.unlock();
   solution.status = to_status(result.status);
   solution.message = result.message;
   solution.iterations = result.iterations;

@@ -8,13 +8,16 @@
 // fields recompute_quality() fills, with algorithm "pdhg-gpu". Then the seam's other paths:
 // a Model that fails validation (kModelError before any engine call), an engine that cannot
 // be created (kNumericalError with the engine's message, no fallback), an interrupt through
-// SolveControl (kInterrupted), and the iteration table written through the Logger.
+// SolveControl (kInterrupted), and the iteration table written through the Logger. Last,
+// four threads solve different Models through the seam at the same time, as callers of
+// SANKHYA's solve() may: each must get its own Model's answer, bit for bit.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <limits>
 #include <random>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "gpu/pdhg_gpu.hpp"
@@ -168,6 +171,38 @@ int main() {
   std::fclose(log);
   check(l.status == sankhya::SolveStatus::kOptimal || l.status == sankhya::SolveStatus::kFeasible,
         "logged solve status");
+
+  // Concurrent callers: every thread's answers must be its own Model's.
+  {
+    constexpr int kThreads = 4, kRounds = 3;
+    std::vector<sankhya::Model> models;
+    std::vector<sankhya::Solution> wants;
+    for (int k = 0; k < kThreads; ++k) {
+      models.push_back(make_model(30 + k, k % 2 == 1));
+      wants.push_back(sankhya::pdhg::solve_pdhg(models.back(), options, quiet, nullptr));
+    }
+    std::vector<int> wrong(kThreads, 0);
+    std::vector<std::thread> threads;
+    for (int k = 0; k < kThreads; ++k) {
+      threads.emplace_back([&, k] {
+        sankhya::Logger own(nullptr);
+        for (int r = 0; r < kRounds; ++r) {
+          const sankhya::Solution got =
+              sankhya::gpu::solve_pdhg_gpu(models[k], options, own, nullptr);
+          const sankhya::Solution& want = wants[k];
+          if (got.status != want.status || got.iterations != want.iterations ||
+              !same(got.col_value, want.col_value) || !same(got.row_dual, want.row_dual) ||
+              !same(got.objective, want.objective)) {
+            ++wrong[k];
+          }
+        }
+      });
+    }
+    for (auto& t : threads) t.join();
+    for (int k = 0; k < kThreads; ++k) {
+      check(wrong[k] == 0, "concurrent callers get their own answers");
+    }
+  }
 
   if (g_failures != 0) {
     std::printf("%d failures\n", g_failures);

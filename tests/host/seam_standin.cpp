@@ -14,6 +14,7 @@
 // (standin_set_device), and counts the solves it ran (standin_solve_count), so a test can
 // tell whether SANKHYA's solve() reached the seam or took its own CPU path. Test
 // infrastructure only; nothing here is part of the engine.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -36,7 +37,7 @@ namespace {
 
 thread_local std::string g_error;
 int g_fail_create = 0;
-long long g_solves = 0;
+std::atomic<long long> g_solves{0};
 
 // The device the probes describe: a GB300 with 280 GiB free, unless a test says otherwise.
 struct Device {
@@ -74,7 +75,7 @@ void standin_set_device(int available, int major, int minor, unsigned long long 
   g_device = Device{available, major, minor, free_bytes, total_bytes, estimate};
 }
 
-long long standin_solve_count(void) { return g_solves; }
+long long standin_solve_count(void) { return g_solves.load(); }
 
 int sankhya_gb300_device_available(char* description, int32_t capacity) {
   if (description != nullptr && capacity > 0) {
