@@ -14,6 +14,11 @@
  * across this boundary. All pointers are HOST pointers; the engine copies what it needs to
  * the device and owns every device allocation. There is no CPU fallback: with no usable
  * GPU the calls fail with SANKHYA_GB300_ERROR_DEVICE.
+ *
+ * Threads: an engine handle holds one LP (or one batch) and its device state, so calls on
+ * one handle must not overlap; a caller that shares a handle between threads serialises
+ * them, as the seam does for its one engine. Different handles are independent, except that
+ * the kernel-launch count the results report is kept per process.
  */
 #ifndef SANKHYA_GB300_H
 #define SANKHYA_GB300_H
