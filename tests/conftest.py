@@ -52,3 +52,54 @@ def engine(built):
     eng = capi.PdhgEngine(0)
     yield eng
     eng.close()
+
+
+def _reference_tree():
+    import pyoracle
+
+    return pyoracle.REFERENCE_TREE
+
+
+def core_link_args():
+    """Compiler arguments for the reference's whole core (oracle/_ref/libsankhya_core.a, built
+    by `make -C oracle ref-core` as a CUDA build compiles it), the four seam files in place of
+    src/gpu, the C-ABI stand-in (tests/host/seam_standin.cpp) and the checkpoint stub. Skips
+    the calling test where the reference tree or g++ is absent."""
+    import shutil
+    import subprocess
+
+    ref = _reference_tree()
+    if not os.path.isdir(os.path.join(ref, "src", "gpu")) or shutil.which("g++") is None:
+        pytest.skip("the reference tree (or g++) is not present here")
+    import torch
+
+    subprocess.run(["make", "-s", f"-j{os.cpu_count() or 4}", "-C",
+                    os.path.join(ROOT, "oracle"), "ref-core", f"REF={ref}"], check=True)
+    torch_inc = os.path.join(os.path.dirname(torch.__file__), "include")
+    flags = ["-std=c++20", "-O1", "-fPIC", "-DFMT_HEADER_ONLY", "-DSANKHYA_ENABLE_CUDA",
+             "-DSANKHYA_MIN_COMPUTE_ARCH=103", f"-I{ref}/include", f"-I{ref}/src",
+             f"-I{ROOT}/include", f"-I{ROOT}/oracle/ref/standin", "-isystem", torch_inc]
+    seam = os.path.join(ROOT, "sih-26_gb300", "seam")
+    sources = [os.path.join(seam, f + ".cpp")
+               for f in ("pdhg_gpu", "pdhg_multi_gpu", "gpu_memory", "device")]
+    sources += [os.path.join(ROOT, "tests", "host", f)
+                for f in ("seam_standin.cpp", "checkpoint_stub.cpp")]
+    core = os.path.join(ROOT, "oracle", "_ref", "libsankhya_core.a")
+    return flags, sources, core
+
+
+@pytest.fixture(scope="session")
+def reference_core_library(tmp_path_factory):
+    """libsankhya.so built from the reference's core with the seam in place of src/gpu and
+    the CPU stand-in behind the engine's C ABI: what the reference's own Python package
+    (bindings/python/sankhya) loads through SANKHYA_LIBRARY."""
+    import subprocess
+
+    flags, sources, core = core_link_args()
+    lib = str(tmp_path_factory.mktemp("reference_core") / "libsankhya.so")
+    cmd = (["g++", "-shared"] + flags + sources +
+           ["-Wl,--whole-archive", core, "-Wl,--no-whole-archive", "-Wl,--no-undefined",
+            "-fopenmp", "-lz", "-o", lib])
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr[-2000:]
+    return lib

@@ -13,6 +13,7 @@ import textwrap
 import pytest
 
 import pyoracle
+from conftest import core_link_args
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 SEAM = os.path.join(ROOT, "sih-26_gb300", "seam")
@@ -64,32 +65,10 @@ def test_seam_solves_like_the_reference(tmp_path):
     assert run.stdout.strip().endswith("OK"), run.stdout
 
 
-def _core_link_args():
-    """Compiler arguments for the reference's whole core (oracle/_ref/libsankhya_core.a, built
-    by `make -C oracle ref-core` as a CUDA build compiles it), the four seam files in place of
-    src/gpu, the C-ABI stand-in and the checkpoint stub."""
-    if not os.path.isdir(os.path.join(REF, "src", "gpu")) or shutil.which("g++") is None:
-        pytest.skip("the reference tree (or g++) is not present here")
-    import torch
-
-    subprocess.run(["make", "-s", f"-j{os.cpu_count() or 4}", "-C",
-                    os.path.join(ROOT, "oracle"), "ref-core", f"REF={REF}"], check=True)
-    torch_inc = os.path.join(os.path.dirname(torch.__file__), "include")
-    flags = ["-std=c++20", "-O1", "-fPIC", "-DFMT_HEADER_ONLY", "-DSANKHYA_ENABLE_CUDA",
-             "-DSANKHYA_MIN_COMPUTE_ARCH=103", f"-I{REF}/include", f"-I{REF}/src",
-             f"-I{ROOT}/include", f"-I{ROOT}/oracle/ref/standin", "-isystem", torch_inc]
-    sources = [os.path.join(SEAM, f + ".cpp")
-               for f in ("pdhg_gpu", "pdhg_multi_gpu", "gpu_memory", "device")]
-    sources += [os.path.join(ROOT, "tests", "host", f)
-                for f in ("seam_standin.cpp", "checkpoint_stub.cpp")]
-    core = os.path.join(ROOT, "oracle", "_ref", "libsankhya_core.a")
-    return flags, sources, core
-
-
 @pytest.fixture(scope="module")
 def frontend_exe(tmp_path_factory):
     """tests/host/frontend_check.cpp linked with the reference's core and the seam."""
-    flags, sources, core = _core_link_args()
+    flags, sources, core = core_link_args()
     exe = str(tmp_path_factory.mktemp("frontend") / "frontend_check")
     cmd = (["g++"] + flags + sources + [os.path.join(ROOT, "tests", "host", "frontend_check.cpp"),
                                         core, "-fopenmp", "-lz", "-o", exe])
@@ -143,17 +122,11 @@ def test_answers_through_the_seam_pass_the_reference_verifier(frontend_exe, tmp_
     assert "VERIFIED" in check.stdout, check.stdout[-2000:]
 
 
-def test_python_bindings_reach_the_engine_through_the_seam(tmp_path):
+def test_python_bindings_reach_the_engine_through_the_seam(reference_core_library):
     """The reference's own Python package (bindings/python/sankhya) loads a libsankhya.so
     built from its core with the seam in place of src/gpu: Options(gpu=True,
     algorithm="pdhg") reaches the engine once and returns what Options(gpu=False) returns."""
-    flags, sources, core = _core_link_args()
-    lib = str(tmp_path / "libsankhya.so")
-    cmd = (["g++", "-shared"] + flags + sources +
-           ["-Wl,--whole-archive", core, "-Wl,--no-whole-archive", "-Wl,--no-undefined",
-            "-fopenmp", "-lz", "-o", lib])
-    proc = subprocess.run(cmd, capture_output=True, text=True)
-    assert proc.returncode == 0, proc.stderr[-2000:]
+    lib = reference_core_library
     script = textwrap.dedent(f"""
         import ctypes, sys
         sys.path.insert(0, {os.path.join(REF, "bindings", "python")!r})
