@@ -4,6 +4,14 @@ import sys
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+# The checker libraries (the oracle and the reference) run A^T y in an OpenMP parallel region
+# every iteration. On the tests' small LPs a team wider than the free cores waits at every
+# barrier for a descheduled thread, and a solve of 1e6 iterations then takes tens of minutes
+# on a busy machine. Their results do not depend on the team size (each column's sum is
+# serial), so the tests run them on one thread unless the caller says otherwise. The bench's
+# CPU legs set their own thread counts.
+os.environ.setdefault("OMP_NUM_THREADS", "1")
 for sub in ("sih-26_gb300", "oracle"):
     p = os.path.join(ROOT, sub)
     if p not in sys.path:
