@@ -177,7 +177,13 @@ SGB_API int sankhya_gb300_pdhg_destroy(sankhya_gb300_pdhg* engine);
 
 /* Copy an LP to the device: CSC and a CSR copy, unscaled values kept for the evaluation.
  * Fails with SANKHYA_GB300_ERROR_MODEL on the numeric defects Model::validate rejects
- * (src/core/model.cpp:127-240). */
+ * (src/core/model.cpp:127-240): a matrix value that is not finite, a NaN bound, a crossed
+ * bound, a NaN cost, a NaN objective offset; and on a CSC structure that is not well formed
+ * (column starts not from 0 or not monotone, a row index out of range, row indices not
+ * strictly ascending in a column). It also refuses an INFINITE cost, which Model::validate
+ * lets through: on such an LP the reference PDHG returns a NaN objective at its iteration
+ * limit, or never ends when the column can move towards the infinite cost. Negative sizes
+ * or null column starts fail with SANKHYA_GB300_ERROR_ARGUMENT. */
 SGB_API int sankhya_gb300_pdhg_load(sankhya_gb300_pdhg* engine, const sankhya_gb300_lp* lp);
 
 /* Solve the loaded LP: device preconditioning (src/la/scaling.cpp:111-194) and the restarted

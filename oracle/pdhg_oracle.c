@@ -387,22 +387,24 @@ orc_residuals orc_evaluate(const orc_lp* lp, const double* x, const double* y, d
   return r;
 }
 
-/* Model::validate's numeric checks (src/core/model.cpp:127-240): every matrix value and
- * cost finite, no NaN bound, no crossed bound. */
+/* Model::validate's numeric checks (src/core/model.cpp:127-240): every matrix value finite
+ * (:178), no NaN bound and no crossed bound (:210-224), no NaN cost (:214) and no NaN
+ * objective offset (:228). An infinite cost passes, as it does there. */
 static int model_is_valid(const orc_lp* lp) {
   const int32_t nnz = lp->col_starts[lp->cols];
   for (int32_t k = 0; k < nnz; ++k) {
     if (!isfinite(lp->values[k])) return 0;
   }
   for (int32_t j = 0; j < lp->cols; ++j) {
-    if (!isfinite(lp->col_cost[j])) return 0;
     if (isnan(lp->col_lower[j]) || isnan(lp->col_upper[j])) return 0;
     if (lp->col_lower[j] > lp->col_upper[j]) return 0;
+    if (isnan(lp->col_cost[j])) return 0;
   }
   for (int32_t i = 0; i < lp->rows; ++i) {
     if (isnan(lp->row_lower[i]) || isnan(lp->row_upper[i])) return 0;
     if (lp->row_lower[i] > lp->row_upper[i]) return 0;
   }
+  if (isnan(lp->objective_offset)) return 0;
   return 1;
 }
 

@@ -471,6 +471,9 @@ void validate_lp(const sankhya_gb300_lp& lp) {
       throw EngineError{SANKHYA_GB300_ERROR_MODEL, format("row %d has a bad bound", i)};
     }
   }
+  if (std::isnan(lp.objective_offset)) {
+    throw EngineError{SANKHYA_GB300_ERROR_MODEL, "objective offset is NaN"};
+  }
   if (nnz > std::numeric_limits<int>::max()) {
     throw EngineError{SANKHYA_GB300_ERROR_MODEL, "more nonzeros than int32 indices address"};
   }

@@ -79,3 +79,28 @@ def test_zipf_layouts(checker, tmp_path):
     out = _run([checker, rows])
     assert "chunk tiles" in out and not out.split(",")[-1].strip().startswith("0 ")
     _run([checker, cols])
+
+
+def test_model_checks_follow_the_reference(tmp_path):
+    """`tests/host/validate_check.cu`: the engine's model checks (validate_lp, run by both
+    load entry points) accept a valid LP with infinite bounds, empty lines and explicit zeros,
+    and refuse, with the model-error code, every numeric defect the reference's
+    Model::validate refuses (src/core/model.cpp:127-240), the CSC defects a frozen matrix
+    cannot hold, and an infinite cost (the engine's own rule)."""
+    nvcc = os.environ.get("NVCC") or shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc is not available")
+    sys.path.insert(0, os.path.join(ROOT, "sih-26_gb300"))
+    from sankhya_gb300 import _paths, build
+
+    build.build_engine()
+    objdir = os.path.join(os.path.dirname(_paths.ENGINE_LIB), "obj")
+    objs = [os.path.join(objdir, s.replace(".cu", ".o")) for s in build.CUDA_SOURCES]
+    exe = str(tmp_path / "validate_check")
+    cmd = ([nvcc] + build.ARCH +
+           ["-O2", "-std=c++17", "--expt-relaxed-constexpr", "-I", _paths.INCLUDE_DIR, "-I",
+            _paths.CSRC_DIR, os.path.join(ROOT, "tests", "host", "validate_check.cu")] + objs +
+           ["-lcudart", "-o", exe])
+    proc = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    assert proc.returncode == 0, proc.stdout
+    _run([exe])

@@ -64,3 +64,23 @@ def test_evaluate_is_bit_identical(reference, oracle):
     rb, ab, db = reference.evaluate(lp, x, y)
     assert ra == rb
     assert np.array_equal(aa, ab) and np.array_equal(da, db)
+
+
+def test_inputs_at_the_edge_of_validation(reference, oracle):
+    """Model::validate (src/core/model.cpp:214,228) refuses a NaN objective offset and lets an
+    infinite cost through. A NaN offset is a model error on both. With +inf on a column
+    bounded below, the projection holds the column at its bound: both run to the iteration
+    limit with a NaN objective, bit for bit alike. (With the cost pushing a column towards an
+    infinite bound the reference never ends, so that case is not run; the engine refuses any
+    infinite cost.)"""
+    nan_offset = from_dense([[1, 1]], [2], [INF], [1, 1], offset=float("nan"))
+    for impl in (oracle, reference):
+        assert impl.solve(nan_offset, tolerance=1e-8).status_name == "model_error"
+    lp = from_dense([[1, 1]], [2], [INF], [INF, 1.0], col_upper=[10, 10])
+    a = oracle.solve(lp, tolerance=1e-8, iteration_limit=400)
+    b = reference.solve(lp, tolerance=1e-8, iteration_limit=400)
+    assert a.status_name == b.status_name == "iteration_limit"
+    assert a.iterations == b.iterations == 400 and a.restarts == b.restarts
+    assert np.isnan(a.objective) and np.isnan(b.objective)
+    for u, v in ((a.col_value, b.col_value), (a.col_dual, b.col_dual), (a.row_dual, b.row_dual)):
+        assert np.array_equal(u, v, equal_nan=True)
