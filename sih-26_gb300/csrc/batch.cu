@@ -49,6 +49,7 @@ void BatchEngine::require_loaded() const {
 }
 
 void BatchEngine::load(int count, const sankhya_gb300_lp* lps) {
+  Trace trace("batch load");
   if (count <= 0 || lps == nullptr) {
     throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "a batch needs at least one LP"};
   }
@@ -211,6 +212,7 @@ void BatchEngine::load(int count, const sankhya_gb300_lp* lps) {
 
 void BatchEngine::solve(const sankhya_gb300_params& p, sankhya_gb300_batch_item* items,
                         double* device_seconds) {
+  Trace trace("batch solve");
   require_loaded();
   if (p.precision != SANKHYA_GB300_FP64 && p.precision != SANKHYA_GB300_MIXED) {
     throw EngineError{SANKHYA_GB300_ERROR_OPTION, "pdhg_precision must be fp64 or mixed"};
@@ -422,6 +424,7 @@ void BatchEngine::adjoint(const double* const* dl_dx, const double* const* dl_dy
                           const double* dl_df, double* const* dl_dc, double* const* dl_drl,
                           double* const* dl_dru, double* const* dl_dl, double* const* dl_du,
                           sankhya_gb300_adjoint_info* info) {
+  Trace trace("batch adjoint");
   require_loaded();
   if (!solved_) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no solve has run"};
   SGB_CUDA(cudaSetDevice(device_));
@@ -541,6 +544,7 @@ void BatchEngine::finish_adjoint(double* const* dl_dc, double* const* dl_drl,
 }
 
 void BatchEngine::polish(sankhya_gb300_batch_item* items, sankhya_gb300_adjoint_info* info) {
+  Trace trace("batch polish");
   require_loaded();
   if (!solved_) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no solve has run"};
   SGB_CUDA(cudaSetDevice(device_));

@@ -29,7 +29,22 @@
 #include <random>
 #include <thread>
 
+#if defined(__has_include)
+#if __has_include(<nvtx3/nvToolsExt.h>)
+#include <nvtx3/nvToolsExt.h>
+#define SGB_HAVE_NVTX 1
+#endif
+#endif
+
 namespace sgb {
+
+#ifdef SGB_HAVE_NVTX
+Trace::Trace(const char* name) { nvtxRangePushA(name); }
+Trace::~Trace() { nvtxRangePop(); }
+#else
+Trace::Trace(const char*) {}
+Trace::~Trace() {}
+#endif
 
 void cuda_check(cudaError_t err, const char* what, const char* file, int line) {
   if (err == cudaSuccess) return;
@@ -480,6 +495,7 @@ void validate_lp(const sankhya_gb300_lp& lp) {
 }
 
 void Engine::load(const sankhya_gb300_lp& lp) {
+  Trace trace("pdhg load");
   validate_lp(lp);
   const int m = lp.rows, n = lp.cols;
   const long long nnz = lp.col_starts[n];
@@ -912,6 +928,7 @@ void Engine::build_graphs(int steps) {
 void Engine::run_graphs(const sankhya_gb300_params& p, double t0, cudaGraphExec_t* graphs,
                         Ctl* snapshot, bool forward_log, long long iteration_offset,
                         int* stop_status) {
+  Trace trace("pdhg iterations");
   const bool has_time_limit = p.time_limit < 1e300;
   long long logged = 0;
   auto launch = [&](int slot) {
@@ -969,6 +986,7 @@ void Engine::final_evaluation() {
 // Device preconditioning, the spectral-norm estimate and the scaled entry range (the log
 // line of src/pdhg/pdhg.cpp:132-133); the same for both precisions.
 void Engine::setup(const sankhya_gb300_params& p, sankhya_gb300_result* r, double* norm) {
+  Trace trace("pdhg scaling");
   cudaStream_t s = stream_;
   precondition(p.random_seed);
   *norm = power_iteration(p.random_seed);
@@ -986,6 +1004,7 @@ void Engine::setup(const sankhya_gb300_params& p, sankhya_gb300_result* r, doubl
 
 void Engine::solve(const sankhya_gb300_params& p, sankhya_gb300_result* r) {
   require_loaded();
+  Trace trace(p.precision == SANKHYA_GB300_MIXED ? "pdhg solve (mixed)" : "pdhg solve");
   const double t0 = now_seconds();
   std::memset(r, 0, sizeof(*r));
   if (p.precision != SANKHYA_GB300_FP64 && p.precision != SANKHYA_GB300_MIXED) {

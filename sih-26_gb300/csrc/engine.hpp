@@ -12,6 +12,16 @@
 
 namespace sgb {
 
+// A named NVTX range for the lifetime of the object, marking an engine phase on a profiler's
+// timeline (nsys, or ncu's --nvtx filters). The names follow SANKHYA's profiler scopes. With no
+// tool attached NVTX calls return at once; without the NVTX headers this is empty.
+struct Trace {
+  explicit Trace(const char* name);
+  ~Trace();
+  Trace(const Trace&) = delete;
+  Trace& operator=(const Trace&) = delete;
+};
+
 // Raised inside the engine and turned into a status code at the C boundary.
 struct EngineError {
   int code;

@@ -24,6 +24,7 @@
 
 #include "sankhya/solve_control.hpp"
 #include "sankhya_gb300.h"
+#include "util/profiler.hpp"
 
 namespace sankhya::gpu {
 namespace {
@@ -173,6 +174,15 @@ Solution solve_pdhg_gpu(const Model& model, const Options& options, Logger& logg
   solution.dual_bound = result.dual_bound;
   solution.solve_seconds = result.solve_seconds;
   solution.recompute_quality(model);
+  // The profile SANKHYA keeps when its `profile` option is on (src/util/profiler.hpp): the
+  // restart counter the CPU engine keeps (src/pdhg/pdhg.cpp:479), and the GPU solve's two
+  // phases as regions the engine timed itself. The CPU engine's per-step "primal step" and
+  // "dual step" scopes have no host-side counterpart: the steps run inside CUDA graphs.
+  if (Profiler* profiler = logger.profiler(); profiler != nullptr) {
+    if (result.restarts > 0) profiler->count("pdhg restarts", result.restarts);
+    profiler->record("pdhg setup (gpu)", result.setup_seconds);
+    profiler->record("pdhg iterations (gpu)", result.loop_seconds, result.attempts);
+  }
   logger.info("");
   logger.info("Status: {}   objective {:.10e}   iterations {}   restarts {}   time {:.3f}s",
               to_string(solution.status), solution.objective, solution.iterations,

@@ -10,7 +10,9 @@
 // be created (kNumericalError with the engine's message, no fallback), an interrupt through
 // SolveControl (kInterrupted), and the iteration table written through the Logger. Last,
 // four threads solve different Models through the seam at the same time, as callers of
-// SANKHYA's solve() may: each must get its own Model's answer, bit for bit.
+// SANKHYA's solve() may: each must get its own Model's answer, bit for bit. And with a
+// profiler on the Logger, the seam reports the same "pdhg restarts" count as the CPU engine
+// and its two timed phases.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -26,6 +28,7 @@
 #include "sankhya/options.hpp"
 #include "sankhya/pdhg.hpp"
 #include "sankhya/solve_control.hpp"
+#include "util/profiler.hpp"
 
 extern "C" void standin_fail_create(int fail);
 
@@ -202,6 +205,36 @@ int main() {
     for (int k = 0; k < kThreads; ++k) {
       check(wrong[k] == 0, "concurrent callers get their own answers");
     }
+  }
+
+  // The profile: the same restart counter as the CPU engine, and the GPU phases.
+  {
+    const sankhya::Model model = make_model(17, false);
+    sankhya::Options o = make_options();
+    o.set_bool("pdhg_stop_at_request", false);
+    o.set_double("pdhg_tolerance", 1e-8);
+    sankhya::Profiler cpu_profile(sankhya::ProfileMode::kBasic);
+    sankhya::Profiler gpu_profile(sankhya::ProfileMode::kBasic);
+    sankhya::Logger cpu_log(nullptr), gpu_log(nullptr);
+    cpu_log.set_profiler(&cpu_profile);
+    gpu_log.set_profiler(&gpu_profile);
+    const sankhya::Solution c = sankhya::pdhg::solve_pdhg(model, o, cpu_log, nullptr);
+    const sankhya::Solution g = sankhya::gpu::solve_pdhg_gpu(model, o, gpu_log, nullptr);
+    auto counter = [](const sankhya::Profiler& p, const char* name) -> long long {
+      for (const auto& k : p.counters()) {
+        if (k.name == name) return k.value;
+      }
+      return -1;
+    };
+    const long long restarts = counter(cpu_profile, "pdhg restarts");
+    check(restarts > 0, "profile: the CPU engine restarted");
+    check(counter(gpu_profile, "pdhg restarts") == restarts, "profile: same restart count");
+    bool phases = false;
+    for (const auto& r : gpu_profile.regions()) {
+      if (r.name == "pdhg iterations (gpu)" && r.calls == g.iterations) phases = true;
+    }
+    check(phases, "profile: the GPU iterations region");
+    check(g.iterations == c.iterations, "profile: same solve");
   }
 
   if (g_failures != 0) {

@@ -17,6 +17,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -173,6 +174,15 @@ int sankhya_gb300_pdhg_solve(sankhya_gb300_pdhg* e, const sankhya_gb300_params* 
   if (p->log != nullptr) p->log(p->log_user, 40, e->solution.objective, 1e-3, 2e-3, 0.25);
   r->status = to_code(e->solution.status);
   r->iterations = e->solution.iterations;
+  // The restart count is not a Solution field; the engine's message carries it
+  // ("... after N iterations and R restarts ...", src/pdhg/pdhg.cpp:519-548). Every step of
+  // the CPU engine counts as one attempt here, and its time as the loop's.
+  const std::size_t at = e->solution.message.find(" iterations and ");
+  r->restarts = at == std::string::npos
+                    ? 0
+                    : std::atoll(e->solution.message.c_str() + at + std::strlen(" iterations and "));
+  r->attempts = e->solution.iterations;
+  r->loop_seconds = e->solution.solve_seconds;
   r->objective = e->solution.objective;
   r->dual_bound = e->solution.dual_bound;
   r->solve_seconds = e->solution.solve_seconds;
