@@ -133,6 +133,22 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
+def host_cpu():
+    """The host's CPU model (lscpu's "Model name") and architecture, for the CPU baseline."""
+    import platform
+
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:  # noqa: BLE001 - a missing lscpu only loses the description
+        pass
+    return {"model": model, "machine": platform.machine(), "logical_cpus": os.cpu_count()}
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -498,6 +514,7 @@ def main():
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": workload_config(lp, "fp64"),
                 "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
+                                 "host": host_cpu(),
                                  "sample": f"per step: oracle setup + {sample} FP64 iterations "
                                            f"on {threads} threads, extrapolated to "
                                            f"{FP64_ITERATIONS_TO_1E8} iterations"},
@@ -589,6 +606,7 @@ def main():
         except Exception as exc:  # noqa: BLE001
             single = {"error": f"{type(exc).__name__}: {exc}"}
         cpu = {"value": setup + per_it * its, "unit": "s", "cores": threads, "kind": "port",
+               "host": host_cpu(),
                "sample": f"oracle setup + {args.cpu_iterations} FP64 iterations on {threads} "
                          f"threads ({sample_s:.1f} s of CPU work), extrapolated to {its} "
                          f"iterations",

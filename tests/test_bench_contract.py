@@ -129,6 +129,7 @@ def test_default_line(monkeypatch):
     cpu = line["cpu_baseline"]
     assert cpu["kind"] == "port" and cpu["cores"] >= 1 and cpu["value"] > 0
     assert cpu["single_thread"].get("cores") == 1
+    assert cpu["host"]["machine"] and cpu["host"]["logical_cpus"] >= cpu["cores"]
     e2e = line["e2e"]
     assert e2e["h2d_bytes_per_step"] > 0 and e2e["d2h_bytes_per_step"] > 0
     assert line["gpu_launches"] > 0
@@ -143,5 +144,6 @@ def test_reference_line(monkeypatch):
     assert line["impl"] == "reference"
     assert line["value"] > 0 and line["unit"] == "s"
     assert line["cpu_baseline"]["value"] == line["value"]
+    assert line["cpu_baseline"]["host"]["machine"]
     assert line["e2e"] == {"value": line["value"], "unit": "s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
