@@ -4,8 +4,9 @@ Bars (see each test):
 * device preconditioning: Dr, Dc and the scaled values bit-identical to the reference's
   build_scaling; the spectral-norm estimate within 1e-14 relative (its two norms are summed
   in a different order);
-* sparse products on short rows: bit-identical to SparseMatrix::multiply /
-  transpose_multiply (same summation order); on long rows, within 1e-13 relative;
+* sparse products: SparseMatrix::multiply / transpose_multiply's summation order, with
+  FMA, so every entry is within 1e-14 * sum |a_ij| |v_j| of the reference's (a few ulps), on
+  short rows and on long rows summed in chunks;
 * solves: the same status, the objective within 1e-6 relative of the oracle's (the
   engine's parity bar; the achieved difference is printed), the reported point's relative KKT
   (re-evaluated by the oracle's own evaluate) within the requested tolerance.
