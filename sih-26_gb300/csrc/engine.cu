@@ -274,7 +274,9 @@ size_t estimate_memory(long long rows, long long cols, long long nnz, int precis
   if (precision == SANKHYA_GB300_MIXED) {
     bytes += 2 * z * sizeof(float) + (10 * n + 8 * m) * sizeof(float);
   }
-  bytes += 8u << 20;  // partial-sum buffers and the control block (generous)
+  // Fixed: the kernels' device code (a 5.8 MB fatbin, loaded at the first launch, after a
+  // caller's memory check), the partial-sum buffers and the control block.
+  bytes += 16u << 20;
   return bytes;
 }
 

@@ -16,12 +16,17 @@
 //     reference's CPU PDHG;
 //  5. algorithm=auto routes a model of 100,000 rows to the GPU when the device answers;
 //  6. the C API (sankhya_solve with the gpu option set) reaches the seam;
-//  7. the version banner names the device the seam reports.
+//  7. the version banner names the device the seam reports;
+//  8. tests/unit/test_multi_gpu.cpp:191-228 restated: solve_pdhg_multi_gpu with the virtual
+//     devices {0, 0} gives the single-device answer (afiro, 1e-6, no polish). The reference
+//     expects its own "pdhg-cuda-multi" algorithm name there; this seam keeps an LP on one
+//     device and says "pdhg-gpu".
 //
 // `frontend_check --write model.mps out.sol` instead solves the model once through solve()
 // with algorithm=pdhg, gpu=true (tolerance 1e-8, no polish) and writes the answer with the
 // reference's own writer (io::write_solution), for the reference's independent verifier
 // (tools/verify_solution.py). It fails if the solve did not go through the seam.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -33,6 +38,8 @@
 #include "sankhya/options.hpp"
 #include "sankhya/sankhya.h"
 #include "sankhya/version.hpp"
+#include "gpu/pdhg_gpu.hpp"
+#include "gpu/pdhg_multi_gpu.hpp"
 
 extern "C" {
 void standin_fail_create(int fail);
@@ -269,6 +276,24 @@ int main(int argc, char** argv) {
   // 7. The banner reports the device through the seam's probe.
   check(std::string(sankhya::banner()).find("GB300 (stand-in)") != std::string::npos,
         std::string("banner names the device: ") + sankhya::banner());
+
+  // 8. Two virtual devices on device 0.
+  {
+    sankhya::Options o;
+    o.set_bool("log_to_console", false);
+    o.set_double("pdhg_tolerance", 1e-6);
+    o.set_bool("pdhg_polish", false);
+    o.set_int("iteration_limit", 500000);
+    sankhya::Logger silent(nullptr);
+    const sankhya::Solution single = sankhya::gpu::solve_pdhg_gpu(model, o, silent);
+    const sankhya::Solution multi = sankhya::gpu::solve_pdhg_multi_gpu(model, o, {0, 0}, silent);
+    check(single.status == sankhya::SolveStatus::kOptimal, "virtual devices: single optimal");
+    check(multi.status == sankhya::SolveStatus::kOptimal, "virtual devices: multi optimal");
+    check(std::fabs(multi.objective - single.objective) <=
+              1e-5 * std::max(1.0, std::fabs(single.objective)),
+          "virtual devices: the single-device objective");
+    check(multi.algorithm == "pdhg-gpu", "virtual devices: one device (" + multi.algorithm + ")");
+  }
 
   if (g_failures == 0) std::printf("OK\n");
   return g_failures == 0 ? 0 : 1;

@@ -152,3 +152,26 @@ def test_python_bindings_reach_the_engine_through_the_seam(reference_core_librar
                          timeout=600, env=env)
     assert run.returncode == 0, run.stdout[-2000:] + run.stderr[-2000:]
     assert run.stdout.startswith("OK"), run.stdout
+
+
+def test_reference_unit_tests_of_the_replaced_pieces(tmp_path):
+    """`tests/host/seam_units_check.cpp`: the reference's tests of the VRAM estimate and
+    reserve (tests/unit/test_gpu_memory.cpp) and of the compute-capability gate
+    (tests/unit/test_gpu_device.cpp), restated against seam/gpu_memory.cpp linked with the
+    engine library itself, at this engine's minimum architecture 10.3."""
+    flags, _, _ = core_link_args()
+    sys.path.insert(0, os.path.join(ROOT, "sih-26_gb300"))
+    from sankhya_gb300 import _paths, build
+
+    build.build_engine()
+    libdir = os.path.dirname(_paths.ENGINE_LIB)
+    exe = str(tmp_path / "seam_units_check")
+    cmd = (["g++"] + flags + [os.path.join(SEAM, "gpu_memory.cpp"),
+                              os.path.join(ROOT, "tests", "host", "seam_units_check.cpp"),
+                              f"-L{libdir}", "-lsankhya_gb300", f"-Wl,-rpath,{libdir}",
+                              "-o", exe])
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr[-2000:]
+    run = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, run.stdout[-2000:] + run.stderr[-2000:]
+    assert run.stdout.strip().endswith("OK"), run.stdout
