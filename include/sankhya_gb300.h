@@ -216,7 +216,8 @@ SGB_API int sankhya_gb300_pdhg_spmv(sankhya_gb300_pdhg* engine, int32_t op, int3
  * pointers; the work is enqueued on `stream` (a cudaStream_t; NULL = the engine's stream)
  * and the call returns without waiting for it. Its only scratch is a fixed device array of
  * SANKHYA_GB300_NOALLOC_MAX_CHUNKS partial sums (one per 2048 entries of each row longer than
- * 2048) plus a counter; a matrix that needs more slots is refused with
+ * 2048) plus a counter, 128 KiB that every GPU which loads this library keeps until the
+ * process exits; a matrix that needs more slots is refused with
  * SANKHYA_GB300_ERROR_ARGUMENT. The first call on a device sets that scratch up (finds it and
  * clears the counter, waiting for the stream) and must come before any stream capture.
  * Calls on one device share the scratch: calls that overlap in time race, so order them
