@@ -28,6 +28,10 @@ def _cases():
            dict(tolerance=1e-8, restart=False, iteration_limit=3000))
     yield ("seed_5", lpgen.planted_uniform(100, 250, 5, seed=9),
            dict(tolerance=1e-6, random_seed=5))
+    # Zipf row lengths and values of log-uniform magnitude over [1e-3, 1e3]: the badly scaled
+    # family, where the scaling does the most work.
+    yield ("zipf_badly_scaled", lpgen.planted_zipf(300, 600, 6000, max_len=400, seed=4),
+           dict(tolerance=1e-8, iteration_limit=20000))
 
 
 @pytest.mark.parametrize("name,lp,kw", list(_cases()), ids=[c[0] for c in _cases()])
