@@ -200,25 +200,42 @@ class Oracle:
                            _ptr(act, ctypes.c_double), _ptr(red, ctypes.c_double))
         return r.as_dict(), act, red
 
-    # Restatement-only helpers.
     def multiply(self, lp, x):
+        """y = A x (SparseMatrix::multiply)."""
         lp = lp.contiguous()
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.zeros(lp.rows)
+        if self.reference:
+            c, keep = self._clp(lp)
+            self.lib.ref_multiply.argtypes = [ctypes.POINTER(CLp), _D, _D]
+            self.lib.ref_multiply.restype = None
+            self.lib.ref_multiply(ctypes.byref(c), _ptr(x, ctypes.c_double),
+                                  _ptr(y, ctypes.c_double))
+            return y
         self.lib.orc_multiply(lp.rows, lp.cols, _ptr(lp.col_starts, ctypes.c_int32),
                               _ptr(lp.row_index, ctypes.c_int32), _ptr(lp.values, ctypes.c_double),
                               _ptr(x, ctypes.c_double), _ptr(y, ctypes.c_double))
         return y
 
     def transpose_multiply(self, lp, y):
+        """x = A^T y (SparseMatrix::transpose_multiply)."""
         lp = lp.contiguous()
         y = np.ascontiguousarray(y, dtype=np.float64)
         x = np.zeros(lp.cols)
+        if self.reference:
+            c, keep = self._clp(lp)
+            self.lib.ref_transpose_multiply.argtypes = [ctypes.POINTER(CLp), _D, _D]
+            self.lib.ref_transpose_multiply.restype = None
+            self.lib.ref_transpose_multiply(ctypes.byref(c), _ptr(y, ctypes.c_double),
+                                            _ptr(x, ctypes.c_double))
+            return x
         self.lib.orc_transpose_multiply(lp.rows, lp.cols, _ptr(lp.col_starts, ctypes.c_int32),
                                         _ptr(lp.row_index, ctypes.c_int32),
                                         _ptr(lp.values, ctypes.c_double), _ptr(y, ctypes.c_double),
                                         _ptr(x, ctypes.c_double))
         return x
+
+    # Restatement-only helper.
 
     def power_start(self, seed, count):
         out = np.zeros(count)

@@ -187,6 +187,18 @@ orc_residuals ref_evaluate(const orc_lp* lp, const double* x, const double* y, d
   return to_c(r);
 }
 
+// The reference's sparse products on the LP's matrix: y = A x (SparseMatrix::multiply,
+// src/la/sparse.cpp:232-242,261-264) and x = A^T y (transpose_multiply, :244-259,266-269).
+void ref_multiply(const orc_lp* lp, const double* x, double* y) {
+  const sankhya::Model model = to_model(lp);
+  model.matrix.multiply(x, y);
+}
+
+void ref_transpose_multiply(const orc_lp* lp, const double* y, double* x) {
+  const sankhya::Model model = to_model(lp);
+  model.matrix.transpose_multiply(y, x);
+}
+
 // ---- Models built by the reference's own code ------------------------------------------
 
 struct ref_model {

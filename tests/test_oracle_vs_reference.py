@@ -88,3 +88,42 @@ def test_inputs_at_the_edge_of_validation(reference, oracle):
     assert np.isnan(a.objective) and np.isnan(b.objective)
     for u, v in ((a.col_value, b.col_value), (a.col_dual, b.col_dual), (a.row_dual, b.row_dual)):
         assert np.array_equal(u, v, equal_nan=True)
+
+
+def _random_lp(rng, m, n, density):
+    """A random m x n matrix in CSC with the given density (explicit zeros dropped)."""
+    dense = np.where(rng.random((m, n)) < density, rng.normal(size=(m, n)), 0.0)
+    starts, rows, vals = [0], [], []
+    for j in range(n):
+        nz = np.flatnonzero(dense[:, j])
+        rows += nz.tolist()
+        vals += dense[nz, j].tolist()
+        starts.append(len(rows))
+    from sankhya_gb300.model import LP
+
+    lp = LP(m, n, np.array(starts, np.int32), np.array(rows, np.int32), np.array(vals),
+            np.zeros(n), np.zeros(n), np.full(n, 1.0), np.zeros(m), np.zeros(m))
+    return lp, dense
+
+
+def test_products_match_the_reference_and_a_dense_product(reference, oracle):
+    """The oracle's A x and A^T y (src/la/sparse.cpp:232-269) against the reference's own
+    SparseMatrix products, bit for bit, and against a dense product to 1e-9 as the
+    reference's FuzzMatVecAgainstDenseReference holds them (tests/unit/test_sparse.cpp:190-226):
+    500 matrices of 1-40 rows and columns at densities 0.02, 0.1, 0.4 and 0.95. A third of the
+    vector entries are zero (A x skips those columns) and some are -0.0."""
+    rng = np.random.default_rng(20260825)
+    densities = (0.02, 0.1, 0.4, 0.95)
+    for trial in range(500):
+        m, n = (int(v) for v in rng.integers(1, 41, size=2))
+        lp, dense = _random_lp(rng, m, n, densities[trial % 4])
+        x = rng.normal(size=n)
+        x[rng.random(n) < 1 / 3] = 0.0
+        x[rng.random(n) < 0.05] = -0.0
+        y = rng.normal(size=m)
+        ax, aty = oracle.multiply(lp, x), oracle.transpose_multiply(lp, y)
+        assert np.array_equal(ax, reference.multiply(lp, x)), trial
+        assert np.array_equal(np.signbit(ax), np.signbit(reference.multiply(lp, x))), trial
+        assert np.array_equal(aty, reference.transpose_multiply(lp, y)), trial
+        assert np.all(np.abs(ax - dense @ x) <= 1e-9), trial
+        assert np.all(np.abs(aty - dense.T @ y) <= 1e-9), trial
