@@ -49,8 +49,16 @@ def test_solve_is_bit_identical(reference, oracle, name, lp, kw):
     assert np.array_equal(a.row_dual, b.row_dual)
 
 
-def test_scaling_and_norm_are_bit_identical(reference, oracle):
-    lp = lpgen.planted_blocks(4, 60, 120, 9, seed=11)
+_SCALING_CASES = [
+    ("blocks", lambda: lpgen.planted_blocks(4, 60, 120, 9, seed=11)),
+    ("zipf_badly_scaled", lambda: lpgen.planted_zipf(300, 600, 6000, max_len=400, seed=4)),
+    ("general_free", lambda: lpgen.planted_general(50, 80, 3, seed=6, maximize=True, free=True)),
+]
+
+
+@pytest.mark.parametrize("make", [c[1] for c in _SCALING_CASES], ids=[c[0] for c in _SCALING_CASES])
+def test_scaling_and_norm_are_bit_identical(reference, oracle, make):
+    lp = make()
     a = oracle.build_scaling(lp)
     b = reference.build_scaling(lp)
     for k in ("values", "row", "col", "cost", "col_lower", "col_upper", "row_lower", "row_upper",
@@ -59,8 +67,9 @@ def test_scaling_and_norm_are_bit_identical(reference, oracle):
     assert oracle.spectral_norm(lp, 30, 1) == reference.spectral_norm(lp, 30, 1)
 
 
-def test_evaluate_is_bit_identical(reference, oracle):
-    lp = lpgen.planted_general(50, 80, 3, seed=4)
+@pytest.mark.parametrize("make", [c[1] for c in _SCALING_CASES], ids=[c[0] for c in _SCALING_CASES])
+def test_evaluate_is_bit_identical(reference, oracle, make):
+    lp = make()
     rng = np.random.default_rng(0)
     x = rng.normal(size=lp.cols)
     y = rng.normal(size=lp.rows)
