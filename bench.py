@@ -149,6 +149,13 @@ def host_cpu():
     return {"model": model, "machine": platform.machine(), "logical_cpus": os.cpu_count()}
 
 
+# What the CPU baseline runs: the C restatement of the reference's PDHG, which the tests hold
+# bit-identical to the reference's own sources compiled on x86-64.
+CPU_BASELINE_PORT_OF = ("sankhya::pdhg::solve_pdhg (src/pdhg/pdhg.cpp) restated in C; "
+                        "bit-identical to the reference's own build on x86-64 "
+                        "(tests/test_oracle_vs_reference.py)")
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -514,7 +521,7 @@ def main():
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": workload_config(lp, "fp64"),
                 "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
-                                 "host": host_cpu(),
+                                 "port_of": CPU_BASELINE_PORT_OF, "host": host_cpu(),
                                  "sample": f"per step: oracle setup + {sample} FP64 iterations "
                                            f"on {threads} threads, extrapolated to "
                                            f"{FP64_ITERATIONS_TO_1E8} iterations"},
@@ -606,7 +613,7 @@ def main():
         except Exception as exc:  # noqa: BLE001
             single = {"error": f"{type(exc).__name__}: {exc}"}
         cpu = {"value": setup + per_it * its, "unit": "s", "cores": threads, "kind": "port",
-               "host": host_cpu(),
+               "port_of": CPU_BASELINE_PORT_OF, "host": host_cpu(),
                "sample": f"oracle setup + {args.cpu_iterations} FP64 iterations on {threads} "
                          f"threads ({sample_s:.1f} s of CPU work), extrapolated to {its} "
                          f"iterations",
