@@ -147,3 +147,34 @@ def test_reference_line(monkeypatch):
     assert line["cpu_baseline"]["host"]["machine"]
     assert line["e2e"] == {"value": line["value"], "unit": "s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+
+
+def test_pinned_inputs_are_exact_copies(monkeypatch):
+    """bench.pinned_lp copies the LP into tensors allocated with pin_memory=True. Without a
+    device here the allocation is made ordinary; the copy must still be exact and keep every
+    dtype, and a failure anywhere must fall back to the LP itself."""
+    torch = pytest.importorskip("torch")
+    import bench
+    from sankhya_gb300 import build, lpgen
+
+    build.build_lpgen()
+    lp = lpgen.planted_uniform(30, 70, 4, seed=2)
+    real_empty = torch.empty
+    monkeypatch.setattr(torch.cuda, "is_available", lambda: True)
+    monkeypatch.setattr(torch, "empty",
+                        lambda *a, pin_memory=False, **k: real_empty(*a, **k))
+    out, pinned = bench.pinned_lp(lp)
+    assert pinned and out is not lp
+    for name in ("col_starts", "row_index", "values", "col_cost", "col_lower", "col_upper",
+                 "row_lower", "row_upper"):
+        a, b = getattr(lp, name), getattr(out, name)
+        assert b.dtype == a.dtype and np.array_equal(a, b), name
+    assert (out.rows, out.cols, out.sense, out.objective_offset) == (lp.rows, lp.cols, lp.sense,
+                                                                     lp.objective_offset)
+
+    def fail(*a, **k):
+        raise RuntimeError("no page-locked memory")
+
+    monkeypatch.setattr(torch, "empty", fail)
+    same, pinned = bench.pinned_lp(lp)
+    assert same is lp and not pinned
