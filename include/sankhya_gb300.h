@@ -221,7 +221,13 @@ SGB_API int sankhya_gb300_pdhg_spmv(sankhya_gb300_pdhg* engine, int32_t op, int3
  * SANKHYA_GB300_ERROR_ARGUMENT. The first call on a device sets that scratch up (finds it and
  * clears the counter, waiting for the stream) and must come before any stream capture.
  * Calls on one device share the scratch: calls that overlap in time race, so order them
- * (one stream, or events between streams). */
+ * (one stream, or events between streams). The scratch's device address is looked up once
+ * per device index and kept for the life of the process: after cudaDeviceReset (or anything
+ * else that destroys the device's primary context) the kept address is stale, so a process
+ * that resets a device must not call this entry point on it again. The call does not wait
+ * for the product, so it cannot report a failure of the product itself: if a bounded wait in
+ * the product gives up (a copy that never lands), the rows it could not finish are set to
+ * NaN instead of being left with a result that looks valid. */
 #define SANKHYA_GB300_NOALLOC_MAX_CHUNKS 16384
 SGB_API int sankhya_gb300_pdhg_spmv_noalloc(sankhya_gb300_pdhg* engine, int32_t op,
                                             int32_t scaled, const double* device_in,

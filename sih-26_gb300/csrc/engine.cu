@@ -100,6 +100,7 @@ template struct DeviceArray<BatchOutcome>;
 template struct DeviceArray<AdjointOutcome>;
 template struct DeviceArray<signed char>;
 template struct DeviceArray<long long>;
+template struct DeviceArray<ChunkSeg>;
 
 namespace {
 
@@ -303,8 +304,10 @@ Engine::Engine(int device) : device_(device) {
   SGB_CUDA(cudaMemset(ctl_.ptr, 0, sizeof(Ctl)));
   ctl_mixed_.allocate(1);
   SGB_CUDA(cudaMemset(ctl_mixed_.ptr, 0, sizeof(Ctl)));
-  configure_tile_kernels();
-  configure_mixed_kernels();
+  if (!configure_tile_kernels() || !configure_mixed_kernels()) {
+    throw EngineError{SANKHYA_GB300_ERROR_DEVICE,
+                      format("device %d refused the kernels' shared-memory limits", device)};
+  }
 }
 
 Engine::~Engine() {
@@ -353,6 +356,12 @@ void Engine::allocate_mixed() {
   }
   for (DeviceArray<double>* a : {&anchor_x_, &aty64_}) a->allocate(n);
   for (DeviceArray<double>* a : {&anchor_y_, &ax64_}) a->allocate(m);
+  for (ChunkDev* D : {&ck_csc_f_, &ck_csr_f_}) {
+    if (!D->split) continue;
+    D->fval.allocate_padded(static_cast<size_t>(D->nmain), kPad, s);
+    D->foval.allocate_padded(static_cast<size_t>(D->nouter), kPad, s);
+    D->fouter.allocate_padded(static_cast<size_t>(D->nrows), kPad, s);
+  }
   fill_mixed_buffers();
   mixed_ready_ = true;
 }
@@ -392,25 +401,21 @@ void Engine::fill_mixed_buffers() {
   b.v_best = vbest_.ptr;
   b.part_primal = part_primal_.ptr;
   b.part_dual = part_dual_.ptr;
-  b.chunk_primal = chunk_primal_.ptr;
-  b.chunk_dual = chunk_dual_.ptr;
+  b.csc_k = chunk_set(ck_csc_f_, csc_ptr_.ptr, csc_idx_.ptr, csc_f_.ptr);
+  b.csr_k = chunk_set(ck_csr_f_, csr_ptr_.ptr, csr_idx_.ptr, csr_f_.ptr);
+  b.piece_primal = ck_csc_f_.pieces.ptr;
+  b.piece_dual = ck_csr_f_.pieces.ptr;
   b.part_rows0 = part_rows0_.ptr;
   b.part_cols = part_cols_.ptr;
   b.part_rows1 = part_rows1_.ptr;
   b.chunk_cols = chunk_cols_.ptr;
   b.chunk_rows = chunk_rows_.ptr;
-  b.csc.tile_win = step_csc_f_.tile_win.ptr;
-  b.csc.windows = step_csc_f_.windows.ptr;
-  b.csc.wmax = step_csc_f_.wmax;
-  b.csr.tile_win = step_csr_f_.tile_win.ptr;
-  b.csr.windows = step_csr_f_.windows.ptr;
-  b.csr.wmax = step_csr_f_.wmax;
   b.grid_primal = grid_csc_f_;
   b.grid_dual = grid_csr_f_;
-  b.grid_step_primal = step_csc_f_.grid;
-  b.grid_step_dual = step_csr_f_.grid;
-  b.smem_primal = step_csc_f_.smem;
-  b.smem_dual = step_csr_f_.smem;
+  b.grid_step_primal = ck_csc_f_.grid;
+  b.grid_step_dual = ck_csr_f_.grid;
+  b.smem_primal = ck_csc_f_.smem;
+  b.smem_dual = ck_csr_f_.smem;
   b.m = m_;
   b.n = n_;
 }
@@ -581,13 +586,15 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   const size_t z = static_cast<size_t>(nnz);
 
   // The step passes' windows of the gathered vector: the column passes gather y (m rows),
-  // the row passes the packed (2x' - x, x' - x) (n columns). SANKHYA_GB300_WINDOW_CAP caps
-  // the capacity (0 turns staging off), so tests can force partial windows on small LPs.
+  // the row passes the packed (2x' - x, x' - x) (FP64) or du (FP32) (n columns).
+  // SANKHYA_GB300_WINDOW_CAP caps the capacity (0 turns staging off), so tests can force
+  // partial windows on small LPs; in the FP32 chunk layouts it also splits every layout whose
+  // windows hold any entry, so tests run the split form.
   int cap = -1;
   if (const char* env = std::getenv("SANKHYA_GB300_WINDOW_CAP")) cap = std::max(0, std::atoi(env)) & ~3;
   const auto make_layout = [&](StepLayout& L, const std::vector<Tile>& tiles, const int* idx,
-                               int extent, int pass, bool mixed) {
-    int wmax = mixed ? mixed_window_capacity(pass) : fp64_window_capacity(pass);
+                               int extent, int pass) {
+    int wmax = fp64_window_capacity(pass);
     if (cap >= 0) wmax = std::min(wmax, cap);
     std::vector<int> tile_win;
     std::vector<int2> windows;
@@ -610,19 +617,18 @@ void Engine::load(const sankhya_gb300_lp& lp) {
     L.nwindows = static_cast<int>(windows.size());
     L.wmax = 0;
     for (const int2& w : windows) L.wmax = std::max(L.wmax, w.y);
-    L.smem = mixed ? mixed_step_smem(pass, L.wmax) : fp64_step_smem(pass, L.wmax);
-    const int per_sm = mixed ? mixed_step_blocks_per_sm(pass, L.smem)
-                             : fp64_step_blocks_per_sm(pass, L.smem);
+    L.smem = fp64_step_smem(pass, L.wmax);
+    const int per_sm = fp64_step_blocks_per_sm(pass, L.smem);
     L.grid = std::max(1, std::min(static_cast<int>(tiles.size()), per_sm * num_sms_));
     L.tile_win.upload(tile_win.data(), tile_win.size(), s);
     L.windows.upload(windows.data(), windows.size(), s);
   };
-  make_layout(step_csc_, ctiles, lp.row_index, m, 0, false);
-  make_layout(step_csr_, rtiles, ridx.data(), n, 1, false);
-  make_layout(step_csc_f_, ctiles_f, lp.row_index, m, 0, true);
-  make_layout(step_csr_f_, rtiles_f, ridx.data(), n, 1, true);
-  grid_c = std::max({grid_c, step_csc_.grid, step_csc_f_.grid});
-  grid_r = std::max({grid_r, step_csr_.grid, step_csr_f_.grid});
+  make_layout(step_csc_, ctiles, lp.row_index, m, 0);
+  make_layout(step_csr_, rtiles, ridx.data(), n, 1);
+  plan_layout(ck_csc_f_, cptr, lp.row_index, n, m, 0, cap);
+  plan_layout(ck_csr_f_, rptr, ridx.data(), m, n, 1, cap);
+  grid_c = std::max({grid_c, step_csc_.grid, ck_csc_f_.grid});
+  grid_r = std::max({grid_r, step_csr_.grid, ck_csr_f_.grid});
 
   // Row pointers are staged per tile in 16-byte units too: kPad entries of padding.
   csc_ptr_.upload_padded(cptr.data(), cptr.size(), kPad, s);
@@ -666,8 +672,8 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   part_cols_.allocate(static_cast<size_t>(grid_c + 1) * kEvalColSlots);
   part_rows1_.allocate(static_cast<size_t>(grid_r) * kEvalRowSlots);
   chunk_primal_.allocate(static_cast<size_t>(nchunks_csc_) + 1);
-  chunk_cols_.allocate(2 * static_cast<size_t>(nchunks_csc_) + 2);
   chunk_dual_.allocate(2 * static_cast<size_t>(nchunks_csr_) + 2);
+  chunk_cols_.allocate(2 * static_cast<size_t>(nchunks_csc_) + 2);
   chunk_rows_.allocate(2 * static_cast<size_t>(nchunks_csr_) + 2);
   chunk_spmv_.allocate(static_cast<size_t>(std::max(nchunks_csc_, nchunks_csr_)) + 1);
   scalars_.allocate(static_cast<size_t>(pgrid) * 2 + 16);
@@ -677,6 +683,87 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   SGB_CUDA(cudaStreamSynchronize(s));
   fill_buffers();
   loaded_ = true;
+}
+
+// One FP32 step pass's chunk layout: planned on the host (plan_chunks), uploaded, and its
+// piece and split buffers allocated. Windows are kept over every entry when they hold at least
+// 99.9% of them and the layout is split from 50% up; a capacity set through
+// SANKHYA_GB300_WINDOW_CAP (window_cap >= 0) splits any layout whose windows hold an entry.
+void Engine::plan_layout(ChunkDev& D, const std::vector<int>& lptr, const int* lidx, int lines,
+                         int extent, int pass, int window_cap) {
+  cudaStream_t s = stream_;
+  int wmax = mixed_window_capacity(pass);
+  if (window_cap >= 0) wmax = std::min(wmax, window_cap);
+  const double split_min = window_cap >= 0 ? 0.0 : 0.5;
+  // The outer sums stage their products in the block's warp buffers.
+  const int round_cap = (kChunkThreads / 32) * kChunkCapF;
+  ChunkPlan P = plan_chunks(lptr, lidx, lines, extent, kChunkCapF, wmax, num_sms_,
+                            static_cast<int>(sizeof(float)), split_min, 0.999, round_cap);
+  if (P.error) throw EngineError{SANKHYA_GB300_ERROR_DEVICE, "chunk layout planning failed"};
+  D.nrows = lines;
+  D.split = P.split;
+  D.nlong = static_cast<int>(P.longs.size());
+  D.npieces = P.npieces;
+  D.wmax = P.wmax;
+  D.grid = P.grid;
+  D.staged = P.staged;
+  D.coverage = P.coverage;
+  D.smem = mixed_step_smem(pass, P.wmax);
+  D.chunks.upload(P.chunks.data(), P.chunks.size(), s);
+  D.longs.upload(P.longs.data(), P.longs.size(), s);
+  D.segs.upload(P.segs.data(), P.segs.size(), s);
+  D.seg_start.upload(P.seg_start.data(), P.seg_start.size(), s);
+  D.pieces.allocate(static_cast<size_t>(D.npieces) + 1);
+  D.nmain = D.nouter = 0;
+  if (P.split) {
+    D.nmain = static_cast<long long>(P.idx.size());
+    D.nouter = static_cast<long long>(P.oidx.size());
+    D.ptr.upload_padded(P.ptr.data(), P.ptr.size(), kPad, s);
+    D.idx.upload_padded(P.idx.data(), P.idx.size(), kPad, s);
+    D.map.upload(P.map.data(), P.map.size(), s);
+    D.optr.upload_padded(P.optr.data(), P.optr.size(), kPad, s);
+    D.oidx.upload_padded(P.oidx.data(), P.oidx.size(), kPad, s);
+    D.omap.upload(P.omap.data(), P.omap.size(), s);
+    D.orounds.upload(P.orounds.data(), P.orounds.size(), s);
+    D.oround_start.upload(P.oround_start.data(), P.oround_start.size(), s);
+  } else {
+    for (DeviceArray<int>* a : {&D.ptr, &D.idx, &D.map, &D.optr, &D.oidx, &D.omap}) a->release();
+    D.orounds.release();
+    D.oround_start.release();
+  }
+  D.fval.release();
+  D.foval.release();
+  D.fouter.release();
+}
+
+ChunkSet<float> Engine::chunk_set(const ChunkDev& D, const int* full_ptr, const int* full_idx,
+                                  const float* full_val) const {
+  ChunkSet<float> c{};
+  c.chunks = D.chunks.ptr;
+  c.segs = D.segs.ptr;
+  c.seg_start = D.seg_start.ptr;
+  c.longs = D.longs.ptr;
+  c.nlong = D.nlong;
+  c.npieces = D.npieces;
+  c.nrows = D.nrows;
+  c.wmax = D.wmax;
+  if (D.split) {
+    c.ptr = D.ptr.ptr;
+    c.idx = D.idx.ptr;
+    c.optr = D.optr.ptr;
+    c.oidx = D.oidx.ptr;
+    c.orounds = D.orounds.ptr;
+    c.oround_start = D.oround_start.ptr;
+    c.val = D.fval.ptr;
+    c.oval = D.foval.ptr;
+    c.outer = D.fouter.ptr;
+  } else {
+    c.ptr = full_ptr;
+    c.idx = full_idx;
+    c.val = full_val;
+    c.outer = nullptr;
+  }
+  return c;
 }
 
 void Engine::fill_buffers() {
@@ -780,6 +867,20 @@ void Engine::precondition(long long seed) {
   scaled_ = true;
 }
 
+// The FP32 scaled values of the split chunk layouts' main and outer parts, gathered from the
+// full layouts' FP64 scaled values (each mixed solve, after the preconditioning).
+void Engine::fill_split_values() {
+  cudaStream_t s = stream_;
+  const std::pair<ChunkDev*, const double*> layouts[] = {{&ck_csc_f_, csc_s_.ptr},
+                                                          {&ck_csr_f_, csr_s_.ptr}};
+  for (const auto& l : layouts) {
+    ChunkDev& D = *l.first;
+    if (!D.split) continue;
+    launch_gather_values(l.second, D.map.ptr, D.fval.ptr, D.nmain, s);
+    launch_gather_values(l.second, D.omap.ptr, D.foval.ptr, D.nouter, s);
+  }
+}
+
 // src/la/scaling.cpp:161-194 on the device. The start vector is the reference's own
 // std::mt19937(seed) + uniform_real_distribution(-1, 1) stream, drawn on the host.
 double Engine::power_iteration(long long seed) {
@@ -797,17 +898,17 @@ double Engine::power_iteration(long long seed) {
   for (int step = 0; step < iterations; ++step) {
     launch_sumsq(power_v_.ptr, n_, scalars_.ptr, norms + 2 * step, tickets_.ptr, s, grid);
     launch_scale_div(power_v_.ptr, n_, norms + 2 * step, s);
-    launch_spmv(step_.csr, power_v_.ptr, power_av_.ptr, chunk_spmv_.ptr, tickets_.ptr + 1, s,
-                grid_csr_);
-    launch_spmv(step_.csc, power_av_.ptr, power_v_.ptr, chunk_spmv_.ptr, tickets_.ptr + 1, s,
-                grid_csc_);
+    launch_spmv(step_.csr, power_v_.ptr, power_av_.ptr, chunk_spmv_.ptr, tickets_.ptr + 1,
+                product_error(), s, grid_csr_);
+    launch_spmv(step_.csc, power_av_.ptr, power_v_.ptr, chunk_spmv_.ptr, tickets_.ptr + 1,
+                product_error(), s, grid_csc_);
     launch_sumsq(power_v_.ptr, n_, scalars_.ptr, norms + 2 * step + 1, tickets_.ptr, s, grid);
   }
   SGB_CUDA(cudaGetLastError());
   std::vector<double> host(2 * iterations);
   SGB_CUDA(cudaMemcpyAsync(host.data(), norms, host.size() * sizeof(double),
                            cudaMemcpyDeviceToHost, s));
-  SGB_CUDA(cudaStreamSynchronize(s));
+  check_product_error();
   double norm = 0.0;
   for (int step = 0; step < iterations; ++step) {
     if (std::sqrt(host[2 * step]) == 0.0) return 1.0;
@@ -847,13 +948,33 @@ void Engine::spmv(int op, int scaled, const double* in, double* out) {
   dout.allocate(static_cast<size_t>(out_len));
   TileSet<double> a = op == 0 ? step_.csr : step_.csc;
   if (!scaled) a.val = op == 0 ? csr_raw_.ptr : csc_raw_.ptr;
-  launch_spmv(a, din.ptr, dout.ptr, chunk_spmv_.ptr, tickets_.ptr + 1, s,
+  launch_spmv(a, din.ptr, dout.ptr, chunk_spmv_.ptr, tickets_.ptr + 1, product_error(), s,
               op == 0 ? grid_csr_ : grid_csc_);
   SGB_CUDA(cudaGetLastError());
   if (out_len > 0) {
     SGB_CUDA(cudaMemcpyAsync(out, dout.ptr, out_len * sizeof(double), cudaMemcpyDeviceToHost, s));
   }
-  SGB_CUDA(cudaStreamSynchronize(s));
+  check_product_error();
+}
+
+// The error word of the tile products (k_spmv), read at a synchronising point: it waits for
+// the stream, and a product whose bounded wait gave up since the last check makes the call
+// fail with a device error (the word is cleared for the next one).
+void Engine::check_product_error() {
+  unsigned int word = 0;
+  SGB_CUDA(cudaMemcpyAsync(&word, product_error(), sizeof(word), cudaMemcpyDeviceToHost,
+                           stream_));
+  SGB_CUDA(cudaStreamSynchronize(stream_));
+  if (product_error_status(word) != SANKHYA_GB300_OK) {
+    SGB_CUDA(cudaMemsetAsync(product_error(), 0, sizeof(word), stream_));
+    SGB_CUDA(cudaStreamSynchronize(stream_));
+    throw EngineError{product_error_status(word), "a sparse product's tile copy did not complete "
+                                                  "in time; its result was not used"};
+  }
+}
+
+int product_error_status(unsigned int word) {
+  return word == 0 ? SANKHYA_GB300_OK : SANKHYA_GB300_ERROR_DEVICE;
 }
 
 static_assert(kNoAllocMaxChunks == SANKHYA_GB300_NOALLOC_MAX_CHUNKS,
@@ -885,9 +1006,10 @@ void Engine::spmv_noalloc(int op, int scaled, const double* in, double* out,
   cudaStream_t s = stream != nullptr ? stream : stream_;
   double* chunks = nullptr;
   unsigned int* ticket = nullptr;
-  SGB_CUDA(noalloc_scratch(device_, s, &chunks, &ticket));
+  unsigned int* error = nullptr;
+  SGB_CUDA(noalloc_scratch(device_, s, &chunks, &ticket, &error));
   if (!scaled) a.val = op == 0 ? csr_raw_.ptr : csc_raw_.ptr;
-  launch_spmv(a, in, out, chunks, ticket, s, op == 0 ? grid_csr_ : grid_csc_);
+  launch_spmv(a, in, out, chunks, ticket, error, s, op == 0 ? grid_csr_ : grid_csc_);
   SGB_CUDA(cudaGetLastError());
 }
 
@@ -1137,6 +1259,7 @@ void Engine::solve_mixed(const sankhya_gb300_params& p, sankhya_gb300_result* r,
   launch_to_float(csr_s_.ptr, csr_f_.ptr, nnz_, s);
   launch_to_float(cs_.ptr, csf_.ptr, n_, s);
   extra_launches_ += 3;
+  fill_split_values();
   launch_project_start(n_, ls_.ptr, us_.ptr, anchor_x_.ptr, s);
   launch_fill(anchor_y_.ptr, m_, 0.0, s);
   extra_launches_ += 2;
@@ -1240,13 +1363,15 @@ void Engine::solve_mixed(const sankhya_gb300_params& p, sankhya_gb300_result* r,
   };
   for (;; ++rounds) {
     // Anchor residuals in FP64, then the scales of this round's correction problem.
-    launch_spmv(step_.csr, anchor_x_.ptr, ax64_.ptr, chunk_spmv_.ptr, tickets_.ptr + 1, s, grid_csr_);
-    launch_spmv(step_.csc, anchor_y_.ptr, aty64_.ptr, chunk_spmv_.ptr, tickets_.ptr + 1, s, grid_csc_);
+    launch_spmv(step_.csr, anchor_x_.ptr, ax64_.ptr, chunk_spmv_.ptr, tickets_.ptr + 1,
+                product_error(), s, grid_csr_);
+    launch_spmv(step_.csc, anchor_y_.ptr, aty64_.ptr, chunk_spmv_.ptr, tickets_.ptr + 1,
+                product_error(), s, grid_csc_);
     launch_round_measure(rb, s);
     extra_launches_ += 3;
     double out[3];
     SGB_CUDA(cudaMemcpyAsync(out, rb.out, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
-    SGB_CUDA(cudaStreamSynchronize(s));
+    check_product_error();
     // 1 / residual, never below 1, at most 1e3 times the previous scale and 1e15 overall: an
     // anchor whose residual is exactly zero must not push the FP32 data out of range.
     const auto scale = [&](double residual, double prev) {
@@ -1331,8 +1456,8 @@ void Engine::solve_mixed(const sankhya_gb300_params& p, sankhya_gb300_result* r,
   launches_ = launches_setup + extra_launches_ +
               graphs_launched_ * graph_kernel_launches(mgraph_steps_);
   r->kernel_launches = launches_;
-  r->staged_fraction[0] = step_csc_f_.staged;
-  r->staged_fraction[1] = step_csr_f_.staged;
+  r->staged_fraction[0] = ck_csc_f_.staged;
+  r->staged_fraction[1] = ck_csr_f_.staged;
   r->iterations = total_it;
   r->attempts = total_att;
   r->restarts = restarts;

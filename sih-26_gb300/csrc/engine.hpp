@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 
+#include "chunks.cuh"
 #include "kernels.cuh"
 #include "mixed.cuh"
 #include "sankhya_gb300.h"
@@ -82,6 +83,9 @@ class Engine {
   void run_graphs(const sankhya_gb300_params& p, double t0, cudaGraphExec_t* graphs,
                   Ctl* snapshot, bool forward_log, long long iteration_offset, int* stop_status);
   void final_evaluation();
+  // The tile products' error word (tickets_ slot 3, zero after load) and its check.
+  unsigned int* product_error() const { return tickets_.ptr + 3; }
+  void check_product_error();
   void setup(const sankhya_gb300_params& p, sankhya_gb300_result* r, double* norm);
   void solve_fp64(const sankhya_gb300_params& p, sankhya_gb300_result* r, double t0);
   void solve_mixed(const sankhya_gb300_params& p, sankhya_gb300_result* r, double t0);
@@ -105,14 +109,15 @@ class Engine {
   int nchunks_csr_ = 0, nchunks_csc_ = 0;
   int lanes_csr_ = 1, lanes_csc_ = 1;
   int grid_csr_ = 1, grid_csc_ = 1;
-  // The FP32 kernels' tile layout (same chunks of long rows, `lanes` threads per row).
+  // The FP32 evaluation kernels' tile layout (same chunks of long rows, `lanes` threads per
+  // row).
   int ntiles_csr_f_ = 0, ntiles_csc_f_ = 0;
   int lanes_csr_f_ = 1, lanes_csc_f_ = 1;
   int grid_csr_f_ = 1, grid_csc_f_ = 1;
   DeviceArray<Tile> csc_tiles_f_, csr_tiles_f_;
-  // The step passes' gathered-vector windows per layout (FP64 CSC / CSR, FP32 CSC / CSR):
-  // tile -> window id, the {lo, len} list, the capacity, and the grid and dynamic shared
-  // memory of the step kernel that stages them.
+  // The FP64 step passes' gathered-vector windows per layout (CSC / CSR): tile -> window
+  // id, the {lo, len} list, the capacity, and the grid and dynamic shared memory of the step
+  // kernel that stages them.
   struct StepLayout {
     DeviceArray<int> tile_win;
     DeviceArray<int2> windows;
@@ -122,7 +127,32 @@ class Engine {
     int smem = 0;
     double staged = 0.0;  // share of the nonzeros gathered from a staged window
   };
-  StepLayout step_csc_, step_csr_, step_csc_f_, step_csr_f_;
+  StepLayout step_csc_, step_csr_;
+  // The FP32 step passes' chunk layouts (chunks.cuh): CSC (column pass) and CSR (row pass).
+  // A split layout owns its main and outer index arrays (and the maps from their entries to
+  // the full layout's, through which each solve fills their values); otherwise it reads the
+  // full layout's arrays.
+  struct ChunkDev {
+    DeviceArray<Tile> chunks;
+    DeviceArray<int2> orounds;
+    DeviceArray<LongRow> longs;
+    DeviceArray<ChunkSeg> segs;
+    DeviceArray<int> seg_start, oround_start;
+    DeviceArray<int> ptr, idx, map, optr, oidx, omap;
+    DeviceArray<float> fval, foval, fouter;
+    DeviceArray<double> pieces;  // piece partials (NP per piece)
+    int nlong = 0, npieces = 0, wmax = 0, grid = 1, smem = 0, nrows = 0;
+    bool split = false;
+    long long nmain = 0, nouter = 0;
+    double staged = 0.0;    // share of the nonzeros gathered from a staged window
+    double coverage = 0.0;  // share the windows would hold over the whole layout
+  };
+  ChunkDev ck_csc_f_, ck_csr_f_;
+  void plan_layout(ChunkDev& D, const std::vector<int>& ptr, const int* idx, int lines,
+                   int extent, int pass, int window_cap);
+  void fill_split_values();
+  ChunkSet<float> chunk_set(const ChunkDev& D, const int* full_ptr, const int* full_idx,
+                            const float* full_val) const;
 
   // Pattern (shared by scaled and unscaled values).
   DeviceArray<int> csc_ptr_, csc_idx_, csr_ptr_, csr_idx_;
@@ -176,6 +206,30 @@ class Engine {
 };
 
 size_t estimate_memory(long long rows, long long cols, long long nnz, int precision);
+
+// The step passes' chunk layout of one matrix layout (layout.cu): `ptr` / `idx` its lines
+// and indices over a gathered vector of `extent` elements, `cap` entries per chunk, `wmax`
+// the window capacity, `grid` blocks, `elem_bytes` the gathered element's size. Windows are
+// kept over every entry when they hold at least `full_min` of them; between `split_min` and
+// that, the layout is split into main and outer parts; below it, nothing is staged. A split
+// layout's outer entries are summed in rounds of at most `outer_round_cap` entries.
+struct ChunkPlan {
+  int cap = 0, grid = 1, wmax = 0, npieces = 0;
+  bool split = false, error = false;
+  double coverage = 0.0, staged = 0.0;
+  std::vector<Tile> chunks;
+  std::vector<int2> orounds;
+  std::vector<LongRow> longs;
+  std::vector<ChunkSeg> segs;
+  std::vector<int> seg_start, oround_start;
+  std::vector<int> ptr, idx, map, optr, oidx, omap;  // split layouts only
+};
+ChunkPlan plan_chunks(const std::vector<int>& ptr, const int* idx, int lines, int extent, int cap,
+                      int wmax, int grid, int elem_bytes, double split_min, double full_min,
+                      int outer_round_cap);
+
+// The status a tile product's error word maps to: 0 = ok, otherwise a device error.
+int product_error_status(unsigned int word);
 
 // Throws EngineError (ARGUMENT / MODEL) when an LP is malformed.
 void validate_lp(const sankhya_gb300_lp& lp);

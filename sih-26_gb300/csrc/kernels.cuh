@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "chunks.cuh"
 #include "tiles.cuh"
 
 namespace sgb {
@@ -166,17 +167,20 @@ void launch_scale_vectors(int m, int n, const double* cost, const double* l, con
                           const double* rl, const double* ru, const double* dr, const double* dc,
                           double* cs, double* ls, double* us, double* rls, double* rus,
                           cudaStream_t s);
-// y = A x with the tile kernel (CSR gives A x; CSC gives A^T x). chunk holds a.nchunks
-// doubles; ticket is one device counter that is zero on entry and on exit.
 // Fixed device scratch of the allocation-free product: chunk partials for at most
-// kNoAllocMaxChunks chunk tiles and its completion counter. Set up once per device (the
-// symbol addresses, and the counter cleared to zero) under a lock; later calls only read the
-// cached addresses.
+// kNoAllocMaxChunks chunk tiles, its completion counter and its error word. Set up once per
+// device (the symbol addresses, and the counter and error word cleared to zero) under a
+// lock; later calls only read the cached addresses.
 constexpr int kNoAllocMaxChunks = 16384;
-cudaError_t noalloc_scratch(int device, cudaStream_t s, double** chunks, unsigned int** ticket);
+cudaError_t noalloc_scratch(int device, cudaStream_t s, double** chunks, unsigned int** ticket,
+                            unsigned int** error);
 
+// y = A x with the tile kernel (CSR gives A x; CSC gives A^T x). chunk holds a.nchunks
+// doubles; ticket is one device counter that is zero on entry and on exit. A bounded wait
+// that gives up sets *error (which the caller clears and reads) and leaves NaN in the rows
+// the product could not finish.
 void launch_spmv(TileSet<double> a, const double* x, double* y, double* chunk,
-                 unsigned int* ticket, cudaStream_t s, int grid);
+                 unsigned int* ticket, unsigned int* error, cudaStream_t s, int grid);
 // out[0] = sum v^2, deterministic; part holds grid doubles.
 void launch_sumsq(const double* v, int count, double* part, double* out, unsigned int* ticket,
                   cudaStream_t s, int grid);
@@ -194,7 +198,11 @@ int tile_blocks_per_sm();
 int fp64_window_capacity(int pass);
 int fp64_step_smem(int pass, int wmax);
 int fp64_step_blocks_per_sm(int pass, int smem);
-// Sets the dynamic shared-memory limit of the tile kernels once per process.
-void configure_tile_kernels();
+// Sets the dynamic shared-memory limits of the FP64 kernels on the current device (once per
+// device); false if the device refused.
+bool configure_tile_kernels();
+// Fills dst[k] = src[map[k]] in FP32 (the values of a split layout's part), k < count.
+void launch_gather_values(const double* src, const int* map, float* dst, long long count,
+                          cudaStream_t s);
 
 }  // namespace sgb

@@ -29,7 +29,8 @@ namespace sgb {
 
 struct MixedBuffers {
   Ctl* ctl;                  // the inner loop's control block
-  TileSet<float> csc, csr;   // scaled values in FP32
+  TileSet<float> csc, csr;   // scaled values in FP32 (evaluation tile layouts)
+  ChunkSet<float> csc_k, csr_k;  // the step passes' chunk layouts
   float* u[2];
   float* v[2];
   float* u_sum;
@@ -51,15 +52,15 @@ struct MixedBuffers {
   float* v_best;
   double* part_primal;   // [grid_primal]
   double* part_dual;     // [grid_dual * 2]
-  double* chunk_primal;  // [csc.nchunks]
-  double* chunk_dual;    // [csr.nchunks * 2]
+  double* piece_primal;  // [csc_k.npieces]
+  double* piece_dual;    // [csr_k.npieces]
   double* part_rows0;    // [grid_dual * kEvalRowSlots]
   double* part_cols;     // [(grid_primal + 1) * kEvalColSlots]
   double* part_rows1;    // [grid_dual * kEvalRowSlots]
   double* chunk_cols;    // [csc.nchunks * 2]
   double* chunk_rows;    // [csr.nchunks * 2]
   int grid_primal, grid_dual;     // evaluation passes
-  int grid_step_primal, grid_step_dual;  // step passes (one block per SM when staging)
+  int grid_step_primal, grid_step_dual;  // step passes (one block of kChunkThreads per SM)
   int smem_primal, smem_dual;     // step passes' dynamic shared memory
   int m, n;
 };
@@ -95,13 +96,14 @@ void launch_round_build(const RoundBuffers& r, cudaStream_t s);
 void launch_round_update(const RoundBuffers& r, cudaStream_t s);
 void launch_to_float(const double* src, float* dst, long long count, cudaStream_t s);
 void launch_fill_float(float* v, int count, float value, cudaStream_t s);
-void configure_mixed_kernels();
-// Resident FP32 tile blocks per SM (occupancy query).
+// Sets the dynamic shared-memory limits of the FP32 kernels on the current device (once per
+// device); false if the device refused.
+bool configure_mixed_kernels();
+// Resident FP32 evaluation tile blocks per SM (occupancy query).
 int mixed_blocks_per_sm();
-// The FP32 step passes (pass 0 = column pass, 1 = row pass): window capacity, dynamic shared
-// memory for a window of `wmax` elements, and blocks per SM with it.
+// The FP32 step passes (pass 0 = column pass, 1 = row pass): window capacity and dynamic
+// shared memory for a window of `wmax` elements (one block of kChunkThreads per SM).
 int mixed_window_capacity(int pass);
 int mixed_step_smem(int pass, int wmax);
-int mixed_step_blocks_per_sm(int pass, int smem);
 
 }  // namespace sgb

@@ -16,20 +16,22 @@
 #include "mixed.cuh"
 #include "tiles.cuh"
 
+#include <algorithm>
+#include <mutex>
+
 namespace sgb {
 
 namespace {
 
 constexpr int kScratch = 16 * (kWideBlockThreads / 32);
-// The FP32 tile blocks run 16 consumer warps (the FP32 layouts' lanes are chosen for them).
+constexpr int kChunkScratch = 2 * (kChunkThreads / 32);
+// The FP32 evaluation tile blocks run 16 consumer warps (the FP32 layouts' lanes are chosen
+// for them).
 using EvalPipeF = TilePipe<float, 2, 0, kWideThreads>;
 constexpr int kSmemF = EvalPipeF::bytes();
-// The step passes keep two tiles in flight beside the staged window; each tile brings its
-// rows' operands: u, cf, lf, uf, u_sum (column pass) and v, gu, gl, yhat, v_sum, A u (row
-// pass).
-constexpr int kStepStagesF = 3;
-using PrimalPipeF = TilePipe<float, kStepStagesF, 5, kWideThreads>;
-using DualPipeF = TilePipe<float, kStepStagesF, 6, kWideThreads>;
+// The step passes' chunk geometry: 256 entries per chunk, one gathered float per entry (v in
+// the column pass, du in the row pass).
+using StepSmemF = ChunkSmem<float, float, 1, kChunkCapF>;
 
 __device__ __forceinline__ void raise_error(Ctl* c) {
   c->error = 1;
@@ -41,50 +43,52 @@ __device__ __forceinline__ int grid_stride_begin() {
 }
 
 // ---- Inner step ----------------------------------------------------------------------------
-__global__ void __launch_bounds__(kWideBlockThreads) k_primal_f(MixedBuffers b) {
+__global__ void __launch_bounds__(kChunkThreads, 1) k_primal_f(MixedBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
-  __shared__ double scratch[kScratch];
+  __shared__ double scratch[kChunkScratch];
   Ctl* ctl = b.ctl;
-  if (ctl->done != kRunning || ctl->eval_now != 0) return;
-  if (ctl->iteration >= ctl->iteration_limit) {
+  // Every control field the pass reads, loaded together before the first test.
+  const int done = ctl->done, eval_now = ctl->eval_now, cur = ctl->cur;
+  const bool add = ctl->pending_add != 0;
+  const long long iteration = ctl->iteration, limit = ctl->iteration_limit;
+  const double omega = ctl->omega, eta = ctl->eta;
+  if (done != kRunning || eval_now != 0) return;
+  if (iteration >= limit) {
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->done = kIterationLimit;
     return;
   }
-  const int cur = ctl->cur;
+  const float* __restrict__ u = b.u[cur];
   float* __restrict__ un = b.u[cur ^ 1];
   const float* __restrict__ v = b.v[cur];
-  const double omega = ctl->omega;
-  const float tau = static_cast<float>(ctl->eta / omega);
-  const bool add = ctl->pending_add != 0;
+  const float tau = static_cast<float>(eta / omega);
   float mvf = 0.0f;
-  PrimalPipeF pipe;
-  pipe.setup(dsmem);
-  pipe.rsrc[0] = b.u[cur];
-  pipe.rsrc[1] = b.cf;
-  pipe.rsrc[2] = b.lf;
-  pipe.rsrc[3] = b.uf;
-  pipe.rsrc[4] = b.u_sum;
-  Window<float> win;
-  win.setup(v, pipe, dsmem);
-  auto gather = [&](int row, float a, float* acc) { acc[0] = fmaf(a, win.get(row), acc[0]); };
-  auto epi = [&](int j, const float* s) {
-    const float uj = pipe.row(0, j);
-    if (add) b.u_sum[j] = pipe.row(4, j) + uj;
-    const float g = pipe.row(1, j) + s[0];
-    const float unj = clamp_box(fmaf(-tau, g, uj), pipe.row(2, j), pipe.row(3, j));
+  // Operands of column j: u, cf, lf, uf and (when the last step is still to be added) u_sum.
+  auto load = [&](int j, float* o) {
+    o[0] = u[j];
+    o[1] = b.cf[j];
+    o[2] = b.lf[j];
+    o[3] = b.uf[j];
+    o[4] = add ? b.u_sum[j] : 0.0f;
+  };
+  auto epi = [&](int j, const float* s, const float* o) {
+    const float uj = o[0];
+    if (add) b.u_sum[j] = o[4] + uj;
+    const float g = o[1] + s[0];
+    const float unj = clamp_box(fmaf(-tau, g, uj), o[2], o[3]);
     un[j] = unj;
     const float d = unj - uj;
     b.du[j] = d;
     mvf = fmaf(d, d, mvf);
   };
-  if (!run_tiles<1, float>(pipe, b.csc, win, b.chunk_primal, gather, epi) &&
+  if (!run_chunks<1, 5, float, float, kChunkCapF>(b.csc_k, v, dsmem, b.piece_primal, load,
+                                                  epi) &&
       threadIdx.x == 0) {
     raise_error(ctl);
   }
   double mv[1] = {static_cast<double>(mvf)};
   if (!arrive_last<1>(mv, scratch, b.part_primal, &ctl->ticket[kTicketPrimal])) return;
   mvf = 0.0f;
-  run_long_rows<1, float>(b.csc, b.chunk_primal, epi);
+  run_chunk_long_rows<1, 5, float>(b.csc_k, b.piece_primal, load, epi);
   mv[0] = static_cast<double>(mvf);
   double longs[1], total[1];
   block_sum<1>(mv, scratch, longs);
@@ -95,43 +99,43 @@ __global__ void __launch_bounds__(kWideBlockThreads) k_primal_f(MixedBuffers b) 
   }
 }
 
-__global__ void __launch_bounds__(kWideBlockThreads) k_dual_f(MixedBuffers b) {
+__global__ void __launch_bounds__(kChunkThreads, 1) k_dual_f(MixedBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
-  __shared__ double scratch[kScratch];
+  __shared__ double scratch[kChunkScratch];
   Ctl* ctl = b.ctl;
-  if (ctl->done != kRunning || ctl->eval_now != 0) return;
-  const int cur = ctl->cur;
-  float* __restrict__ vn = b.v[cur ^ 1];
-  float* __restrict__ aun = b.au[cur ^ 1];
-  const double omega = ctl->omega;
-  const float sigma = static_cast<float>(ctl->eta * omega);
-  const float inv_sigma = 1.0f / sigma;
+  const int done = ctl->done, eval_now = ctl->eval_now, cur = ctl->cur;
   const bool add = ctl->pending_add != 0;
+  const double omega = ctl->omega, eta = ctl->eta;
+  if (done != kRunning || eval_now != 0) return;
+  const float* __restrict__ v = b.v[cur];
+  float* __restrict__ vn = b.v[cur ^ 1];
+  const float* __restrict__ au = b.au[cur];
+  float* __restrict__ aun = b.au[cur ^ 1];
+  const float sigma = static_cast<float>(eta * omega);
+  const float inv_sigma = 1.0f / sigma;
   float a0 = 0.0f, a1 = 0.0f;  // sum dv^2, sum dv (A du)
-  DualPipeF pipe;
-  pipe.setup(dsmem);
-  pipe.rsrc[0] = b.v[cur];
-  pipe.rsrc[1] = b.gu;
-  pipe.rsrc[2] = b.gl;
-  pipe.rsrc[3] = b.yhat;
-  pipe.rsrc[4] = b.v_sum;
-  pipe.rsrc[5] = b.au[cur];
-  Window<float> win;
-  win.setup(b.du, pipe, dsmem);
-  auto gather = [&](int col, float a, float* acc) { acc[0] = fmaf(a, win.get(col), acc[0]); };
-  auto epi = [&](int i, const float* s) {
-    const float vi = pipe.row(0, i);
-    if (add) b.v_sum[i] = pipe.row(4, i) + vi;
-    const float gu = pipe.row(1, i), gl = pipe.row(2, i);
-    const float au = pipe.row(5, i);
+  // Operands of row i: v, gu, gl, yhat, A u and (when the last step is still to be added)
+  // v_sum.
+  auto load = [&](int i, float* o) {
+    o[0] = v[i];
+    o[1] = b.gu[i];
+    o[2] = b.gl[i];
+    o[3] = b.yhat[i];
+    o[4] = au[i];
+    o[5] = add ? b.v_sum[i] : 0.0f;
+  };
+  auto epi = [&](int i, const float* s, const float* o) {
+    const float vi = o[0];
+    if (add) b.v_sum[i] = o[5] + vi;
+    const float gu = o[1], gl = o[2];
     const float adu = s[0];
-    aun[i] = au + adu;
-    const float abar = fmaf(2.0f, adu, au);  // A ubar
+    aun[i] = o[4] + adu;
+    const float abar = fmaf(2.0f, adu, o[4]);  // A ubar
     float vni;
     if (gu == gl) {
       vni = fmaf(sigma, gu + abar, vi);
     } else {
-      const float yhat = pipe.row(3, i);
+      const float yhat = o[3];
       const float t = fmaf(yhat + vi, inv_sigma, abar);
       if (t + gu > 0.0f) {
         vni = fmaf(sigma, gu + abar, vi);
@@ -146,14 +150,15 @@ __global__ void __launch_bounds__(kWideBlockThreads) k_dual_f(MixedBuffers b) {
     a0 = fmaf(d, d, a0);
     a1 = fmaf(d, adu, a1);
   };
-  if (!run_tiles<1, float>(pipe, b.csr, win, b.chunk_dual, gather, epi) &&
+  if (!run_chunks<1, 6, float, float, kChunkCapF>(b.csr_k, b.du, dsmem, b.piece_dual, load,
+                                                  epi) &&
       threadIdx.x == 0) {
     raise_error(ctl);
   }
   double acc2[2] = {static_cast<double>(a0), static_cast<double>(a1)};
   if (!arrive_last<2>(acc2, scratch, b.part_dual, &ctl->ticket[kTicketDual])) return;
   a0 = a1 = 0.0f;
-  run_long_rows<1, float>(b.csr, b.chunk_dual, epi);
+  run_chunk_long_rows<1, 6, float>(b.csr_k, b.piece_dual, load, epi);
   acc2[0] = a0;
   acc2[1] = a1;
   double longs[2], total[2];
@@ -505,73 +510,96 @@ __global__ void k_fill_float(float* v, int count, float value) {
   for (int k = grid_stride_begin(); k < count; k += gridDim.x * blockDim.x) v[k] = value;
 }
 
-int g_sms = 0;
 int egrid(long long count) {
-  if (g_sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    sms = 1;
   }
   long long blocks = (count + 255) / 256;
-  const long long cap = static_cast<long long>(g_sms) * 8;
+  const long long cap = static_cast<long long>(sms) * 8;
   if (blocks > cap) blocks = cap;
   return blocks < 1 ? 1 : static_cast<int>(blocks);
 }
 
+// Per-device state: whether the kernels' shared-memory limits are set on the device, and
+// the evaluation kernels' occupancy there.
+constexpr int kMaxDevices = 64;
+struct MixedConfig {
+  bool configured;
+  int per_sm;
+};
+std::mutex g_mixed_mutex;
+MixedConfig g_mixed[kMaxDevices];
+
 }  // namespace
 
-void configure_mixed_kernels() {
-  static bool done = false;
-  if (done) return;
-  cudaFuncSetAttribute(k_primal_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       max_dynamic_smem(reinterpret_cast<const void*>(k_primal_f)));
-  cudaFuncSetAttribute(k_dual_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       max_dynamic_smem(reinterpret_cast<const void*>(k_dual_f)));
-  cudaFuncSetAttribute(k_evalf_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemF);
-  cudaFuncSetAttribute(k_evalf_rows1, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemF);
-  done = true;
+bool configure_mixed_kernels() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return false;
+  }
+  std::lock_guard<std::mutex> lock(g_mixed_mutex);
+  MixedConfig& c = g_mixed[dev];
+  if (c.configured) return true;
+  const cudaError_t errs[] = {
+      cudaFuncSetAttribute(k_primal_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           max_dynamic_smem(reinterpret_cast<const void*>(k_primal_f))),
+      cudaFuncSetAttribute(k_dual_f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           max_dynamic_smem(reinterpret_cast<const void*>(k_dual_f))),
+      cudaFuncSetAttribute(k_evalf_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemF),
+      cudaFuncSetAttribute(k_evalf_rows1, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemF)};
+  for (cudaError_t e : errs) {
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+  }
+  int a = 0, b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_evalf_rows1, kWideBlockThreads,
+                                                    kSmemF) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_evalf_cols, kWideBlockThreads,
+                                                    kSmemF) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  c.per_sm = std::max(1, std::min(a, b));
+  c.configured = true;
+  return true;
 }
 
 int mixed_blocks_per_sm() {
-  static int per_sm = 0;
-  if (per_sm == 0) {
-    configure_mixed_kernels();
-    int a = 0, b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k_evalf_rows1, kWideBlockThreads, kSmemF);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_evalf_cols, kWideBlockThreads, kSmemF);
-    per_sm = a < b ? a : b;
-    if (per_sm <= 0) per_sm = 1;
-  }
-  return per_sm;
+  if (!configure_mixed_kernels()) return 1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(g_mixed_mutex);
+  return g_mixed[dev].per_sm > 0 ? g_mixed[dev].per_sm : 1;
 }
 
+// The window a block of kChunkThreads stages: what is left beside its warp buffers, at most
+// kWindowBytesMax, in gathered floats (a multiple of 1024).
 int mixed_window_capacity(int pass) {
   configure_mixed_kernels();
-  return pass == 0 ? window_capacity(reinterpret_cast<const void*>(k_primal_f),
-                                     PrimalPipeF::bytes(), sizeof(float))
-                   : window_capacity(reinterpret_cast<const void*>(k_dual_f),
-                                     DualPipeF::bytes(), sizeof(float));
+  const void* k = pass == 0 ? reinterpret_cast<const void*>(k_primal_f)
+                            : reinterpret_cast<const void*>(k_dual_f);
+  const int budget =
+      std::min(max_dynamic_smem(k) - StepSmemF::bytes(kChunkThreads / 32, 0), kWindowBytesMax);
+  return budget > 0 ? (budget / static_cast<int>(sizeof(float))) & ~1023 : 0;
 }
 
 int mixed_step_smem(int pass, int wmax) {
-  return (pass == 0 ? PrimalPipeF::bytes() : DualPipeF::bytes()) +
-         window_bytes(wmax, sizeof(float));
-}
-
-int mixed_step_blocks_per_sm(int pass, int smem) {
-  configure_mixed_kernels();
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, pass == 0 ? k_primal_f : k_dual_f, kWideBlockThreads, static_cast<size_t>(smem));
-  return per_sm > 0 ? per_sm : 1;
+  (void)pass;
+  return StepSmemF::bytes(kChunkThreads / 32, wmax);
 }
 
 void launch_mixed_primal(const MixedBuffers& b, cudaStream_t s) {
-  k_primal_f<<<b.grid_step_primal, kWideBlockThreads, b.smem_primal, s>>>(b);
+  k_primal_f<<<b.grid_step_primal, kChunkThreads, b.smem_primal, s>>>(b);
 }
 
 void launch_mixed_dual(const MixedBuffers& b, cudaStream_t s) {
-  k_dual_f<<<b.grid_step_dual, kWideBlockThreads, b.smem_dual, s>>>(b);
+  k_dual_f<<<b.grid_step_dual, kChunkThreads, b.smem_dual, s>>>(b);
 }
 
 void launch_mixed_step(const MixedBuffers& b, cudaStream_t s) {

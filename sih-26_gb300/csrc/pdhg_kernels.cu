@@ -1,6 +1,8 @@
 // pdhg_kernels.cu -- the FP64 hot path of the GB300 PDHG engine.
 //
-// Per attempted step (src/pdhg/pdhg.cpp:220-335) there are TWO kernels:
+// Per attempted step (src/pdhg/pdhg.cpp:220-335) there are TWO kernels, both on the tile
+// engine of tiles.cuh (the FP32 method's step kernels run on the warp chunks of chunks.cuh
+// instead; on GB300's FP64 pipe these tile kernels measured faster than chunk versions):
 //   k_primal  one pass over the CSC copy of Ahat: A^T y gathered per column, fused with the
 //             projected primal update x' = proj(x - tau (c + A^T y)), xbar = 2x' - x and
 //             dx = x' - x (written once per column so the row pass needs one FMA per entry
@@ -22,6 +24,7 @@
 #include "kernels.cuh"
 #include "tiles.cuh"
 
+#include <algorithm>
 #include <cstdio>
 #include <mutex>
 
@@ -30,8 +33,6 @@ namespace sgb {
 namespace {
 
 long long g_launches = 0;
-int g_tile_blocks_per_sm = 0;
-int g_num_sms = 0;
 
 constexpr int kScratch = 16 * (kBlockThreads / 32);
 // The step passes keep one tile in flight beside the staged window (a larger window pays
@@ -40,6 +41,41 @@ constexpr int kScratch = 16 * (kBlockThreads / 32);
 constexpr int kStepStages = 2;
 using PrimalPipe = TilePipe<double, kStepStages, 5>;
 using DualPipe = TilePipe<double, kStepStages, 4>;
+
+// Per-device state: whether the kernels' shared-memory limits are set on the device, and
+// its occupancy and SM count (an engine on device 1 needs its own opt-in).
+constexpr int kMaxDevices = 64;
+struct DeviceConfig {
+  bool configured;
+  int tile_blocks_per_sm;
+  int sms;
+};
+std::mutex g_config_mutex;
+DeviceConfig g_config[kMaxDevices];
+
+int current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
+  }
+  return dev >= 0 && dev < kMaxDevices ? dev : -1;
+}
+
+int device_sms() {
+  const int dev = current_device();
+  if (dev < 0) return 1;
+  std::lock_guard<std::mutex> lock(g_config_mutex);
+  if (g_config[dev].sms == 0) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+      cudaGetLastError();
+      sms = 1;
+    }
+    g_config[dev].sms = sms > 0 ? sms : 1;
+  }
+  return g_config[dev].sms;
+}
 
 __device__ __forceinline__ void raise_error(Ctl* c) {
   c->error = 1;
@@ -519,17 +555,33 @@ __global__ void k_scale_vectors(int m, int n, const double* cost, const double* 
   }
 }
 
-// y = A x with products summed in ascending index order per row.
+// y = A x with products summed in ascending index order per row. A block whose bounded wait
+// gives up (a tile copy that never lands) sets *error and writes NaN to every row of its tile
+// range and to the partials of its chunk tiles (so a long row it took part in sums to NaN):
+// a product that could not be finished is never left looking like a result.
 __global__ void __launch_bounds__(kBlockThreads) k_spmv(TileSet<double> a, const double* x,
                                                        double* y, double* chunk,
-                                                       unsigned int* ticket) {
+                                                       unsigned int* ticket,
+                                                       unsigned int* error) {
   extern __shared__ __align__(16) unsigned char dsmem[];
-  __shared__ double scratch[kScratch];
   auto gather = [&](int col, double v, double* acc) { acc[0] = fma(v, __ldg(x + col), acc[0]); };
   auto epi = [&](int r, const double* s) { y[r] = 0.0 + s[0]; };
   TilePipe<double> pipe;
   pipe.setup(dsmem);
-  run_tiles<1, double>(pipe, a, chunk, gather, epi);
+  if (!run_tiles<1, double>(pipe, a, chunk, gather, epi)) {
+    int first, last;
+    block_tile_range(a.ntiles, first, last);
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    for (int t = first; t < last; ++t) {
+      const Tile tl = a.tiles[t];
+      if (tl.r1 < 0) {
+        if (threadIdx.x == 0) chunk[-tl.r1 - 1] = nan;
+      } else {
+        for (int r = tl.r0 + static_cast<int>(threadIdx.x); r < tl.r1; r += blockDim.x) y[r] = nan;
+      }
+    }
+    if (threadIdx.x == 0) atomicExch(error, 1u);
+  }
   if (a.nlong == 0) return;
   __shared__ int s_last;
   if (threadIdx.x == 0) {
@@ -624,42 +676,60 @@ __global__ void k_fill(double* v, int count, double value) {
 }
 
 int elementwise_grid(int count) {
-  if (g_num_sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-  }
   int blocks = (count + 255) / 256;
-  const int cap = g_num_sms * 8;
+  const int cap = device_sms() * 8;
   if (blocks > cap) blocks = cap;
   return blocks < 1 ? 1 : blocks;
 }
 
 constexpr int kTileSmem = TilePipe<double>::bytes();
 
+__global__ void k_gather_values(const double* __restrict__ src, const int* __restrict__ map,
+                                float* __restrict__ dst, long long count) {
+  for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < count;
+       k += static_cast<long long>(gridDim.x) * blockDim.x) {
+    dst[k] = static_cast<float>(src[map[k]]);
+  }
+}
+
 }  // namespace
 
-void configure_tile_kernels() {
-  static bool done = false;
-  if (done) return;
-  cudaFuncSetAttribute(k_primal, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       max_dynamic_smem(reinterpret_cast<const void*>(k_primal)));
-  cudaFuncSetAttribute(k_dual, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       max_dynamic_smem(reinterpret_cast<const void*>(k_dual)));
-  cudaFuncSetAttribute(k_eval_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
-  cudaFuncSetAttribute(k_eval_rows1, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
-  cudaFuncSetAttribute(k_spmv, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem);
-  done = true;
+bool configure_tile_kernels() {
+  const int dev = current_device();
+  if (dev < 0) return false;
+  std::lock_guard<std::mutex> lock(g_config_mutex);
+  DeviceConfig& c = g_config[dev];
+  if (c.configured) return true;
+  const cudaError_t errs[] = {
+      cudaFuncSetAttribute(k_primal, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           max_dynamic_smem(reinterpret_cast<const void*>(k_primal))),
+      cudaFuncSetAttribute(k_dual, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           max_dynamic_smem(reinterpret_cast<const void*>(k_dual))),
+      cudaFuncSetAttribute(k_eval_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem),
+      cudaFuncSetAttribute(k_eval_rows1, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem),
+      cudaFuncSetAttribute(k_spmv, cudaFuncAttributeMaxDynamicSharedMemorySize, kTileSmem)};
+  for (cudaError_t e : errs) {
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval_rows1, kBlockThreads,
+                                                    kTileSmem) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  c.tile_blocks_per_sm = per_sm > 0 ? per_sm : 1;
+  c.configured = true;
+  return true;
 }
 
 int tile_blocks_per_sm() {
-  if (g_tile_blocks_per_sm == 0) {
-    configure_tile_kernels();
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_eval_rows1, kBlockThreads, kTileSmem);
-    g_tile_blocks_per_sm = per_sm > 0 ? per_sm : 1;
-  }
-  return g_tile_blocks_per_sm;
+  if (!configure_tile_kernels()) return 1;
+  const int dev = current_device();
+  std::lock_guard<std::mutex> lock(g_config_mutex);
+  return dev >= 0 ? g_config[dev].tile_blocks_per_sm : 1;
 }
 
 long long kernel_launch_count() { return g_launches; }
@@ -680,8 +750,12 @@ int fp64_step_smem(int pass, int wmax) {
 int fp64_step_blocks_per_sm(int pass, int smem) {
   configure_tile_kernels();
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, pass == 0 ? k_primal : k_dual, kBlockThreads, static_cast<size_t>(smem));
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, pass == 0 ? k_primal : k_dual, kBlockThreads, static_cast<size_t>(smem)) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
   return per_sm > 0 ? per_sm : 1;
 }
 
@@ -698,6 +772,14 @@ void launch_dual_pass(const StepBuffers& b, cudaStream_t s) {
 void launch_pdhg_step(const StepBuffers& b, cudaStream_t s) {
   launch_primal_pass(b, s);
   launch_dual_pass(b, s);
+}
+
+void launch_gather_values(const double* src, const int* map, float* dst, long long count,
+                          cudaStream_t s) {
+  if (count <= 0) return;
+  ++g_launches;
+  k_gather_values<<<elementwise_grid(static_cast<int>(std::min<long long>(count, 1 << 30))),
+                           256, 0, s>>>(src, map, dst, count);
 }
 
 void launch_evaluation(const EvalBuffers& e, cudaStream_t s) {
@@ -733,15 +815,16 @@ void launch_scale_vectors(int m, int n, const double* cost, const double* l, con
 }
 
 void launch_spmv(TileSet<double> a, const double* x, double* y, double* chunk,
-                 unsigned int* ticket, cudaStream_t s, int grid) {
+                 unsigned int* ticket, unsigned int* error, cudaStream_t s, int grid) {
   if (a.nrows == 0) return;
   ++g_launches;
-  k_spmv<<<grid, kBlockThreads, kTileSmem, s>>>(a, x, y, chunk, ticket);
+  k_spmv<<<grid, kBlockThreads, kTileSmem, s>>>(a, x, y, chunk, ticket, error);
 }
 
 namespace {
 
 // The allocation-free product's scratch: file-scope device arrays, never cudaMalloc'd.
+// g_noalloc_ticket[0] is the product's completion counter, [1] its error word.
 static __device__ __align__(256) double g_noalloc_chunks[kNoAllocMaxChunks];
 static __device__ __align__(256) unsigned int g_noalloc_ticket[4];
 
@@ -756,7 +839,8 @@ NoAllocSlot g_noalloc_slots[kNoAllocMaxDevices];
 
 }  // namespace
 
-cudaError_t noalloc_scratch(int device, cudaStream_t s, double** chunks, unsigned int** ticket) {
+cudaError_t noalloc_scratch(int device, cudaStream_t s, double** chunks, unsigned int** ticket,
+                            unsigned int** error) {
   if (device < 0 || device >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
   NoAllocSlot& slot = g_noalloc_slots[device];
@@ -770,7 +854,8 @@ cudaError_t noalloc_scratch(int device, cudaStream_t s, double** chunks, unsigne
     err = cudaGetSymbolAddress(&t, g_noalloc_ticket);
     if (err != cudaSuccess) return err;
     // The completion counter must start at zero; k_spmv's last block puts it back to zero.
-    // The chunk partials need no clearing: each is written before it is read.
+    // The error word starts at zero too. The chunk partials need no clearing: each is
+    // written before it is read.
     err = cudaMemsetAsync(t, 0, sizeof(g_noalloc_ticket), s);
     if (err != cudaSuccess) return err;
     err = cudaStreamSynchronize(s);
@@ -781,6 +866,7 @@ cudaError_t noalloc_scratch(int device, cudaStream_t s, double** chunks, unsigne
   }
   *chunks = slot.chunks;
   *ticket = slot.ticket;
+  *error = slot.ticket + 1;
   return cudaSuccess;
 }
 

@@ -20,10 +20,10 @@ from . import _paths
 
 NVCC = os.environ.get("NVCC", shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CUDA_SOURCES = ["pdhg_kernels.cu", "mixed_kernels.cu", "batch_kernels.cu", "engine.cu", "batch.cu",
-                "capi.cu"]
-HEADERS = ["common.cuh", "kernels.cuh", "tiles.cuh", "decisions.cuh", "mixed.cuh", "batch.cuh",
-           "engine.hpp", "batch_engine.hpp"]
+CUDA_SOURCES = ["pdhg_kernels.cu", "mixed_kernels.cu", "batch_kernels.cu", "engine.cu", "layout.cu",
+                "batch.cu", "capi.cu"]
+HEADERS = ["common.cuh", "kernels.cuh", "tiles.cuh", "chunks.cuh", "decisions.cuh", "mixed.cuh",
+           "batch.cuh", "engine.hpp", "batch_engine.hpp"]
 
 
 def _stale(target, sources):

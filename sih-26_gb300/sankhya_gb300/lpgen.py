@@ -41,7 +41,11 @@ def _load():
     global _lib
     if _lib is None:
         if not os.path.exists(_paths.LPGEN_LIB):
-            raise RuntimeError(f"{_paths.LPGEN_LIB} is not built; run __graft_entry__.build()")
+            # The generators are plain C and compile in a second, so a fresh checkout (or a
+            # test collection that runs before build()) builds them on first use.
+            from . import build
+
+            build.build_lpgen()
         lib = ctypes.CDLL(_paths.LPGEN_LIB)
         for name in ("lpgen_planted_uniform", "lpgen_planted_general",
                      "lpgen_planted_nondegenerate"):
