@@ -99,6 +99,9 @@ def _run(monkeypatch, argv):
     monkeypatch.setattr(bench, "BATCH_LPS", 6)
     monkeypatch.setattr(bench, "BATCH_NODES", 4)
     monkeypatch.setattr(bench, "BATCH_SEQUENTIAL_SAMPLE", (2, 1))
+    monkeypatch.setattr(bench, "ZIPF_SHAPE", (300, 600, 3000))
+    monkeypatch.setattr(bench, "REFERENCE_SAMPLE_ITERATIONS", 8)
+    monkeypatch.setattr(bench, "CPU_TIME_LIMIT", 0.5)
     full_adjoint = bench.adjoint_section
     monkeypatch.setattr(bench, "adjoint_section",
                         lambda device: full_adjoint(device, lps_count=3, shape=(60, 120),
@@ -136,6 +139,21 @@ def test_default_line(monkeypatch):
     assert "error" not in line["batched"] and "error" not in line["adjoint"]
     assert set(line["batched"]) == {"independent", "bnb_nodes"}
     assert line["adjoint"]["fd_max_rel_err"] < 1e-5
+    zipf = line["zipf"]
+    assert "error" not in zipf, zipf
+    for prec in ("mixed", "fp64"):
+        assert zipf[prec]["relative_kkt"] >= 0 and zipf[prec]["seconds"] >= 0
+    # The parity verdict and the FP64 summary close the line, where a reader that keeps only
+    # its end still sees them.
+    assert list(line)[-2:] == ["fp64", "parity"]
+    parity = line["parity"]
+    assert set(parity) >= {"mixed", "fp64", "objective_rel_diff_mixed_vs_fp64",
+                           "speedup_of_mixed", "same_answer"}
+    assert parity["same_answer"] is True
+    limited = cpu["time_limited_run"]
+    assert "error" not in limited and limited["time_limit_s"] == 0.5
+    assert cpu["extrapolated"] is True
+    assert e2e["pin_seconds"] >= 0 and e2e["value_with_pinning"] >= e2e["value"]
 
 
 def test_reference_line(monkeypatch):
@@ -145,6 +163,9 @@ def test_reference_line(monkeypatch):
     assert line["value"] > 0 and line["unit"] == "s"
     assert line["cpu_baseline"]["value"] == line["value"]
     assert line["cpu_baseline"]["host"]["machine"]
+    measured = line["cpu_baseline"]["measured"]
+    assert measured["iterations"] == 8 and measured["s_per_iteration"] > 0
+    assert line["cpu_baseline"]["extrapolated"] is True
     assert line["e2e"] == {"value": line["value"], "unit": "s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
 
