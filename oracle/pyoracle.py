@@ -18,7 +18,11 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libsankhya_ref.so")
-REFERENCE_TREE = os.environ.get("SANKHYA_REFERENCE_TREE", "/root/reference")
+# The reference checkout: SANKHYA_REFERENCE_TREE, else a `reference` directory beside this
+# checkout. Where neither exists the reference checkers are not built and their tests skip.
+REFERENCE_TREE = os.environ.get(
+    "SANKHYA_REFERENCE_TREE",
+    os.path.normpath(os.path.join(HERE, os.pardir, os.pardir, "reference")))
 
 STATUS_NAMES = {0: "not_solved", 1: "optimal", 2: "feasible", 3: "infeasible",
                 5: "iteration_limit", 6: "time_limit", 8: "numerical_error", 9: "model_error",

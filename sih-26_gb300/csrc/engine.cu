@@ -114,8 +114,10 @@ bool finite_bound_host(double v) { return !(std::isinf(v) || std::fabs(v) >= 1e3
 }  // namespace
 
 // Greedy row tiles: consecutive rows while the tile has at most min(kMaxTileRows,
-// threads / lanes) rows and at most kCap nonzeros; a row longer than kCap becomes chunk tiles of kCap entries each,
-// listed as a LongRow so its chunk partials can be combined in chunk order.
+// threads / lanes) rows and at most kCap nonzeros; a row longer than kCap becomes chunk tiles
+// of kCap entries each, listed as a LongRow so its chunk partials can be combined in chunk
+// order. With one lane per row, a row of more than kWarpRowMin entries (and at most kCap)
+// gets a tile of its own, which one warp sums (see run_tiles).
 void build_tiles(const std::vector<int>& ptr, int lines, int lanes, int threads,
                  std::vector<Tile>* tiles, std::vector<LongRow>* longs, int* nchunks) {
   tiles->clear();
@@ -139,7 +141,9 @@ void build_tiles(const std::vector<int>& ptr, int lines, int lanes, int threads,
     }
     const int begin = r;
     ++r;
-    while (r < lines && r - begin < max_rows && ptr[r + 1] - ptr[r] <= kCap &&
+    const bool warp_row = lanes == 1 && len > kWarpRowMin;
+    while (!warp_row && r < lines && r - begin < max_rows && ptr[r + 1] - ptr[r] <= kCap &&
+           (lanes != 1 || ptr[r + 1] - ptr[r] <= kWarpRowMin) &&
            ptr[r + 1] - ptr[begin] <= kCap) {
       ++r;
     }

@@ -46,6 +46,10 @@ constexpr int kBlockThreads = kTileThreads + 32;  // plus the producer warp
 constexpr int kWideThreads = 512;  // consumer threads of the FP32 tile blocks
 constexpr int kWideBlockThreads = kWideThreads + 32;
 constexpr int kMaxTileRows = 256;  // rows of a tile, whatever the block size
+// A row longer than this, in a layout of one lane per row, gets a tile of its own that one
+// consumer warp sums (a WARP ROW): one thread walking a row of hundreds or thousands of
+// dependent gathers holds up its whole block (the load-balance failure of long rows).
+constexpr int kWarpRowMin = 64;
 constexpr long long kWaitLimit = 1LL << 24;
 
 struct Tile {
@@ -487,7 +491,26 @@ __device__ __forceinline__ bool run_tiles(TilePipe<V, NB, NR, CT>& pipe, const T
       const int base = tile.k0 & ~3;
       const int* __restrict__ sidx = pipe.idx(b);
       const V* __restrict__ sval = pipe.val(b);
-      if (tile.r1 < 0) {
+      if (tile.r1 == tile.r0 + 1 && tile.k1 - tile.k0 > kWarpRowMin) {
+        // A warp row: lanes take entries l, l + 32, ... in order, a fixed xor tree adds them,
+        // and lane 0 runs the epilogue with the row's staged operands.
+        if (warp == i % (CT / 32)) {
+          if (NR > 0) {
+            pipe.cur_rows = pipe.rows(b);
+            pipe.row_base = tile.r0 & ~3;
+            pipe.rows_staged = true;
+          }
+          A acc[NP];
+#pragma unroll
+          for (int q = 0; q < NP; ++q) acc[q] = A(0);
+          for (int k = tile.k0 - base + lane; k < tile.k1 - base; k += 32) {
+            gather(sidx[k], sval[k], acc);
+          }
+#pragma unroll
+          for (int q = 0; q < NP; ++q) acc[q] = warp_sum(acc[q]);
+          if (lane == 0) epi(tile.r0, acc);
+        }
+      } else if (tile.r1 < 0) {
         if (warp == i % (CT / 32)) {
           A acc[NP];
 #pragma unroll

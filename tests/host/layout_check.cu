@@ -10,13 +10,22 @@
 //   * every window starts and ends on a 4-element bound, holds at most wmax elements, lies
 //     inside the padded gathered vector, and the staged count build_windows returns is the
 //     number of entries that fall inside their tile's window;
+//   * with one lane per row, a row of more than kWarpRowMin entries has a tile of its own;
+//   * the chunk plans of the FP32 step passes (plan_chunks): chunks cover the lines in order
+//     within kChunkRows rows and `cap` entries, long rows as pieces; every block's segments
+//     cover its chunks in order with windows on 4-element bounds inside the padded vector;
+//     a split layout's main and outer parts partition the entries, every main entry of a
+//     windowed chunk lies in its window, and the outer rounds write every row exactly once,
+//     by the block whose chunks hold it, within the staging space;
 // plus the FP32 lane rule and the step graph's launch count. Given a file, it checks the
 // layouts the engine builds for that pattern instead (read_pattern).
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <random>
 #include <vector>
 
+#include "chunks.cuh"
 #include "engine.hpp"
 #include "kernels.cuh"
 #include "tiles.cuh"
@@ -112,6 +121,9 @@ void check_tiles(const Pattern& p, int lanes, int threads, const std::vector<Til
     if (tile.k0 != p.ptr[tile.r0] || tile.k1 != p.ptr[tile.r1]) fail("tile entries do not match its rows", tile.k0, tile.k1);
     for (int r = tile.r0; r < tile.r1; ++r) {
       if (p.ptr[r + 1] - p.ptr[r] > kCap) fail("long row inside a short tile", r, p.ptr[r + 1] - p.ptr[r]);
+      if (lanes == 1 && tile.r1 - tile.r0 > 1 && p.ptr[r + 1] - p.ptr[r] > kWarpRowMin) {
+        fail("warp row shares its tile", r, p.ptr[r + 1] - p.ptr[r]);
+      }
     }
     // Row pointer and row operand copies.
     const int w0 = tile.r0 & ~3;
@@ -156,6 +168,117 @@ void check_windows(const Pattern& p, const std::vector<Tile>& tiles, int wmax) {
   if (count != covered) fail("staged count", covered, count);
 }
 
+// The chunk plan of an FP32 step pass for pattern p (see plan_chunks).
+void check_chunk_plan(const Pattern& p, int wmax, int grid, double split_min) {
+  const int cap = kChunkCapF;
+  const int round_cap = (kChunkThreads / 32) * kChunkCapF;
+  const ChunkPlan P = plan_chunks(p.ptr, p.idx.data(), p.lines, p.extent, cap, wmax, grid, 4,
+                                  split_min, 0.999, round_cap);
+  if (P.error) fail("plan_chunks reported an error", p.lines, wmax);
+  const long long nnz = p.ptr[p.lines];
+  const std::vector<int>& ptr = P.split ? P.ptr : p.ptr;
+  const std::vector<int>& idx = P.split ? P.idx : p.idx;
+  if (static_cast<int>(ptr.size()) != p.lines + 1) fail("main row pointers", static_cast<long long>(ptr.size()), p.lines);
+  // Chunks.
+  int row = 0, piece = 0;
+  size_t li = 0;
+  const long long T = static_cast<long long>(P.chunks.size());
+  for (long long c = 0; c < T; ++c) {
+    const Tile& ch = P.chunks[static_cast<size_t>(c)];
+    if (ch.k1 - ch.k0 > cap || ch.k0 > ch.k1) fail("chunk entries", ch.k0, ch.k1);
+    if (ch.r1 < 0) {
+      if (li >= P.longs.size() || P.longs[li].row != ch.r0) fail("piece without its long row", ch.r0, static_cast<long long>(li));
+      if (-ch.r1 - 1 != piece) fail("piece slot order", -ch.r1 - 1, piece);
+      if (ch.r0 != row) fail("piece row", ch.r0, row);
+      ++piece;
+      if (ch.k1 == ptr[static_cast<size_t>(row) + 1]) {
+        if (li < P.longs.size() && P.longs[li].chunk0 + P.longs[li].nchunks != piece) fail("long row pieces", P.longs[li].nchunks, piece);
+        ++li;
+        ++row;
+      }
+      continue;
+    }
+    if (ch.r0 != row) fail("chunks out of order", ch.r0, row);
+    if (ch.r1 <= ch.r0 || ch.r1 - ch.r0 > kChunkRows) fail("chunk rows", ch.r0, ch.r1);
+    if (ch.k0 != ptr[static_cast<size_t>(ch.r0)] || ch.k1 != ptr[static_cast<size_t>(ch.r1)]) fail("chunk entries do not match its rows", ch.k0, ch.k1);
+    row = ch.r1;
+  }
+  if (row != p.lines) fail("chunks do not cover every line", row, p.lines);
+  if (piece != P.npieces || li != P.longs.size()) fail("piece count", piece, P.npieces);
+  // Segments: every block's in order, together every chunk once.
+  if (static_cast<int>(P.seg_start.size()) != grid + 1) fail("segment starts", static_cast<long long>(P.seg_start.size()), grid + 1);
+  long long next = 0, inside = 0;
+  const int ext4 = (p.extent + 3) & ~3;
+  std::vector<int> chunk_block(static_cast<size_t>(T), -1);
+  for (int b = 0; b < grid; ++b) {
+    for (int s = P.seg_start[b]; s < P.seg_start[b + 1]; ++s) {
+      const ChunkSeg& sg = P.segs[static_cast<size_t>(s)];
+      if (sg.c0 != next || sg.c1 <= sg.c0 || sg.c1 > T) fail("segment chunks", sg.c0, next);
+      if (sg.len > 0) {
+        if (sg.lo % 4 != 0 || sg.len % 4 != 0) fail("window not on 4-element bounds", sg.lo, sg.len);
+        if (sg.lo < 0 || sg.lo + sg.len > ext4 || sg.lo + sg.len > p.extent + kPad) fail("window beyond the padded vector", sg.lo, sg.len);
+        if (sg.len > P.wmax || P.wmax > std::max(wmax, ext4)) fail("window length", sg.len, P.wmax);
+      }
+      for (int c = sg.c0; c < sg.c1 && c < T; ++c) {
+        chunk_block[static_cast<size_t>(c)] = b;
+        const Tile& ch = P.chunks[static_cast<size_t>(c)];
+        for (int k = ch.k0; k < ch.k1; ++k) {
+          const bool in = sg.len > 0 && static_cast<unsigned>(idx[static_cast<size_t>(k)] - sg.lo) < static_cast<unsigned>(sg.len);
+          inside += in;
+          // A split layout's main entries in a windowed chunk are all inside the window.
+          if (P.split && sg.len > 0 && ch.r1 >= 0 && !in) fail("main entry outside its window", k, idx[static_cast<size_t>(k)]);
+        }
+      }
+      next = sg.c1;
+    }
+  }
+  if (next != T) fail("segments do not cover every chunk", next, T);
+  if (nnz > 0 && std::abs(static_cast<double>(inside) / static_cast<double>(nnz) - P.staged) > 1e-12) {
+    fail("staged share", inside, nnz);
+  }
+  if (!P.split) {
+    if (!P.orounds.empty() || !P.oidx.empty()) fail("outer part of an unsplit layout", static_cast<long long>(P.oidx.size()), 0);
+    return;
+  }
+  // Split: main and outer entries partition the layout's entries, in row order.
+  if (static_cast<long long>(P.map.size() + P.omap.size()) != nnz) fail("split entry count", static_cast<long long>(P.map.size() + P.omap.size()), nnz);
+  std::vector<char> seen(static_cast<size_t>(nnz), 0);
+  for (size_t k = 0; k < P.map.size(); ++k) {
+    const int f = P.map[k];
+    if (f < 0 || f >= nnz || seen[static_cast<size_t>(f)]++ || P.idx[k] != p.idx[static_cast<size_t>(f)]) fail("main map", static_cast<long long>(k), f);
+  }
+  for (size_t k = 0; k < P.omap.size(); ++k) {
+    const int f = P.omap[k];
+    if (f < 0 || f >= nnz || seen[static_cast<size_t>(f)]++ || P.oidx[k] != p.idx[static_cast<size_t>(f)]) fail("outer map", static_cast<long long>(k), f);
+  }
+  for (int r = 0; r < p.lines; ++r) {
+    const int full = p.ptr[r + 1] - p.ptr[r];
+    const int parts = (P.ptr[r + 1] - P.ptr[r]) + (P.optr[r + 1] - P.optr[r]);
+    if (full != parts) fail("row split", r, full - parts);
+  }
+  // Outer rounds: every row once, in order, by the block whose chunks hold it.
+  if (static_cast<int>(P.oround_start.size()) != grid + 1) fail("round starts", static_cast<long long>(P.oround_start.size()), grid + 1);
+  std::vector<int> row_block(static_cast<size_t>(p.lines), -1);
+  int orow = 0;
+  for (int b = 0; b < grid; ++b) {
+    for (int q = P.oround_start[b]; q < P.oround_start[b + 1]; ++q) {
+      const int2 rr = P.orounds[static_cast<size_t>(q)];
+      if (rr.x != orow || rr.y <= rr.x) fail("outer rounds out of order", rr.x, orow);
+      if (P.optr[rr.y] - P.optr[rr.x] > round_cap) fail("outer round exceeds the staging space", P.optr[rr.y] - P.optr[rr.x], round_cap);
+      for (int r = rr.x; r < rr.y && r < p.lines; ++r) row_block[static_cast<size_t>(r)] = b;
+      orow = rr.y;
+    }
+  }
+  if (orow != p.lines) fail("outer rounds do not cover every row", orow, p.lines);
+  for (long long c = 0; c < T; ++c) {
+    const Tile& ch = P.chunks[static_cast<size_t>(c)];
+    if (ch.r1 < 0) continue;
+    for (int r = ch.r0; r < ch.r1; ++r) {
+      if (row_block[static_cast<size_t>(r)] != chunk_block[static_cast<size_t>(c)]) fail("outer sum written by another block", r, chunk_block[static_cast<size_t>(c)]);
+    }
+  }
+}
+
 // A pattern from a file: int32 lines, int32 extent, int32 ptr[lines + 1], int32 idx[nnz].
 bool read_pattern(const char* path, Pattern* p) {
   std::FILE* f = std::fopen(path, "rb");
@@ -197,6 +320,7 @@ int check_file(const char* path) {
     for (int wmax : {0, 16384, 40960}) check_windows(p, tiles, wmax);
     chunks += nchunks;
   }
+  for (int wmax : {0, 32768}) check_chunk_plan(p, wmax, 152, 0.5);
   if (g_failures != 0) {
     std::printf("%d failures\n", g_failures);
     return 1;
@@ -236,6 +360,14 @@ int main(int argc, char** argv) {
           build_tiles(p.ptr, p.lines, lanes, threads, &tiles, &longs, &nchunks);
           check_tiles(p, lanes, threads, tiles, longs, nchunks);
           for (int wmax : {0, 1024, 8192, 40000}) check_windows(p, tiles, wmax);
+          ++layouts;
+        }
+      }
+      // The FP32 chunk plans: unstaged, windowed and split forms, and grids larger than the
+      // number of chunks.
+      for (int wmax : {0, 1024, 4096, 8192, 32768}) {
+        for (int grid : {1, 7, 152, 4000}) {
+          for (double split_min : {0.0, 0.5}) check_chunk_plan(p, wmax, grid, split_min);
           ++layouts;
         }
       }
