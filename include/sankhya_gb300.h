@@ -275,10 +275,42 @@ SGB_API int sankhya_gb300_batch_load(sankhya_gb300_batch* batch, int32_t count,
 SGB_API int sankhya_gb300_batch_solve(sankhya_gb300_batch* batch,
                                       const sankhya_gb300_params* params,
                                       sankhya_gb300_batch_item* items, double* device_seconds);
+/* The schedule of the batch's next solves (no reference counterpart): `lanes` threads share a
+ * row or column in the matrix passes (1, 2, 4, 8, 16 or 32) and each LP is solved by a block
+ * of `threads` threads (128, 256 or 512). lanes = threads = 0 (the default) lets every solve
+ * pick the schedule itself: before the solve it times each of 1, 2, 4 and 8 lanes at 128,
+ * 256 and 512 threads for 200 steps on a sample of the batch (up to four LPs per SM, spread
+ * over the LPs' sizes) and takes the fastest. Sums inside a row or column are taken in a
+ * fixed order for a given schedule, so a fixed schedule gives bit-reproducible solves; an
+ * autotuned one may pick differently from run to run. Anything else is
+ * SANKHYA_GB300_ERROR_ARGUMENT. */
+SGB_API int sankhya_gb300_batch_schedule(sankhya_gb300_batch* batch, int32_t lanes,
+                                         int32_t threads);
+/* The schedule the last solve ran with and the seconds its autotuning took (0 when the
+ * schedule was set). Any pointer may be NULL. */
+SGB_API int sankhya_gb300_batch_last_schedule(sankhya_gb300_batch* batch, int32_t* lanes,
+                                              int32_t* threads, double* tune_seconds);
 /* The reported point of LP `index`, as sankhya_gb300_pdhg_solution. */
 SGB_API int sankhya_gb300_batch_solution(sankhya_gb300_batch* batch, int32_t index,
                                          double* col_value, double* col_dual,
                                          double* row_dual);
+/* Replaces the reported point of LP `index` (after a solve) with the caller's, given as
+ * sankhya_gb300_batch_solution returns it: a warm start for sankhya_gb300_batch_polish, which
+ * reads the active sets from that point and re-solves them for the LP's own data. No
+ * reference counterpart: the reference warm-starts a branch-and-bound node from its parent's
+ * basis inside its simplex (src/mip/branch_and_bound_node.cpp); this is the same hand-over for
+ * the batched engine, e.g. a child node polished from its parent's vertex. */
+SGB_API int sankhya_gb300_batch_set_point(sankhya_gb300_batch* batch, int32_t index,
+                                          const double* col_value, const double* col_dual,
+                                          const double* row_dual);
+/* The infeasibility certificate of LP `index` when the last solve reported it
+ * SANKHYA_GB300_INFEASIBLE (no reference counterpart: the reference's PDHG reports no
+ * infeasibility): `ray` (m entries) receives the dual direction d, in the LP's own units,
+ * whose value
+ *   sum_j min over [l_j, u_j] of (A'd)_j x_j  -  sum_i max over [rl_i, ru_i] of d_i s_i
+ * is positive, which no feasible x allows (every term is finite for a certificate). For any
+ * other status it holds the last direction tested, which proves nothing. */
+SGB_API int sankhya_gb300_batch_ray(sankhya_gb300_batch* batch, int32_t index, double* ray);
 
 /* Gradients through the last batch solve (no reference counterpart: the reference has no
  * differentiation). For L(x, y, f) at the optimum, with x = col_value, y = row_dual (the

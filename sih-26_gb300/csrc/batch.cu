@@ -3,6 +3,7 @@
 #include "batch_engine.hpp"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -175,6 +176,7 @@ void BatchEngine::load(int count, const sankhya_gb300_lp* lps) {
   d_mats_out_.upload(mats_.data(), mats_.size(), s);
   d_inst_.upload(inst_.data(), inst_.size(), s);
   d_order_.upload(order.data(), order.size(), s);
+  order_ = order;
   d_queue_.allocate(4);
   csc_ptr_.upload(cptr.data(), cptr.size(), s);
   csc_idx_.upload(cidx.data(), cidx.size(), s);
@@ -310,6 +312,7 @@ void BatchEngine::solve(const sankhya_gb300_params& p, sankhya_gb300_batch_item*
   b.stop_at_request = p.stop_at_request != 0;
   b.stop_rule = p.stop_rule == SANKHYA_GB300_STOP_RELATIVE ? 1 : 0;
   b.detect_infeasibility = 1;
+  b.lanes = 1;
   if (mixed) {
     b.csc_f = csc_f_.ptr;
     b.csr_f = csr_f_.ptr;
@@ -337,16 +340,36 @@ void BatchEngine::solve(const sankhya_gb300_params& p, sankhya_gb300_batch_item*
     b.refinements = refinements_.ptr;
   }
 
-  buffers_ = b;
-  SGB_CUDA(cudaEventRecord(timing_[0], s));
+  // The scaling launch runs once; with no schedule set, the candidate schedules are timed on
+  // a sample of the batch before the solve (not part of the solve's device time).
   const int scale_grid = std::max(1, std::min(b.nmatrices, num_sms_ * 8));
+  SGB_CUDA(cudaEventRecord(timing_[0], s));
   launch_batch_scaling(b, scale_grid, s);
+  SGB_CUDA(cudaGetLastError());
+  SGB_CUDA(cudaEventRecord(timing_[1], s));
+  SGB_CUDA(cudaEventSynchronize(timing_[1]));
+  float scale_ms = 0.0f;
+  SGB_CUDA(cudaEventElapsedTime(&scale_ms, timing_[0], timing_[1]));
+  int lanes = sched_lanes_, threads = sched_threads_;
+  last_tune_seconds_ = 0.0;
+  if (lanes == 0 || threads == 0) {
+    const auto t0 = std::chrono::steady_clock::now();
+    autotune(b, mixed, &lanes, &threads);
+    last_tune_seconds_ =
+        std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  b.lanes = lanes;
+  last_lanes_ = lanes;
+  last_threads_ = threads;
+  buffers_ = b;
+  SGB_CUDA(cudaMemsetAsync(d_queue_.ptr, 0, 4 * sizeof(unsigned int), s));
+  SGB_CUDA(cudaEventRecord(timing_[0], s));
   if (mixed) {
-    const int grid = std::max(1, std::min(count_, num_sms_ * batch_mixed_blocks_per_sm()));
-    launch_batch_solve_mixed(b, grid, s);
+    const int grid = std::max(1, std::min(count_, num_sms_ * batch_mixed_blocks_per_sm(threads)));
+    launch_batch_solve_mixed(b, grid, threads, s);
   } else {
-    const int grid = std::max(1, std::min(count_, num_sms_ * batch_blocks_per_sm()));
-    launch_batch_solve(b, grid, s);
+    const int grid = std::max(1, std::min(count_, num_sms_ * batch_blocks_per_sm(threads)));
+    launch_batch_solve(b, grid, threads, s);
   }
   SGB_CUDA(cudaGetLastError());
   SGB_CUDA(cudaEventRecord(timing_[1], s));
@@ -364,7 +387,7 @@ void BatchEngine::solve(const sankhya_gb300_params& p, sankhya_gb300_batch_item*
   SGB_CUDA(cudaStreamSynchronize(s));
   float ms = 0.0f;
   SGB_CUDA(cudaEventElapsedTime(&ms, timing_[0], timing_[1]));
-  if (device_seconds != nullptr) *device_seconds = 1e-3 * ms;
+  if (device_seconds != nullptr) *device_seconds = 1e-3 * (scale_ms + ms);
   for (int k = 0; k < count_; ++k) {
     const BatchOutcome& o = out[static_cast<size_t>(k)];
     sankhya_gb300_batch_item& it = items[k];
@@ -386,6 +409,74 @@ void BatchEngine::solve(const sankhya_gb300_params& p, sankhya_gb300_batch_item*
     it.refinements = rounds[static_cast<size_t>(k)];
   }
   solved_ = true;
+}
+
+void BatchEngine::set_schedule(int lanes, int threads) {
+  const bool automatic = lanes == 0 && threads == 0;
+  const bool lanes_ok = lanes >= 1 && lanes <= 32 && (lanes & (lanes - 1)) == 0;
+  const bool threads_ok = threads == 128 || threads == 256 || threads == 512;
+  if (!automatic && !(lanes_ok && threads_ok)) {
+    throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT,
+                      "a batch schedule is lanes 1, 2, 4, 8, 16 or 32 and threads 128, 256 or "
+                      "512 (or 0 and 0 to autotune)"};
+  }
+  sched_lanes_ = lanes;
+  sched_threads_ = threads;
+}
+
+void BatchEngine::last_schedule(int* lanes, int* threads, double* tune_seconds) const {
+  if (lanes != nullptr) *lanes = last_lanes_;
+  if (threads != nullptr) *threads = last_threads_;
+  if (tune_seconds != nullptr) *tune_seconds = last_tune_seconds_;
+}
+
+// The autotuner. Candidates: 1, 2, 4 or 8 lanes per row or column, 128, 256 or 512 threads
+// per LP. Each runs the batch's own solve kernel, for kTuneSteps accepted steps, on the same
+// sample: up to four LPs per SM taken at even strides through the solve order (so large and
+// small LPs are both in it), from scratch, with the batch's own options. The fastest by
+// device time wins; the sample's outcomes are overwritten by the solve that follows.
+void BatchEngine::autotune(BatchBuffers b, bool mixed, int* lanes, int* threads) {
+  constexpr long long kTuneSteps = 200;
+  cudaStream_t s = stream_;
+  const int sample = std::max(1, std::min(count_, 4 * num_sms_));
+  std::vector<int> pick(static_cast<size_t>(sample));
+  for (int k = 0; k < sample; ++k) {
+    pick[static_cast<size_t>(k)] =
+        order_[static_cast<size_t>(static_cast<long long>(k) * count_ / sample)];
+  }
+  d_tune_order_.upload(pick.data(), pick.size(), s);
+  b.order = d_tune_order_.ptr;
+  b.ninstances = sample;
+  b.iteration_limit = std::min(b.iteration_limit, kTuneSteps);
+  float best_ms = 0.0f;
+  *lanes = 1;
+  *threads = kBatchThreads;
+  bool first = true;
+  for (int t : {128, 256, 512}) {
+    for (int l : {1, 2, 4, 8}) {
+      b.lanes = l;
+      SGB_CUDA(cudaMemsetAsync(d_queue_.ptr, 0, 4 * sizeof(unsigned int), s));
+      SGB_CUDA(cudaEventRecord(timing_[0], s));
+      if (mixed) {
+        const int grid = std::max(1, std::min(sample, num_sms_ * batch_mixed_blocks_per_sm(t)));
+        launch_batch_solve_mixed(b, grid, t, s);
+      } else {
+        const int grid = std::max(1, std::min(sample, num_sms_ * batch_blocks_per_sm(t)));
+        launch_batch_solve(b, grid, t, s);
+      }
+      SGB_CUDA(cudaGetLastError());
+      SGB_CUDA(cudaEventRecord(timing_[1], s));
+      SGB_CUDA(cudaEventSynchronize(timing_[1]));
+      float ms = 0.0f;
+      SGB_CUDA(cudaEventElapsedTime(&ms, timing_[0], timing_[1]));
+      if (first || ms < best_ms) {
+        best_ms = ms;
+        *lanes = l;
+        *threads = t;
+        first = false;
+      }
+    }
+  }
 }
 
 void BatchEngine::solution(int index, double* col_value, double* col_dual, double* row_dual) {
@@ -420,6 +511,52 @@ void BatchEngine::solution(int index, double* col_value, double* col_dual, doubl
   }
 }
 
+void BatchEngine::ray(int index, double* ray) {
+  require_loaded();
+  if (!solved_) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no solve has run"};
+  if (index < 0 || index >= count_) {
+    throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no such LP in the batch"};
+  }
+  if (ray == nullptr) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "null ray"};
+  SGB_CUDA(cudaSetDevice(device_));
+  const BatchInstance& I = inst_[static_cast<size_t>(index)];
+  if (I.m > 0) {
+    SGB_CUDA(cudaMemcpyAsync(ray, ray_.ptr + I.row, static_cast<size_t>(I.m) * sizeof(double),
+                             cudaMemcpyDeviceToHost, stream_));
+  }
+  SGB_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void BatchEngine::set_point(int index, const double* col_value, const double* col_dual,
+                            const double* row_dual) {
+  require_loaded();
+  if (!solved_) throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no solve has run"};
+  if (index < 0 || index >= count_) {
+    throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "no such LP in the batch"};
+  }
+  const BatchInstance& I = inst_[static_cast<size_t>(index)];
+  const size_t n = static_cast<size_t>(I.n), m = static_cast<size_t>(I.m);
+  if ((n > 0 && (col_value == nullptr || col_dual == nullptr)) || (m > 0 && row_dual == nullptr)) {
+    throw EngineError{SANKHYA_GB300_ERROR_ARGUMENT, "null point"};
+  }
+  SGB_CUDA(cudaSetDevice(device_));
+  // The inverse of solution(): col_dual = sense * reduced, row_dual = sense * (-y).
+  std::vector<double> red(n), by(m);
+  for (size_t j = 0; j < n; ++j) red[j] = I.sense * col_dual[j];
+  for (size_t i = 0; i < m; ++i) by[i] = -I.sense * row_dual[i];
+  if (n > 0) {
+    SGB_CUDA(cudaMemcpyAsync(best_x_.ptr + I.col, col_value, n * sizeof(double),
+                             cudaMemcpyHostToDevice, stream_));
+    SGB_CUDA(cudaMemcpyAsync(reduced_.ptr + I.col, red.data(), n * sizeof(double),
+                             cudaMemcpyHostToDevice, stream_));
+  }
+  if (m > 0) {
+    SGB_CUDA(cudaMemcpyAsync(best_y_.ptr + I.row, by.data(), m * sizeof(double),
+                             cudaMemcpyHostToDevice, stream_));
+  }
+  SGB_CUDA(cudaStreamSynchronize(stream_));
+}
+
 void BatchEngine::adjoint(const double* const* dl_dx, const double* const* dl_dy,
                           const double* dl_df, double* const* dl_dc, double* const* dl_drl,
                           double* const* dl_dru, double* const* dl_dl, double* const* dl_du,
@@ -439,10 +576,12 @@ void BatchEngine::adjoint(const double* const* dl_dx, const double* const* dl_dy
     if (dl_dx != nullptr && dl_dx[k] != nullptr) {
       std::copy(dl_dx[k], dl_dx[k] + I.n, gx.begin() + I.col);
     }
+    // The kernel differentiates the minimise-space LP (cost sense * c, multipliers
+    // sense * y): y and f enter with the sense, dL/dc leaves with it (finish_adjoint).
     if (dl_dy != nullptr && dl_dy[k] != nullptr) {
-      std::copy(dl_dy[k], dl_dy[k] + I.m, gy.begin() + I.row);
+      for (int i = 0; i < I.m; ++i) gy[static_cast<size_t>(I.row + i)] = I.sense * dl_dy[k][i];
     }
-    if (dl_df != nullptr) gf[static_cast<size_t>(k)] = dl_df[k];
+    if (dl_df != nullptr) gf[static_cast<size_t>(k)] = I.sense * dl_df[k];
   }
   SGB_CUDA(cudaMemcpyAsync(a_gx_.ptr, gx.data(), N * sizeof(double), cudaMemcpyHostToDevice, s));
   SGB_CUDA(cudaMemcpyAsync(a_gy_.ptr, gy.data(), M * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -450,7 +589,8 @@ void BatchEngine::adjoint(const double* const* dl_dx, const double* const* dl_dy
                            cudaMemcpyHostToDevice, s));
   AdjointBuffers a = adjoint_buffers();
   SGB_CUDA(cudaMemsetAsync(d_queue_.ptr + 2, 0, sizeof(unsigned int), s));
-  const int grid = std::max(1, std::min(count_, num_sms_ * batch_blocks_per_sm()));
+  const int grid =
+      std::max(1, std::min(count_, num_sms_ * adjoint_blocks_per_sm(a.smem_vec)));
   launch_batch_adjoint(buffers_, a, grid, s);
   SGB_CUDA(cudaGetLastError());
   finish_adjoint(dl_dc, dl_drl, dl_dru, dl_dl, dl_du, info);
@@ -462,8 +602,32 @@ void BatchEngine::ensure_adjoint_buffers() {
   const size_t M = static_cast<size_t>(std::max(total_m_, 1LL));
   for (DeviceArray<double>* a : {&a_gx_, &a_dc_, &a_dl_, &a_du_}) a->allocate(N);
   for (DeviceArray<double>* a : {&a_gy_, &a_drl_, &a_dru_}) a->allocate(M);
-  for (auto& a : a_cn_) a.allocate(N);
-  for (auto& a : a_rm_) a.allocate(M);
+  for (auto& a : a_kw_) a.allocate(M);
+  a_bcol_.allocate(N);
+  a_cpos_.allocate(N);
+  a_rrow_.allocate(M);
+  a_rpos_.allocate(M);
+  a_kcp_.allocate(N + static_cast<size_t>(count_));
+  a_krp_.allocate(M + static_cast<size_t>(count_));
+  // Each LP's compact basis matrix holds at most its matrix's entries.
+  std::vector<long long> knz(static_cast<size_t>(count_));
+  long long nz = 0;
+  int dim = 1;
+  for (int k = 0; k < count_; ++k) {
+    const BatchInstance& I = inst_[static_cast<size_t>(k)];
+    knz[static_cast<size_t>(k)] = nz;
+    nz += mats_[static_cast<size_t>(I.matrix)].nnz;
+    dim = std::max(dim, std::min(I.m, I.n));
+  }
+  const size_t Z = static_cast<size_t>(std::max(nz, 1LL));
+  a_kci_.allocate(Z);
+  a_kri_.allocate(Z);
+  a_kcv_.allocate(Z);
+  a_krv_.allocate(Z);
+  a_knz_.allocate(knz.size());
+  SGB_CUDA(cudaMemcpy(a_knz_.ptr, knz.data(), knz.size() * sizeof(long long),
+                      cudaMemcpyHostToDevice));
+  a_smem_vec_ = std::min(dim, kAdjSmemVec);
   a_gf_.allocate(static_cast<size_t>(count_));
   a_cs_.allocate(N);
   a_rs_.allocate(M);
@@ -481,23 +645,24 @@ AdjointBuffers BatchEngine::adjoint_buffers() {
   a.du = a_du_.ptr;
   a.drl = a_drl_.ptr;
   a.dru = a_dru_.ptr;
-  a.cn0 = a_cn_[0].ptr;
-  a.cn1 = a_cn_[1].ptr;
-  a.cn2 = a_cn_[2].ptr;
-  a.cn3 = a_cn_[3].ptr;
-  a.cn4 = a_cn_[4].ptr;
-  a.cn5 = a_cn_[5].ptr;
-  a.rm0 = a_rm_[0].ptr;
-  a.rm1 = a_rm_[1].ptr;
-  a.rm2 = a_rm_[2].ptr;
-  a.rm3 = a_rm_[3].ptr;
-  a.rm4 = a_rm_[4].ptr;
-  a.rm5 = a_rm_[5].ptr;
+  for (int k = 0; k < kAdjVectors; ++k) a.kw[k] = a_kw_[k].ptr;
+  a.bcol = a_bcol_.ptr;
+  a.cpos = a_cpos_.ptr;
+  a.rrow = a_rrow_.ptr;
+  a.rpos = a_rpos_.ptr;
+  a.kcp = a_kcp_.ptr;
+  a.krp = a_krp_.ptr;
+  a.kci = a_kci_.ptr;
+  a.kri = a_kri_.ptr;
+  a.kcv = a_kcv_.ptr;
+  a.krv = a_krv_.ptr;
+  a.knz = a_knz_.ptr;
   a.col_state = a_cs_.ptr;
   a.row_state = a_rs_.ptr;
   a.outcome = a_out_.ptr;
   a.max_iterations = 20000;
   a.cg_tolerance = 1e-13;
+  a.smem_vec = a_smem_vec_;
   return a;
 }
 
@@ -525,6 +690,11 @@ void BatchEngine::finish_adjoint(double* const* dl_dc, double* const* dl_drl,
   };
   for (int k = 0; k < count_; ++k) {
     const BatchInstance& I = inst_[static_cast<size_t>(k)];
+    if (I.sense < 0.0) {
+      for (long long j = I.col; j < I.col + I.n; ++j) {
+        dc[static_cast<size_t>(j)] = -dc[static_cast<size_t>(j)];
+      }
+    }
     put(dl_dc, k, dc, I.col, I.n);
     put(dl_dl, k, dl, I.col, I.n);
     put(dl_du, k, du, I.col, I.n);
@@ -552,7 +722,8 @@ void BatchEngine::polish(sankhya_gb300_batch_item* items, sankhya_gb300_adjoint_
   ensure_adjoint_buffers();
   AdjointBuffers a = adjoint_buffers();
   SGB_CUDA(cudaMemsetAsync(d_queue_.ptr + 3, 0, sizeof(unsigned int), s));
-  const int grid = std::max(1, std::min(count_, num_sms_ * batch_blocks_per_sm()));
+  const int grid =
+      std::max(1, std::min(count_, num_sms_ * adjoint_blocks_per_sm(a.smem_vec)));
   launch_batch_polish(buffers_, a, grid, s);
   SGB_CUDA(cudaGetLastError());
   std::vector<BatchOutcome> out(static_cast<size_t>(count_));

@@ -26,7 +26,13 @@
 
 namespace sgb {
 
-constexpr int kBatchThreads = 256;
+constexpr int kBatchThreads = 256;     // scaling launches
+constexpr int kBatchMaxThreads = 512;  // the largest block a batched solve runs with
+constexpr int kAdjThreads = 512;       // adjoint and polish launches
+constexpr int kAdjVectors = 9;         // compact per-LP vectors of the square solves
+// The square solves gather from two vectors of |B| entries; they sit in shared memory for
+// |B| up to this many (2 x 96 KB), else in global memory.
+constexpr int kAdjSmemVec = 12288;
 
 // A distinct constraint matrix. Offsets index the packed arrays of BatchBuffers.
 struct BatchMatrix {
@@ -92,6 +98,9 @@ struct BatchBuffers {
   double tolerance;
   long long iteration_limit;
   int use_restarts, stop_at_request, stop_rule, detect_infeasibility;
+  // The schedule: threads that share a row or column in the matrix passes (a power of two,
+  // at most 32; the block size is the launch's).
+  int lanes;
 };
 
 // The adjoint of a solved batch (batch_kernels.cu, k_batch_adjoint): per LP, upstream
@@ -100,30 +109,41 @@ struct BatchBuffers {
 // and the column bounds.
 struct AdjointOutcome {
   int basic_cols, active_rows;  // |B| and |R|: equal for a nondegenerate optimum
-  int iterations[2];            // conjugate-gradient iterations of the two solves
-  double residual[2];           // their final relative residuals
-  int status;  // 0 ok, 1 degenerate (|B| != |R|), 2 not converged, 3 maximisation (unsupported)
+  int iterations[2];            // conjugate-gradient iterations of the two square solves
+  double residual[2];           // their final relative residuals ||h - S u|| / ||h||
+  int status;  // 0 ok, 1 degenerate (|B| != |R|), 2 not converged
 };
 
 struct AdjointBuffers {
   const double *gx, *gy, *gf;                      // upstream (gx, gy per LP slices; gf per LP)
   double *dc, *dl, *du, *drl, *dru;                // results
-  double *cn0, *cn1, *cn2, *cn3, *cn4, *cn5;       // n-sized scratch per LP
-  double *rm0, *rm1, *rm2, *rm3, *rm4, *rm5;       // m-sized scratch per LP
+  double* kw[kAdjVectors];                         // m-sized compact vectors per LP
+  int *bcol, *cpos;                                // basic columns; a column's number in B
+  int *rrow, *rpos;                                // active rows; a row's number in R
+  int *kcp, *krp;                                  // A_RB's CSC / CSR starts (n+1, m+1 per LP)
+  int *kci, *kri;                                  // their entries' positions
+  double *kcv, *krv;                               // and values
+  const long long* knz;                            // per LP: offset of its entries
   signed char *col_state, *row_state;              // active sets
   AdjointOutcome* outcome;
-  int max_iterations;
+  int max_iterations;                              // per conjugate-gradient run
   double cg_tolerance;
+  int smem_vec;                                    // |B| up to which the gathers use smem
 };
 
 void launch_batch_scaling(const BatchBuffers& b, int grid, cudaStream_t s);
+// The adjoint and polish launches run kAdjThreads-thread blocks with 2 * a.smem_vec
+// doubles of dynamic shared memory; adjoint_blocks_per_sm is their occupancy.
 void launch_batch_adjoint(const BatchBuffers& b, const AdjointBuffers& a, int grid,
                           cudaStream_t s);
 void launch_batch_polish(const BatchBuffers& b, const AdjointBuffers& a, int grid,
                          cudaStream_t s);
-void launch_batch_solve(const BatchBuffers& b, int grid, cudaStream_t s);
-void launch_batch_solve_mixed(const BatchBuffers& b, int grid, cudaStream_t s);
-int batch_mixed_blocks_per_sm();
-int batch_blocks_per_sm();
+int adjoint_blocks_per_sm(int smem_vec);
+// The solve launches run blocks of `threads` threads (a multiple of 32, at most
+// kBatchMaxThreads); the occupancy queries are for that block size.
+void launch_batch_solve(const BatchBuffers& b, int grid, int threads, cudaStream_t s);
+void launch_batch_solve_mixed(const BatchBuffers& b, int grid, int threads, cudaStream_t s);
+int batch_mixed_blocks_per_sm(int threads);
+int batch_blocks_per_sm(int threads = kBatchThreads);
 
 }  // namespace sgb

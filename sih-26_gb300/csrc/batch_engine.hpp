@@ -19,6 +19,11 @@ class BatchEngine {
   void solve(const sankhya_gb300_params& params, sankhya_gb300_batch_item* items,
              double* device_seconds);
   void solution(int index, double* col_value, double* col_dual, double* row_dual);
+  // The last direction LP `index` tested as a Farkas certificate (m entries, unscaled).
+  void ray(int index, double* ray);
+  // Replaces LP `index`'s reported point (the triple solution() returns).
+  void set_point(int index, const double* col_value, const double* col_dual,
+                 const double* row_dual);
   void adjoint(const double* const* dl_dx, const double* const* dl_dy, const double* dl_df,
                double* const* dl_dc, double* const* dl_drl, double* const* dl_dru,
                double* const* dl_dl, double* const* dl_du, sankhya_gb300_adjoint_info* info);
@@ -27,9 +32,18 @@ class BatchEngine {
   void polish(sankhya_gb300_batch_item* items, sankhya_gb300_adjoint_info* info);
   int count() const { return count_; }
   int distinct_matrices() const { return static_cast<int>(mats_.size()); }
+  // The schedule of the next solves: lanes per row or column (1, 2, 4, 8, 16 or 32) and
+  // threads per LP (128, 256 or 512); 0 and 0 let each solve pick it (autotune).
+  void set_schedule(int lanes, int threads);
+  // The schedule the last solve ran with, and the seconds its autotuning took (0 if the
+  // schedule was set).
+  void last_schedule(int* lanes, int* threads, double* tune_seconds) const;
 
  private:
   void require_loaded() const;
+  // Times every candidate schedule on a sample of the batch (a few hundred steps of up to
+  // four LPs per SM, spread over the size order) and returns the fastest.
+  void autotune(BatchBuffers b, bool mixed, int* lanes, int* threads);
   void ensure_adjoint_buffers();
   AdjointBuffers adjoint_buffers();
   void finish_adjoint(double* const* dl_dc, double* const* dl_drl, double* const* dl_dru,
@@ -37,6 +51,11 @@ class BatchEngine {
                       sankhya_gb300_adjoint_info* info);
 
   int device_ = 0;
+  int sched_lanes_ = 0, sched_threads_ = 0;        // 0: autotune
+  int last_lanes_ = 1, last_threads_ = kBatchThreads;
+  double last_tune_seconds_ = 0.0;
+  std::vector<int> order_;                         // the solve order (largest LP first)
+  DeviceArray<int> d_tune_order_;
   cudaStream_t stream_ = nullptr;
   cudaEvent_t timing_[2] = {nullptr, nullptr};
   int num_sms_ = 0;
@@ -69,7 +88,11 @@ class BatchEngine {
   // Adjoint (allocated on first use).
   bool adjoint_ready_ = false;
   DeviceArray<double> a_gx_, a_gy_, a_gf_, a_dc_, a_dl_, a_du_, a_drl_, a_dru_;
-  DeviceArray<double> a_cn_[6], a_rm_[6];
+  DeviceArray<double> a_kw_[kAdjVectors];
+  DeviceArray<int> a_bcol_, a_cpos_, a_rrow_, a_rpos_, a_kcp_, a_krp_, a_kci_, a_kri_;
+  DeviceArray<double> a_kcv_, a_krv_;
+  DeviceArray<long long> a_knz_;
+  int a_smem_vec_ = 0;
   DeviceArray<signed char> a_cs_, a_rs_;
   DeviceArray<AdjointOutcome> a_out_;
   long long total_n_ = 0, total_m_ = 0, mat_n_ = 0, mat_m_ = 0;

@@ -12,6 +12,8 @@
 // order, so the two agree to rounding, not bit for bit.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "batch.cuh"
 #include "common.cuh"
 #include "decisions.cuh"
@@ -21,7 +23,7 @@
 namespace sgb {
 namespace {
 
-constexpr int kBScratch = 16 * (kBatchThreads / 32);
+constexpr int kBScratch = 16 * (kBatchMaxThreads / 32);
 // A dual change d is accepted as a Farkas certificate when its value (see batch_farkas) is
 // above this share of the magnitude of the terms that make it up, at two evaluations in a
 // row. For a feasible LP the value is <= 0 in exact arithmetic.
@@ -168,7 +170,17 @@ struct LpView {
   double *y[2], *y_sum, *y_rst, *yu[2], *best_y;
   double* ray;
   double bound_norm, cost_norm;
+  int lanes;  // threads that share a row or column in the matrix passes (a power of two)
 };
+
+// The lanes of a line group (`lanes` consecutive threads, aligned inside a warp) add their
+// partial sums in a fixed xor tree; every lane receives the total. Every thread of the warp
+// calls it (the line loops below run the same number of iterations in every thread).
+template <typename V>
+__device__ __forceinline__ V lanes_sum(V s, int lanes) {
+  for (int o = lanes >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  return s;
+}
 
 __device__ LpView make_view(const BatchBuffers& b, const BatchInstance& I, const BatchMatrix& M) {
   LpView v;
@@ -215,6 +227,7 @@ __device__ LpView make_view(const BatchBuffers& b, const BatchInstance& I, const
   v.ray = b.ray + r;
   v.bound_norm = I.bound_norm;
   v.cost_norm = I.cost_norm;
+  v.lanes = b.lanes > 0 ? b.lanes : 1;
   return v;
 }
 
@@ -236,9 +249,16 @@ __device__ void b_primal(const LpView& v, Ctl* c, double* scratch) {
   const double tau = c->eta / omega;
   const bool add = c->pending_add != 0;
   double mv[1] = {0.0};
-  for (int j = threadIdx.x; j < v.n; j += T) {
+  // `lanes` threads per column: lane s sums entries s, s + lanes, ... in order.
+  const int L = v.lanes, G = T / L, sub = threadIdx.x & (L - 1);
+  for (int base = 0; base < v.n; base += G) {
+    const int j = base + static_cast<int>(threadIdx.x) / L;
     double acc = 0.0;
-    for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) acc = fma(v.csv[k], y[v.ci[k]], acc);
+    if (j < v.n) {
+      for (int k = v.cp[j] + sub; k < v.cp[j + 1]; k += L) acc = fma(v.csv[k], y[v.ci[k]], acc);
+    }
+    acc = lanes_sum(acc, L);
+    if (j >= v.n || sub != 0) continue;
     const double xj = x[j];
     if (add) v.x_sum[j] += xj;
     const double gradient = v.cs[j] + acc;
@@ -264,13 +284,20 @@ __device__ void b_dual(const LpView& v, Ctl* c, double* scratch) {
   const double sigma = c->eta * omega;
   const bool add = c->pending_add != 0;
   double acc2[2] = {0.0, 0.0};
-  for (int i = threadIdx.x; i < v.m; i += T) {
+  const int L = v.lanes, G = T / L, sub = threadIdx.x & (L - 1);
+  for (int base = 0; base < v.m; base += G) {
+    const int i = base + static_cast<int>(threadIdx.x) / L;
     double s0 = 0.0, s1 = 0.0;
-    for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
-      const double2 p = v.xd[v.ri[k]];
-      s0 = fma(v.rsv[k], p.x, s0);
-      s1 = fma(v.rsv[k], p.y, s1);
+    if (i < v.m) {
+      for (int k = v.rp[i] + sub; k < v.rp[i + 1]; k += L) {
+        const double2 p = v.xd[v.ri[k]];
+        s0 = fma(v.rsv[k], p.x, s0);
+        s1 = fma(v.rsv[k], p.y, s1);
+      }
     }
+    s0 = lanes_sum(s0, L);
+    s1 = lanes_sum(s1, L);
+    if (i >= v.m || sub != 0) continue;
     const double yi = y[i];
     if (add) v.y_sum[i] += yi;
     const double rl = v.rls[i], ru = v.rus[i];
@@ -352,13 +379,20 @@ __device__ void b_evaluate(const LpView& v, Ctl* c, double* scratch, bool fin) {
     }
   }
   __syncthreads();
-  for (int j = t; j < v.n; j += T) {
+  const int L = v.lanes, G = T / L, sub = t & (L - 1);
+  for (int base = 0; base < v.n; base += G) {
+    const int j = base + t / L;
     double sq[2] = {0.0, 0.0};
-    for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) {
-      const int row = v.ci[k];
-      sq[0] = fma(v.craw[k], v.yu[0][row], sq[0]);
-      if (avg) sq[1] = fma(v.craw[k], v.yu[1][row], sq[1]);
+    if (j < v.n) {
+      for (int k = v.cp[j] + sub; k < v.cp[j + 1]; k += L) {
+        const int row = v.ci[k];
+        sq[0] = fma(v.craw[k], v.yu[0][row], sq[0]);
+        if (avg) sq[1] = fma(v.craw[k], v.yu[1][row], sq[1]);
+      }
     }
+    sq[0] = lanes_sum(sq[0], L);
+    sq[1] = lanes_sum(sq[1], L);
+    if (j >= v.n || sub != 0) continue;
     const double cj = v.cost[j], lj = v.l[j], uj = v.u[j];
     double xc[2];
     if (fin) {
@@ -395,13 +429,19 @@ __device__ void b_evaluate(const LpView& v, Ctl* c, double* scratch, bool fin) {
     }
   }
   __syncthreads();
-  for (int i = t; i < v.m; i += T) {
+  for (int base = 0; base < v.m; base += G) {
+    const int i = base + t / L;
     double a[2] = {0.0, 0.0};
-    for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
-      const int col = v.ri[k];
-      a[0] = fma(v.rraw[k], v.xu[0][col], a[0]);
-      if (avg) a[1] = fma(v.rraw[k], v.xu[1][col], a[1]);
+    if (i < v.m) {
+      for (int k = v.rp[i] + sub; k < v.rp[i + 1]; k += L) {
+        const int col = v.ri[k];
+        a[0] = fma(v.rraw[k], v.xu[0][col], a[0]);
+        if (avg) a[1] = fma(v.rraw[k], v.xu[1][col], a[1]);
+      }
     }
+    a[0] = lanes_sum(a[0], L);
+    a[1] = lanes_sum(a[1], L);
+    if (i >= v.m || sub != 0) continue;
     const double rl = v.rl[i], ru = v.ru[i];
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
@@ -530,7 +570,7 @@ __device__ void b_apply(const LpView& v, const Ctl* c) {
 }
 
 // Four blocks per SM: the LP's pointers live in shared memory (s_view), not in registers.
-__global__ void __launch_bounds__(kBatchThreads, 4) k_batch_solve(BatchBuffers b) {
+__global__ void __launch_bounds__(kBatchMaxThreads, 2) k_batch_solve(BatchBuffers b) {
   __shared__ double scratch[kBScratch];
   __shared__ int s_item;
   __shared__ Ctl s_ctl;
@@ -712,9 +752,15 @@ __device__ void bm_primal(const LpView& v, const MixView& f, Ctl* c, double* scr
   const float tau = static_cast<float>(c->eta / omega);
   const bool add = c->pending_add != 0;
   float mvf = 0.0f;
-  for (int j = threadIdx.x; j < v.n; j += T) {
+  const int L = v.lanes, G = T / L, sub = threadIdx.x & (L - 1);
+  for (int base = 0; base < v.n; base += G) {
+    const int j = base + static_cast<int>(threadIdx.x) / L;
     float acc = 0.0f;
-    for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) acc = fmaf(f.csf[k], vv[v.ci[k]], acc);
+    if (j < v.n) {
+      for (int k = v.cp[j] + sub; k < v.cp[j + 1]; k += L) acc = fmaf(f.csf[k], vv[v.ci[k]], acc);
+    }
+    acc = lanes_sum(acc, L);
+    if (j >= v.n || sub != 0) continue;
     const float uj = u[j];
     if (add) f.u_sum[j] += uj;
     const float g = f.cf[j] + acc;
@@ -741,13 +787,20 @@ __device__ void bm_dual(const LpView& v, const MixView& f, Ctl* c, double* scrat
   const float inv_sigma = 1.0f / sigma;
   const bool add = c->pending_add != 0;
   float a0 = 0.0f, a1 = 0.0f;
-  for (int i = threadIdx.x; i < v.m; i += T) {
+  const int L = v.lanes, G = T / L, sub = threadIdx.x & (L - 1);
+  for (int base = 0; base < v.m; base += G) {
+    const int i = base + static_cast<int>(threadIdx.x) / L;
     float s0 = 0.0f, s1 = 0.0f;
-    for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
-      const float2 p = f.ud[v.ri[k]];
-      s0 = fmaf(f.rsf[k], p.x, s0);
-      s1 = fmaf(f.rsf[k], p.y, s1);
+    if (i < v.m) {
+      for (int k = v.rp[i] + sub; k < v.rp[i + 1]; k += L) {
+        const float2 p = f.ud[v.ri[k]];
+        s0 = fmaf(f.rsf[k], p.x, s0);
+        s1 = fmaf(f.rsf[k], p.y, s1);
+      }
     }
+    s0 = lanes_sum(s0, L);
+    s1 = lanes_sum(s1, L);
+    if (i >= v.m || sub != 0) continue;
     const float vi = vv[i];
     if (add) f.v_sum[i] += vi;
     const float gu = f.gu[i], gl = f.gl[i];
@@ -804,13 +857,20 @@ __device__ void bm_evaluate(const LpView& v, const MixView& f, Ctl* c, double* s
     s[6] += d * d;
   }
   __syncthreads();
-  for (int j = t; j < v.n; j += T) {
+  const int L = v.lanes, G = T / L, sub = t & (L - 1);
+  for (int base = 0; base < v.n; base += G) {
+    const int j = base + t / L;
     float sq[2] = {0.0f, 0.0f};
-    for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) {
-      const int row = v.ci[k];
-      sq[0] = fmaf(f.csf[k], f.vc[0][row], sq[0]);
-      if (avg) sq[1] = fmaf(f.csf[k], f.vc[1][row], sq[1]);
+    if (j < v.n) {
+      for (int k = v.cp[j] + sub; k < v.cp[j + 1]; k += L) {
+        const int row = v.ci[k];
+        sq[0] = fmaf(f.csf[k], f.vc[0][row], sq[0]);
+        if (avg) sq[1] = fmaf(f.csf[k], f.vc[1][row], sq[1]);
+      }
     }
+    sq[0] = lanes_sum(sq[0], L);
+    sq[1] = lanes_sum(sq[1], L);
+    if (j >= v.n || sub != 0) continue;
     const float ucur = f.u[cur][j];
     float cand[2] = {ucur, 0.0f};
     if (avg) cand[1] = (pend ? f.u_sum[j] + ucur : f.u_sum[j]) / count;
@@ -833,13 +893,19 @@ __device__ void bm_evaluate(const LpView& v, const MixView& f, Ctl* c, double* s
     s[11] += d * d;
   }
   __syncthreads();
-  for (int i = t; i < v.m; i += T) {
+  for (int base = 0; base < v.m; base += G) {
+    const int i = base + t / L;
     float a[2] = {0.0f, 0.0f};
-    for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
-      const int col = v.ri[k];
-      a[0] = fmaf(f.rsf[k], f.uc[0][col], a[0]);
-      if (avg) a[1] = fmaf(f.rsf[k], f.uc[1][col], a[1]);
+    if (i < v.m) {
+      for (int k = v.rp[i] + sub; k < v.rp[i + 1]; k += L) {
+        const int col = v.ri[k];
+        a[0] = fmaf(f.rsf[k], f.uc[0][col], a[0]);
+        if (avg) a[1] = fmaf(f.rsf[k], f.uc[1][col], a[1]);
+      }
     }
+    a[0] = lanes_sum(a[0], L);
+    a[1] = lanes_sum(a[1], L);
+    if (i >= v.m || sub != 0) continue;
     const double gu = f.gu[i], gl = f.gl[i], yh = f.yhat[i];
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
@@ -902,7 +968,7 @@ __device__ void bm_evaluate(const LpView& v, const MixView& f, Ctl* c, double* s
 }
 
 // Four blocks per SM, as k_batch_solve.
-__global__ void __launch_bounds__(kBatchThreads, 4) k_batch_solve_mixed(BatchBuffers b) {
+__global__ void __launch_bounds__(kBatchMaxThreads, 2) k_batch_solve_mixed(BatchBuffers b) {
   __shared__ double scratch[kBScratch];
   __shared__ int s_item;
   __shared__ Ctl s_ctl;  // the inner loop's control block
@@ -1149,31 +1215,44 @@ __global__ void __launch_bounds__(kBatchThreads, 4) k_batch_solve_mixed(BatchBuf
   }
 }
 
-// ---- The adjoint ---------------------------------------------------------------------------
+// ---- The adjoint and the polish: square solves with the basis matrix ----------------------
 // At a nondegenerate optimum with basic columns B (strictly inside their bounds), nonbasic
 // columns N at a bound and active rows R (equality rows, and inequality rows whose multiplier
-// is nonzero), the optimum moves, for small changes of the data, along
+// is nonzero), |B| = |R| and the optimum moves, for small changes of the data, along
 //     A_RB dx_B = db_R - A_RN dbound_N,    A_RB' dy_R = dc_B,    dx_N = dbound_N,
 // (y the row multipliers as reported, so dy*/db = 0 and df*/db_R = y_R, df*/dc = x*,
 // df*/dbound_N = d_N, d = c - A'y the reduced costs). For L with upstream gradients g_x, g_y,
 // g_f, with p solving A_RB' p = g_x[B] and q solving A_RB q = g_y[R]:
 //     dL/dc = g_f x* + q (on B),   dL/db_R = p + g_f y_R,
 //     dL/dbound_N = g_x[N] - A_RN' p + g_f d_N,
-// and zero for inactive rows and basic columns' bounds. The two square solves run as
-// Jacobi-preconditioned conjugate gradients on the normal equations, whose operator is a
-// pair of SpMVs with A masked to R x B -- the transposed products of the PDHG step restricted
-// by the projection's Jacobian (1 on B, 0 on N).
+// and zero for inactive rows and basic columns' bounds. Both kernels work in the batch's
+// minimise space (cost sense * c, as src/pdhg/pdhg.cpp:95-111 folds it); the host folds the
+// sense into g_y, g_f and dL/dc, so a maximisation LP is differentiated the same way.
+//
+// The basis matrix is built once per LP in compact form: B and R numbered 0..|B|-1 in index
+// order, A_RB stored as a CSR (lines: active rows; entries: basic-column numbers) and as a
+// CSC (lines: basic columns; entries: active-row numbers). The solves' products then read no
+// masks and gather from vectors of length |B| kept in shared memory. A square solve
+// S u = h (S = A_RB or A_RB') runs as iterative refinement around the normal equations of
+// the second kind: u += F z with (S F) z = h - S u and F = S', by conjugate gradients with
+// the diagonal of S F (the squared lengths of S's lines) as preconditioner. Each pass starts
+// from the current u (the polish from the reported point), so it only removes what is left
+// of the residual; the passes stop when the true residual ||h - S u|| is below the tolerance
+// relative to ||h||.
 struct AdjView {
   const double *gx, *gy;
   double gf;
   double *dc, *dl, *du, *drl, *dru;
-  double *cn[6], *rm[6];
+  double* kw[kAdjVectors];  // compact vectors (|B| entries used)
+  int *bcol, *cpos, *rrow, *rpos;
+  int *kcp, *kci, *krp, *kri;
+  double *kcv, *krv;
   signed char *cs, *rs;
 };
 
 __device__ AdjView make_adj_view(const AdjointBuffers& a, const BatchInstance& I, int li) {
   AdjView w;
-  const long long c = I.col, r = I.row;
+  const long long c = I.col, r = I.row, z = a.knz[li];
   w.gx = a.gx + c;
   w.gy = a.gy + r;
   w.gf = a.gf[li];
@@ -1182,108 +1261,96 @@ __device__ AdjView make_adj_view(const AdjointBuffers& a, const BatchInstance& I
   w.du = a.du + c;
   w.drl = a.drl + r;
   w.dru = a.dru + r;
-  double* const cn[6] = {a.cn0, a.cn1, a.cn2, a.cn3, a.cn4, a.cn5};
-  double* const rm[6] = {a.rm0, a.rm1, a.rm2, a.rm3, a.rm4, a.rm5};
-  for (int k = 0; k < 6; ++k) {
-    w.cn[k] = cn[k] + c;
-    w.rm[k] = rm[k] + r;
-  }
+  for (int k = 0; k < kAdjVectors; ++k) w.kw[k] = a.kw[k] + r;
+  w.bcol = a.bcol + c;
+  w.cpos = a.cpos + c;
+  w.rrow = a.rrow + r;
+  w.rpos = a.rpos + r;
+  w.kcp = a.kcp + c + li;
+  w.krp = a.krp + r + li;
+  w.kci = a.kci + z;
+  w.kri = a.kri + z;
+  w.kcv = a.kcv + z;
+  w.krv = a.krv + z;
   w.cs = a.col_state + c;
   w.rs = a.row_state + r;
   return w;
 }
 
-// t (n) = M' z: t_j = sum over active rows i of A_ij z_i for basic j, 0 elsewhere.
-__device__ void masked_at(const LpView& v, const AdjView& w, const double* z, double* t) {
-  for (int j = threadIdx.x; j < v.n; j += blockDim.x) {
-    double acc = 0.0;
-    if (w.cs[j] == 0) {
-      for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) {
-        const int i = v.ci[k];
-        if (w.rs[i] != 0) acc = fma(v.craw[k], z[i], acc);
-      }
-    }
-    t[j] = acc;
+// block_sum with the totals handed to every thread.
+template <int NV>
+__device__ __forceinline__ void all_sum(double (&v)[NV], double* scratch, double (&out)[NV]) {
+  __shared__ double s_all[NV];
+  block_sum<NV>(v, scratch, out);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; ++q) s_all[q] = out[q];
   }
   __syncthreads();
+#pragma unroll
+  for (int q = 0; q < NV; ++q) out[q] = s_all[q];
 }
 
-// o (m) = M t: o_i = sum over basic columns j of A_ij t_j for active i, 0 elsewhere.
-__device__ void masked_a(const LpView& v, const AdjView& w, const double* t, double* o) {
-  for (int i = threadIdx.x; i < v.m; i += blockDim.x) {
-    double acc = 0.0;
-    if (w.rs[i] != 0) {
-      for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
-        const int j = v.ri[k];
-        if (w.cs[j] == 0) acc = fma(v.rraw[k], t[j], acc);
-      }
+// Exclusive prefix sum of one int per thread over the block (blockDim a multiple of 32);
+// *total receives the block's sum. Every thread calls it.
+__device__ int block_scan(int v, int* total) {
+  __shared__ int s_w[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_w[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int s = lane < nw ? s_w[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
     }
-    o[i] = acc;
+    s_w[lane] = s;
   }
   __syncthreads();
+  const int out = x - v + (warp > 0 ? s_w[warp - 1] : 0);
+  *total = s_w[nw - 1];
+  __syncthreads();
+  return out;
 }
 
-// sum over k < count of a[k] b[k] (mask: entries whose state is nonzero == on), to every thread.
-__device__ double b_dot(const double* a, const double* b, int count, double* scratch) {
-  double acc[1] = {0.0}, out[1];
-  for (int k = threadIdx.x; k < count; k += blockDim.x) acc[0] = fma(a[k], b[k], acc[0]);
-  block_sum<1>(acc, scratch, out);
-  __shared__ double s_dot;
-  if (threadIdx.x == 0) s_dot = out[0];
+// Numbers the k < count with on(k) in index order: list[p] = k and pos[k] = p (-1 for the
+// others). Returns how many (to every thread).
+template <typename On>
+__device__ int compact_set(int count, On on, int* list, int* pos) {
+  int base = 0;
+  for (int start = 0; start < count; start += blockDim.x) {
+    const int k = start + threadIdx.x;
+    const bool f = k < count && on(k);
+    int total = 0;
+    const int e = block_scan(f ? 1 : 0, &total);
+    if (k < count) {
+      pos[k] = f ? base + e : -1;
+      if (f) list[base + e] = k;
+    }
+    base += total;
+  }
   __syncthreads();
-  const double r = s_dot;
-  __syncthreads();
-  return r;
+  return base;
 }
 
-// Preconditioned CG on K x = rhs, K = M M' (ROWS: over the rows, dimension m, entries of
-// inactive rows held at 0) or M' M (over the columns, nonbasic entries held at 0). x, r, z, p,
-// kp and prec have the system's dimension; tmp the other one. prec holds the diagonal of K.
-template <bool ROWS>
-__device__ void b_pcg(const LpView& v, const AdjView& w, const double* rhs, double* x, double* r,
-                      double* z, double* p, double* kp, const double* prec, double* tmp,
-                      double* scratch, int max_it, double tol, int* iterations, double* resid) {
-  const int dim = ROWS ? v.m : v.n;
-  const int T = blockDim.x, t = threadIdx.x;
-  for (int k = t; k < dim; k += T) {
-    const bool on = ROWS ? w.rs[k] != 0 : w.cs[k] == 0;
-    x[k] = 0.0;
-    r[k] = on ? rhs[k] : 0.0;
-    z[k] = r[k] / prec[k];
-    p[k] = z[k];
+// ptr[k] (k < count) holds line k's length on entry and its first entry on exit; ptr[count]
+// receives the total.
+__device__ void starts_from_lengths(int* ptr, int count) {
+  int base = 0;
+  for (int start = 0; start < count; start += blockDim.x) {
+    const int k = start + threadIdx.x;
+    int total = 0;
+    const int e = block_scan(k < count ? ptr[k] : 0, &total);
+    if (k < count) ptr[k] = base + e;
+    base += total;
   }
+  if (threadIdx.x == 0) ptr[count] = base;
   __syncthreads();
-  const double bnorm = sqrt(b_dot(r, r, dim, scratch));
-  double rz = b_dot(r, z, dim, scratch);
-  int it = 0;
-  double rnorm = bnorm;
-  while (bnorm > 0.0 && rnorm > tol * bnorm && it < max_it) {
-    if (ROWS) {
-      masked_at(v, w, p, tmp);
-      masked_a(v, w, tmp, kp);
-    } else {
-      masked_a(v, w, p, tmp);
-      masked_at(v, w, tmp, kp);
-    }
-    const double pkp = b_dot(p, kp, dim, scratch);
-    if (!(pkp > 0.0)) break;
-    const double alpha = rz / pkp;
-    for (int k = t; k < dim; k += T) {
-      x[k] = fma(alpha, p[k], x[k]);
-      r[k] = fma(-alpha, kp[k], r[k]);
-      z[k] = r[k] / prec[k];
-    }
-    __syncthreads();
-    rnorm = sqrt(b_dot(r, r, dim, scratch));
-    const double rz_new = b_dot(r, z, dim, scratch);
-    const double beta = rz_new / rz;
-    rz = rz_new;
-    for (int k = t; k < dim; k += T) p[k] = fma(beta, p[k], z[k]);
-    __syncthreads();
-    ++it;
-  }
-  *iterations = it;
-  *resid = bnorm > 0.0 ? rnorm / bnorm : 0.0;
 }
 
 // The active sets of a reported point (best_x, reduced costs, best_y): column states 0 basic,
@@ -1340,32 +1407,177 @@ __device__ void b_active_sets(const LpView& v, const AdjView& w, double* scratch
   __syncthreads();
 }
 
-// Jacobi diagonals of the two normal-equation operators: M M' (rows) into rm[5], M' M
-// (columns) into cn[0].
-__device__ void b_jacobi(const LpView& v, const AdjView& w) {
+// The compact basis matrix of the active sets in w.cs / w.rs (see above). Returns |B|, with
+// |R| in *nr; the matrix is built only when they are equal.
+__device__ int build_basis(const LpView& v, const AdjView& w, int* nr) {
   const int T = blockDim.x, t = threadIdx.x;
-  for (int i = t; i < v.m; i += T) {
-    double acc = 0.0;
-    if (w.rs[i] != 0) {
-      for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
-        if (w.cs[v.ri[k]] == 0) acc = fma(v.rraw[k], v.rraw[k], acc);
-      }
-    }
-    w.rm[5][i] = acc > 0.0 ? acc : 1.0;
-  }
-  for (int j = t; j < v.n; j += T) {
-    double acc = 0.0;
-    if (w.cs[j] == 0) {
-      for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) {
-        if (w.rs[v.ci[k]] != 0) acc = fma(v.craw[k], v.craw[k], acc);
-      }
-    }
-    w.cn[0][j] = acc > 0.0 ? acc : 1.0;
+  const int nb = compact_set(v.n, [&](int j) { return w.cs[j] == 0; }, w.bcol, w.cpos);
+  const int na = compact_set(v.m, [&](int i) { return w.rs[i] != 0; }, w.rrow, w.rpos);
+  *nr = na;
+  if (nb != na) return nb;
+  for (int p = t; p < nb; p += T) {
+    const int i = w.rrow[p];
+    int len = 0;
+    for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) len += w.cpos[v.ri[k]] >= 0 ? 1 : 0;
+    w.krp[p] = len;
+    const int j = w.bcol[p];
+    len = 0;
+    for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) len += w.rpos[v.ci[k]] >= 0 ? 1 : 0;
+    w.kcp[p] = len;
   }
   __syncthreads();
+  starts_from_lengths(w.krp, nb);
+  starts_from_lengths(w.kcp, nb);
+  for (int p = t; p < nb; p += T) {
+    const int i = w.rrow[p];
+    int o = w.krp[p];
+    for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
+      const int c = w.cpos[v.ri[k]];
+      if (c >= 0) {
+        w.kri[o] = c;
+        w.krv[o] = v.rraw[k];
+        ++o;
+      }
+    }
+    const int j = w.bcol[p];
+    o = w.kcp[p];
+    for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) {
+      const int r = w.rpos[v.ci[k]];
+      if (r >= 0) {
+        w.kci[o] = r;
+        w.kcv[o] = v.craw[k];
+        ++o;
+      }
+    }
+  }
+  __syncthreads();
+  return nb;
 }
 
-__global__ void __launch_bounds__(kBatchThreads) k_batch_adjoint(BatchBuffers b, AdjointBuffers a) {
+// A compact line matrix: line k holds entries ptr[k] .. ptr[k+1]-1 (positions, values).
+struct Lines {
+  const int *ptr, *idx;
+  const double* val;
+};
+
+__device__ __forceinline__ double line_dot(const Lines& L, int k, const double* x) {
+  double s = 0.0;
+  for (int e = L.ptr[k]; e < L.ptr[k + 1]; ++e) s = fma(L.val[e], x[L.idx[e]], s);
+  return s;
+}
+
+// Conjugate gradients on (S F) z = h from z = 0, preconditioned by diag. p and t are the
+// two gathered vectors (shared memory when |B| fits). Stops when ||h - S F z|| (the
+// recurrence's residual) is at most tol ||h||. Returns the iterations.
+__device__ int pcg_sf(const Lines& S, const Lines& F, int nb, const double* h, double* z,
+                      double* r, double* wv, const double* diag, double* p, double* t,
+                      double* scratch, int max_it, double tol) {
+  const int T = blockDim.x, th = threadIdx.x;
+  double a0[2] = {0.0, 0.0};
+  for (int k = th; k < nb; k += T) {
+    const double rk = h[k], wk = rk / diag[k];
+    z[k] = 0.0;
+    r[k] = rk;
+    wv[k] = wk;
+    p[k] = wk;
+    a0[0] = fma(rk, rk, a0[0]);
+    a0[1] = fma(rk, wk, a0[1]);
+  }
+  double s0[2];
+  all_sum<2>(a0, scratch, s0);
+  const double hnorm = sqrt(s0[0]);
+  double rw = s0[1], rnorm = hnorm;
+  int it = 0;
+  while (hnorm > 0.0 && rnorm > tol * hnorm && it < max_it) {
+    double a1[1] = {0.0};
+    for (int k = th; k < nb; k += T) {
+      const double s = line_dot(F, k, p);
+      t[k] = s;
+      a1[0] = fma(s, s, a1[0]);
+    }
+    double pkp[1];
+    all_sum<1>(a1, scratch, pkp);  // also publishes t
+    if (!(pkp[0] > 0.0)) break;
+    const double alpha = rw / pkp[0];
+    double a2[2] = {0.0, 0.0};
+    for (int k = th; k < nb; k += T) {
+      const double s = line_dot(S, k, t);
+      z[k] = fma(alpha, p[k], z[k]);
+      const double rk = fma(-alpha, s, r[k]), wk = rk / diag[k];
+      r[k] = rk;
+      wv[k] = wk;
+      a2[0] = fma(rk, rk, a2[0]);
+      a2[1] = fma(rk, wk, a2[1]);
+    }
+    double s2[2];
+    all_sum<2>(a2, scratch, s2);  // every thread is done reading p and t
+    rnorm = sqrt(s2[0]);
+    const double beta = s2[1] / rw;
+    rw = s2[1];
+    for (int k = th; k < nb; k += T) p[k] = fma(beta, p[k], wv[k]);
+    __syncthreads();
+    ++it;
+  }
+  return it;
+}
+
+constexpr int kRefinePasses = 3;
+
+// S u = h (F = S') by refinement passes around pcg_sf; u holds the starting point on entry
+// and the solution on exit, w.kw[2..6] are used as scratch. Returns the conjugate-gradient
+// iterations; *rel receives ||h - S u|| / ||h|| at the end (0 when h = 0).
+__device__ int solve_square(const Lines& S, const Lines& F, int nb, const double* h, double* u,
+                            const AdjView& w, double* p, double* t, double* scratch, int max_it,
+                            double tol, double* rel) {
+  const int T = blockDim.x, th = threadIdx.x;
+  double* const res = w.kw[2];
+  double* const z = w.kw[3];
+  double* const r = w.kw[4];
+  double* const wv = w.kw[5];
+  double* const diag = w.kw[6];
+  double a0[1] = {0.0};
+  for (int k = th; k < nb; k += T) {
+    double d = 0.0;
+    for (int e = S.ptr[k]; e < S.ptr[k + 1]; ++e) d = fma(S.val[e], S.val[e], d);
+    diag[k] = d > 0.0 ? d : 1.0;
+    a0[0] = fma(h[k], h[k], a0[0]);
+  }
+  double hs[1];
+  all_sum<1>(a0, scratch, hs);
+  const double hnorm = sqrt(hs[0]);
+  int its = 0;
+  for (int pass = 0;; ++pass) {
+    double a1[1] = {0.0};
+    for (int k = th; k < nb; k += T) {
+      const double rk = h[k] - line_dot(S, k, u);
+      res[k] = rk;
+      a1[0] = fma(rk, rk, a1[0]);
+    }
+    double rs[1];
+    all_sum<1>(a1, scratch, rs);
+    const double rnorm = sqrt(rs[0]);
+    *rel = hnorm > 0.0 ? rnorm / hnorm : 0.0;
+    if (*rel <= tol || pass == kRefinePasses) break;
+    its += pcg_sf(S, F, nb, res, z, r, wv, diag, p, t, scratch, max_it, tol * hnorm / rnorm);
+    for (int k = th; k < nb; k += T) u[k] += line_dot(F, k, z);
+    __syncthreads();
+  }
+  return its;
+}
+
+// The two gathered vectors of a solve: shared memory when |B| fits, else w.kw[7], w.kw[8].
+struct Gathered {
+  double *p, *t;
+};
+
+__device__ Gathered gathered(const AdjointBuffers& a, const AdjView& w, double* s_vec, int nb) {
+  if (nb <= a.smem_vec) return Gathered{s_vec, s_vec + a.smem_vec};
+  return Gathered{w.kw[7], w.kw[8]};
+}
+
+__global__ void __launch_bounds__(kAdjThreads, 2) k_batch_adjoint(BatchBuffers b,
+                                                                   AdjointBuffers a) {
+  extern __shared__ double s_vec[];
   __shared__ double scratch[kBScratch];
   __shared__ int s_item;
   __shared__ LpView s_view;
@@ -1385,43 +1597,59 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_adjoint(BatchBuffers b,
     const AdjView& w = s_adj;
     int nb = 0, nr = 0;
     b_active_sets(v, w, scratch, &nb, &nr);
-    b_jacobi(v, w);
-    // The reported multipliers are -y (minimisation) and satisfy A_RB' y_R = c_B, so
-    // q = A_RB^-1 g_y. Solve 1: (M M') z = g_y[R] over the rows, q = M' z.
+    nb = build_basis(v, w, &nr);
     int it1 = 0, it2 = 0;
     double res1 = 0.0, res2 = 0.0;
-    b_pcg<true>(v, w, w.gy, w.rm[0], w.rm[1], w.rm[2], w.rm[3], w.rm[4], w.rm[5], w.cn[1],
-                scratch, a.max_iterations, a.cg_tolerance, &it1, &res1);
-    masked_at(v, w, w.rm[0], w.cn[1]);  // q (on B)
-    for (int j = t; j < v.n; j += T) {
-      const double x = v.best_x[j];
-      w.dc[j] = fma(w.gf, x, w.cs[j] == 0 ? w.cn[1][j] : 0.0);
-    }
-    __syncthreads();
-    // Solve 2: (M' M) z' = g_x[B] over the columns, p = M z'.
-    b_pcg<false>(v, w, w.gx, w.cn[1], w.cn[2], w.cn[3], w.cn[4], w.cn[5], w.cn[0], w.rm[1],
-                 scratch, a.max_iterations, a.cg_tolerance, &it2, &res2);
-    masked_a(v, w, w.cn[1], w.rm[2]);  // p (on R)
-    for (int i = t; i < v.m; i += T) {
-      const signed char st = w.rs[i];
-      const double yrep = -v.best_y[i];  // the reported multiplier
-      const double g = st != 0 ? w.rm[2][i] + w.gf * yrep : 0.0;
-      w.drl[i] = st == 1 ? g : 0.0;
-      w.dru[i] = st == 2 ? g : 0.0;
-    }
-    for (int j = t; j < v.n; j += T) {
-      const signed char st = w.cs[j];
-      double g = 0.0;
-      if (st != 0) {
-        double atp = 0.0;
-        for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) {
-          const int i = v.ci[k];
-          if (w.rs[i] != 0) atp = fma(v.craw[k], w.rm[2][i], atp);
-        }
-        g = w.gx[j] - atp + w.gf * v.reduced[j];
+    if (nb != nr) {
+      for (int j = t; j < v.n; j += T) w.dc[j] = w.dl[j] = w.du[j] = 0.0;
+      for (int i = t; i < v.m; i += T) w.drl[i] = w.dru[i] = 0.0;
+    } else {
+      const Gathered g = gathered(a, w, s_vec, nb);
+      const Lines csr{w.krp, w.kri, w.krv}, csc{w.kcp, w.kci, w.kcv};
+      double* const h = w.kw[0];
+      double* const u = w.kw[1];
+      // q: A_RB q = g_y[R] (the reported multipliers are -y and satisfy A_RB' y_R = c_B).
+      for (int k = t; k < nb; k += T) {
+        h[k] = w.gy[w.rrow[k]];
+        u[k] = 0.0;
       }
-      w.dl[j] = st == 1 ? g : 0.0;
-      w.du[j] = st == 2 ? g : 0.0;
+      __syncthreads();
+      it1 = solve_square(csr, csc, nb, h, u, w, g.p, g.t, scratch, a.max_iterations,
+                         a.cg_tolerance, &res1);
+      for (int j = t; j < v.n; j += T) {
+        const int q = w.cpos[j];
+        w.dc[j] = fma(w.gf, v.best_x[j], q >= 0 ? u[q] : 0.0);
+      }
+      __syncthreads();
+      // p: A_RB' p = g_x[B].
+      for (int k = t; k < nb; k += T) {
+        h[k] = w.gx[w.bcol[k]];
+        u[k] = 0.0;
+      }
+      __syncthreads();
+      it2 = solve_square(csc, csr, nb, h, u, w, g.p, g.t, scratch, a.max_iterations,
+                         a.cg_tolerance, &res2);
+      for (int i = t; i < v.m; i += T) {
+        const signed char st = w.rs[i];
+        const double yrep = -v.best_y[i];  // the reported multiplier
+        const double gi = st != 0 ? u[w.rpos[i]] + w.gf * yrep : 0.0;
+        w.drl[i] = st == 1 ? gi : 0.0;
+        w.dru[i] = st == 2 ? gi : 0.0;
+      }
+      for (int j = t; j < v.n; j += T) {
+        const signed char st = w.cs[j];
+        double gj = 0.0;
+        if (st != 0) {
+          double atp = 0.0;
+          for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) {
+            const int q = w.rpos[v.ci[k]];
+            if (q >= 0) atp = fma(v.craw[k], u[q], atp);
+          }
+          gj = w.gx[j] - atp + w.gf * v.reduced[j];
+        }
+        w.dl[j] = st == 1 ? gj : 0.0;
+        w.du[j] = st == 2 ? gj : 0.0;
+      }
     }
     if (t == 0) {
       AdjointOutcome o;
@@ -1431,11 +1659,9 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_adjoint(BatchBuffers b,
       o.iterations[1] = it2;
       o.residual[0] = res1;
       o.residual[1] = res2;
-      o.status = I.sense < 0.0 ? 3
-                 : nb != nr
-                     ? 1
-                     : ((res1 > 100.0 * a.cg_tolerance || res2 > 100.0 * a.cg_tolerance) ? 2
-                                                                                        : 0);
+      o.status = nb != nr ? 1
+                 : (res1 > 100.0 * a.cg_tolerance || res2 > 100.0 * a.cg_tolerance) ? 2
+                                                                                    : 0;
       a.outcome[li] = o;
     }
   }
@@ -1443,13 +1669,16 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_adjoint(BatchBuffers b,
 
 // Active-set polish of a batch solve (the PDHG -> basis hand-off): at the reported point's
 // active sets, x_B solves A_RB x_B = b_R - A_RN x_N (x_N at its bounds) and the multipliers
-// solve A_RB' y_R = c_B (y = 0 off R), both by the masked conjugate gradients above. The
-// polished point replaces the reported one when the optimum is nondegenerate (|B| = |R|) and
-// the point is primal and dual feasible within 1e-9 (relative); the final evaluation then
-// runs on it and the outcome's residuals, objective and status are rewritten.
-// AdjointOutcome.status: 0 polished, 1 degenerate, 2 CG not converged, 3 maximisation,
-// 4 not a converged solve, 5 the polished point failed the feasibility checks.
-__global__ void __launch_bounds__(kBatchThreads) k_batch_polish(BatchBuffers b, AdjointBuffers a) {
+// solve A_RB' y_R = c_B (y = 0 off R), both by the square solves above, started from the
+// reported point. The polished point replaces the reported one when the optimum is
+// nondegenerate (|B| = |R|) and the point is primal and dual feasible within 1e-9
+// (relative); the final evaluation then runs on it and the outcome's residuals, objective
+// and status are rewritten.
+// AdjointOutcome.status: 0 polished, 1 degenerate, 2 a solve did not converge, 4 not a
+// converged solve, 5 the polished point failed the feasibility checks.
+__global__ void __launch_bounds__(kAdjThreads, 2) k_batch_polish(BatchBuffers b,
+                                                                  AdjointBuffers a) {
+  extern __shared__ double s_vec[];
   __shared__ double scratch[kBScratch];
   __shared__ int s_item;
   __shared__ LpView s_view;
@@ -1472,77 +1701,56 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_polish(BatchBuffers b, 
     int nb = 0, nr = 0;
     b_active_sets(v, w, scratch, &nb, &nr);
     AdjointOutcome o{};
-    o.basic_cols = nb;
-    o.active_rows = nr;
     const bool solved = before.status == SANKHYA_GB300_OPTIMAL ||
                         before.status == SANKHYA_GB300_FEASIBLE;
-    if (I.sense < 0.0 || nb != nr || !solved) {
+    if (solved) nb = build_basis(v, w, &nr);
+    o.basic_cols = nb;
+    o.active_rows = nr;
+    if (nb != nr || !solved) {
       if (t == 0) {
-        o.status = I.sense < 0.0 ? 3 : (!solved ? 4 : 1);
+        o.status = !solved ? 4 : 1;
         a.outcome[li] = o;
       }
       continue;
     }
-    b_jacobi(v, w);
-    // Right-hand sides: rm[4] = b_R - A_RN x_N over the rows; cn[2] = c_B over the columns.
-    const auto row_rhs = [&]() {
-      for (int i = t; i < v.m; i += T) {
-        const signed char st = w.rs[i];
-        double r = 0.0;
-        if (st != 0) {
-          r = st == 1 ? v.rl[i] : v.ru[i];
-          for (int k = v.rp[i]; k < v.rp[i + 1]; ++k) {
-            const signed char cj = w.cs[v.ri[k]];
-            if (cj != 0) r -= v.rraw[k] * (cj == 1 ? v.l[v.ri[k]] : v.u[v.ri[k]]);
-          }
-        }
-        w.rm[4][i] = r;
+    const Gathered g = gathered(a, w, s_vec, nb);
+    const Lines csr{w.krp, w.kri, w.krv}, csc{w.kcp, w.kci, w.kcv};
+    double* const h = w.kw[0];
+    double* const u = w.kw[1];
+    // x_B from b_R - A_RN x_N, starting at the reported x_B.
+    for (int k = t; k < nb; k += T) {
+      const int i = w.rrow[k];
+      double r = w.rs[i] == 1 ? v.rl[i] : v.ru[i];
+      for (int e = v.rp[i]; e < v.rp[i + 1]; ++e) {
+        const signed char cj = w.cs[v.ri[e]];
+        if (cj != 0) r -= v.rraw[e] * (cj == 1 ? v.l[v.ri[e]] : v.u[v.ri[e]]);
       }
-    };
-    const auto col_rhs = [&]() {
-      for (int j = t; j < v.n; j += T) w.cn[2][j] = w.cs[j] == 0 ? v.cost[j] : 0.0;
-    };
-    row_rhs();
-    col_rhs();
+      h[k] = r;
+      u[k] = v.best_x[w.bcol[k]];
+    }
     __syncthreads();
-    int it1 = 0, it2 = 0, itr = 0;
-    double res1 = 0.0, res2 = 0.0, resr = 0.0;
-    // x_B = M' z, (M M') z = rhs. The right-hand side doubles as the operator's output
-    // buffer: b_pcg reads it only before the first product.
-    b_pcg<true>(v, w, w.rm[4], w.rm[0], w.rm[1], w.rm[2], w.rm[3], w.rm[4], w.rm[5], w.cn[1],
-                scratch, a.max_iterations, a.cg_tolerance, &it1, &res1);
-    masked_at(v, w, w.rm[0], v.xu[1]);  // x_B (0 off B)
-    // One pass of iterative refinement: the residual of M x_B = rhs, formed in FP64 against
-    // the rebuilt right-hand side, solved the same way and added. The normal equations square
-    // the basis's condition number, so the first solve alone leaves x_B with an error of
-    // about cond(M)^2 times the CG tolerance; the pass takes that down to the rounding of the
-    // residual itself.
-    row_rhs();
-    masked_a(v, w, v.xu[1], w.rm[1]);
-    for (int i = t; i < v.m; i += T) w.rm[4][i] -= w.rm[1][i];
+    int it1 = 0, it2 = 0;
+    double res1 = 0.0, res2 = 0.0;
+    it1 = solve_square(csr, csc, nb, h, u, w, g.p, g.t, scratch, a.max_iterations,
+                       a.cg_tolerance, &res1);
+    for (int j = t; j < v.n; j += T) {
+      const signed char st = w.cs[j];
+      v.xu[1][j] = st == 0 ? u[w.cpos[j]] : (st == 1 ? v.l[j] : v.u[j]);
+    }
     __syncthreads();
-    b_pcg<true>(v, w, w.rm[4], w.rm[0], w.rm[1], w.rm[2], w.rm[3], w.rm[4], w.rm[5], w.cn[1],
-                scratch, a.max_iterations, a.cg_tolerance, &itr, &resr);
-    masked_at(v, w, w.rm[0], w.cn[1]);
-    for (int j = t; j < v.n; j += T) v.xu[1][j] += w.cn[1][j];
+    // y_R from c_B, starting at the reported multipliers (-y in the solver's sign).
+    for (int k = t; k < nb; k += T) {
+      h[k] = v.cost[w.bcol[k]];
+      u[k] = -v.best_y[w.rrow[k]];
+    }
     __syncthreads();
-    it1 += itr;
-    // y_R = M z', (M' M) z' = c_B.
-    b_pcg<false>(v, w, w.cn[2], w.cn[1], w.cn[3], w.cn[4], w.cn[5], w.cn[2], w.cn[0], w.rm[1],
-                 scratch, a.max_iterations, a.cg_tolerance, &it2, &res2);
-    masked_a(v, w, w.cn[1], w.rm[2]);  // the reported multipliers y_R (0 off R)
-    // The same refinement pass for y_R against c_B.
-    col_rhs();
-    masked_at(v, w, w.rm[2], w.cn[3]);
-    for (int j = t; j < v.n; j += T) w.cn[2][j] -= w.cn[3][j];
-    __syncthreads();
-    b_pcg<false>(v, w, w.cn[2], w.cn[1], w.cn[3], w.cn[4], w.cn[5], w.cn[2], w.cn[0], w.rm[1],
-                 scratch, a.max_iterations, a.cg_tolerance, &itr, &resr);
-    masked_a(v, w, w.cn[1], w.rm[1]);
-    for (int i = t; i < v.m; i += T) w.rm[2][i] += w.rm[1][i];
-    __syncthreads();
-    it2 += itr;
-    // The polished point into xu[1] (columns) and yu[1] (the solver's sign: -y), then checks.
+    it2 = solve_square(csc, csr, nb, h, u, w, g.p, g.t, scratch, a.max_iterations,
+                       a.cg_tolerance, &res2);
+    for (int i = t; i < v.m; i += T) {
+      const int q = w.rpos[i];
+      v.yu[1][i] = q >= 0 ? -u[q] : 0.0;  // the solver's sign
+    }
+    // The checks: bounds of x_B, signs of the nonbasic reduced costs, inactive rows' sides.
     double bad[1] = {0.0};
     double cmax[1] = {0.0};
     for (int j = t; j < v.n; j += T) cmax[0] = dmax(cmax[0], fabs(v.cost[j]));
@@ -1554,7 +1762,7 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_polish(BatchBuffers b, 
     for (int j = t; j < v.n; j += T) {
       const signed char st = w.cs[j];
       const double lj = v.l[j], uj = v.u[j];
-      double x = st == 0 ? v.xu[1][j] : (st == 1 ? lj : uj);
+      double x = v.xu[1][j];
       if (st == 0) {
         const double tol = 1e-9 * dmax(1.0, dmax(fabs(lj), fabs(uj)));
         if ((finite_bound(lj) && x < lj - tol) || (finite_bound(uj) && x > uj + tol)) {
@@ -1563,14 +1771,15 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_polish(BatchBuffers b, 
         x = clamp_box(x, finite_bound(lj) ? lj : -HUGE_VAL, finite_bound(uj) ? uj : HUGE_VAL);
       } else {
         double aty = 0.0;
-        for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) aty = fma(v.craw[k], w.rm[2][v.ci[k]], aty);
+        for (int k = v.cp[j]; k < v.cp[j + 1]; ++k) {
+          aty = fma(v.craw[k], -v.yu[1][v.ci[k]], aty);
+        }
         const double d = v.cost[j] - aty;
         const double tol = 1e-9 * s_cmax;
         if (lj != uj && ((st == 1 && d < -tol) || (st == 2 && d > tol))) bad[0] += 1.0;
       }
       v.xu[1][j] = x;
     }
-    for (int i = t; i < v.m; i += T) v.yu[1][i] = -w.rm[2][i];
     __syncthreads();
     for (int i = t; i < v.m; i += T) {
       if (w.rs[i] != 0 || v.rl[i] == v.ru[i]) continue;
@@ -1610,7 +1819,8 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_polish(BatchBuffers b, 
         out.status = verifiable ? SANKHYA_GB300_OPTIMAL : SANKHYA_GB300_FEASIBLE;
         out.final_residuals = f;
         out.objective = I.offset + s_ctl.model_objective;
-        out.dual_bound = verifiable ? I.sense * f.dual_objective + I.offset : -HUGE_VAL;
+        out.dual_bound = verifiable ? I.sense * f.dual_objective + I.offset
+                                    : (I.sense < 0.0 ? HUGE_VAL : -HUGE_VAL);
         b.outcome[li] = out;
       }
     }
@@ -1627,19 +1837,54 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_polish(BatchBuffers b, 
 
 }  // namespace
 
+namespace {
+size_t adjoint_smem_bytes(int smem_vec) {
+  return 2 * static_cast<size_t>(smem_vec) * sizeof(double);
+}
+}  // namespace
+
 void launch_batch_adjoint(const BatchBuffers& b, const AdjointBuffers& a, int grid,
                           cudaStream_t s) {
-  k_batch_adjoint<<<grid, kBatchThreads, 0, s>>>(b, a);
+  const size_t bytes = adjoint_smem_bytes(a.smem_vec);
+  // A failure here stays the last error, which the caller's launch check reports.
+  cudaFuncSetAttribute(k_batch_adjoint, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       static_cast<int>(bytes));
+  k_batch_adjoint<<<grid, kAdjThreads, bytes, s>>>(b, a);
 }
 
 void launch_batch_polish(const BatchBuffers& b, const AdjointBuffers& a, int grid,
                          cudaStream_t s) {
-  k_batch_polish<<<grid, kBatchThreads, 0, s>>>(b, a);
+  const size_t bytes = adjoint_smem_bytes(a.smem_vec);
+  // A failure here stays the last error, which the caller's launch check reports.
+  cudaFuncSetAttribute(k_batch_polish, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       static_cast<int>(bytes));
+  k_batch_polish<<<grid, kAdjThreads, bytes, s>>>(b, a);
 }
 
-int batch_blocks_per_sm() {
+int adjoint_blocks_per_sm(int smem_vec) {
+  const size_t bytes = adjoint_smem_bytes(smem_vec);
+  int per_sm = 1 << 30;
+  for (const void* f : {reinterpret_cast<const void*>(k_batch_adjoint),
+                        reinterpret_cast<const void*>(k_batch_polish)}) {
+    int n = 0;
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(bytes)) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, f, kAdjThreads, bytes) !=
+            cudaSuccess) {
+      cudaGetLastError();
+      n = 1;
+    }
+    per_sm = std::min(per_sm, n);
+  }
+  return per_sm > 0 ? per_sm : 1;
+}
+
+int batch_blocks_per_sm(int threads) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_solve, kBatchThreads, 0);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_solve, threads, 0) !=
+      cudaSuccess) {
+    cudaGetLastError();
+  }
   return per_sm > 0 ? per_sm : 1;
 }
 
@@ -1647,17 +1892,20 @@ void launch_batch_scaling(const BatchBuffers& b, int grid, cudaStream_t s) {
   k_batch_scale<<<grid, kBatchThreads, 0, s>>>(b);
 }
 
-void launch_batch_solve(const BatchBuffers& b, int grid, cudaStream_t s) {
-  k_batch_solve<<<grid, kBatchThreads, 0, s>>>(b);
+void launch_batch_solve(const BatchBuffers& b, int grid, int threads, cudaStream_t s) {
+  k_batch_solve<<<grid, threads, 0, s>>>(b);
 }
 
-void launch_batch_solve_mixed(const BatchBuffers& b, int grid, cudaStream_t s) {
-  k_batch_solve_mixed<<<grid, kBatchThreads, 0, s>>>(b);
+void launch_batch_solve_mixed(const BatchBuffers& b, int grid, int threads, cudaStream_t s) {
+  k_batch_solve_mixed<<<grid, threads, 0, s>>>(b);
 }
 
-int batch_mixed_blocks_per_sm() {
+int batch_mixed_blocks_per_sm(int threads) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_solve_mixed, kBatchThreads, 0);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_solve_mixed, threads, 0) !=
+      cudaSuccess) {
+    cudaGetLastError();
+  }
   return per_sm > 0 ? per_sm : 1;
 }
 

@@ -215,11 +215,40 @@ SGB_API int sankhya_gb300_batch_solve(sankhya_gb300_batch* batch,
   return guarded([&] { batch->engine->solve(*params, items, device_seconds); });
 }
 
+SGB_API int sankhya_gb300_batch_schedule(sankhya_gb300_batch* batch, int32_t lanes,
+                                         int32_t threads) {
+  if (batch == nullptr) return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null batch");
+  return guarded([&] { batch->engine->set_schedule(lanes, threads); });
+}
+
+SGB_API int sankhya_gb300_batch_last_schedule(sankhya_gb300_batch* batch, int32_t* lanes,
+                                              int32_t* threads, double* tune_seconds) {
+  if (batch == nullptr) return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null batch");
+  return guarded([&] {
+    int l = 0, t = 0;
+    batch->engine->last_schedule(&l, &t, tune_seconds);
+    if (lanes != nullptr) *lanes = l;
+    if (threads != nullptr) *threads = t;
+  });
+}
+
 SGB_API int sankhya_gb300_batch_solution(sankhya_gb300_batch* batch, int32_t index,
                                          double* col_value, double* col_dual,
                                          double* row_dual) {
   if (batch == nullptr) return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null batch");
   return guarded([&] { batch->engine->solution(index, col_value, col_dual, row_dual); });
+}
+
+SGB_API int sankhya_gb300_batch_set_point(sankhya_gb300_batch* batch, int32_t index,
+                                          const double* col_value, const double* col_dual,
+                                          const double* row_dual) {
+  if (batch == nullptr) return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null batch");
+  return guarded([&] { batch->engine->set_point(index, col_value, col_dual, row_dual); });
+}
+
+SGB_API int sankhya_gb300_batch_ray(sankhya_gb300_batch* batch, int32_t index, double* ray) {
+  if (batch == nullptr) return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null batch");
+  return guarded([&] { batch->engine->ray(index, ray); });
 }
 
 SGB_API int sankhya_gb300_batch_adjoint(sankhya_gb300_batch* batch,

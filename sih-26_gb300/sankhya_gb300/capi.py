@@ -105,6 +105,8 @@ EXPORTS = [
     "sankhya_gb300_pdhg_spmv_noalloc", "sankhya_gb300_batch_create",
     "sankhya_gb300_batch_destroy", "sankhya_gb300_batch_load", "sankhya_gb300_batch_solve",
     "sankhya_gb300_batch_solution", "sankhya_gb300_batch_adjoint", "sankhya_gb300_batch_polish",
+    "sankhya_gb300_batch_schedule", "sankhya_gb300_batch_last_schedule",
+    "sankhya_gb300_batch_ray", "sankhya_gb300_batch_set_point",
 ]
 
 _lib = None
@@ -151,6 +153,13 @@ def load_library():
                                                   ctypes.POINTER(CBatchItem), _D]
         lib.sankhya_gb300_batch_solution.argtypes = [ctypes.c_void_p, ctypes.c_int32, _D, _D,
                                                      _D]
+        lib.sankhya_gb300_batch_ray.argtypes = [ctypes.c_void_p, ctypes.c_int32, _D]
+        lib.sankhya_gb300_batch_set_point.argtypes = [ctypes.c_void_p, ctypes.c_int32, _D, _D,
+                                                      _D]
+        lib.sankhya_gb300_batch_schedule.argtypes = [ctypes.c_void_p, ctypes.c_int32,
+                                                     ctypes.c_int32]
+        lib.sankhya_gb300_batch_last_schedule.argtypes = [
+            ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32), _D]
         _PP = ctypes.POINTER(ctypes.POINTER(ctypes.c_double))
         lib.sankhya_gb300_batch_adjoint.argtypes = [ctypes.c_void_p, _PP, _PP, _D, _PP, _PP, _PP,
                                                     _PP, _PP, ctypes.POINTER(CAdjointInfo)]
@@ -393,6 +402,38 @@ class BatchEngine:
                                  it.final_residuals.as_dict(), it.spectral_norm,
                                  it.farkas_value, it.refinements))
         return out, float(sec[0])
+
+    def set_schedule(self, lanes: int = 0, threads: int = 0):
+        """The schedule of the next solves: lanes per row or column and threads per LP;
+        0, 0 (the default) autotunes every solve (sankhya_gb300_batch_schedule)."""
+        _check(self._lib.sankhya_gb300_batch_schedule(self._h, lanes, threads))
+
+    def last_schedule(self):
+        """(lanes, threads, autotuning seconds) of the last solve."""
+        lanes, threads = ctypes.c_int32(), ctypes.c_int32()
+        sec = np.zeros(1)
+        _check(self._lib.sankhya_gb300_batch_last_schedule(self._h, ctypes.byref(lanes),
+                                                           ctypes.byref(threads), _ptr(sec)))
+        return int(lanes.value), int(threads.value), float(sec[0])
+
+    def ray(self, index: int):
+        """The dual direction LP `index` was reported infeasible by (sankhya_gb300_batch_ray);
+        certify.farkas_share checks it."""
+        y = np.zeros(self._lps[index].rows)
+        _check(self._lib.sankhya_gb300_batch_ray(self._h, index, _ptr(y)))
+        return y
+
+    def set_point(self, index: int, col_value, col_dual, row_dual):
+        """Replace LP `index`'s reported point (as solution() returns it): the polish's warm
+        start (sankhya_gb300_batch_set_point)."""
+        lp = self._lps[index]
+        x = np.ascontiguousarray(col_value, dtype=np.float64)
+        d = np.ascontiguousarray(col_dual, dtype=np.float64)
+        y = np.ascontiguousarray(row_dual, dtype=np.float64)
+        if x.shape != (lp.cols,) or d.shape != (lp.cols,) or y.shape != (lp.rows,):
+            raise ValueError("a point of the LP's shape is expected")
+        _check(self._lib.sankhya_gb300_batch_set_point(self._h, index, _ptr(x), _ptr(d),
+                                                       _ptr(y)))
 
     def solution(self, index: int):
         lp = self._lps[index]

@@ -27,6 +27,7 @@ class _Item:
         self.objective = objective
         self.iterations = 1
         self.status_name = "optimal"
+        self.converged = True
 
 
 class ExactBatchEngine:
@@ -73,6 +74,11 @@ class ExactBatchEngine:
     def solution(self, k):
         x, y = self.sol[k]
         return x, None, y
+
+    def set_point(self, k, x, d, y):
+        """The exact polish below re-solves each LP at its planted basis, so the warm start
+        only has to be of the LP's shape."""
+        assert x.shape == (self.lps[k].cols,) and y.shape == (self.lps[k].rows,)
 
     def adjoint(self, gx, gy, gf):
         out = []

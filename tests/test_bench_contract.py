@@ -85,6 +85,12 @@ def _batch_engine():
                 return super().solve(**kw)
             return [_Item(0.0) for _ in self.lps], 0.5
 
+        def set_schedule(self, lanes=0, threads=0):
+            self.schedule = (lanes, threads)
+
+        def last_schedule(self):
+            return 1, 256, 0.0
+
     return StandInBatchEngine
 
 
@@ -102,6 +108,8 @@ def _run(monkeypatch, argv):
     monkeypatch.setattr(bench, "ZIPF_SHAPE", (300, 600, 3000))
     monkeypatch.setattr(bench, "REFERENCE_SAMPLE_ITERATIONS", 8)
     monkeypatch.setattr(bench, "CPU_TIME_LIMIT", 0.5)
+    monkeypatch.setattr(bench, "reference_gpu_section",
+                        lambda: {"ran_on_gpu": False, "s_per_iteration": 0.0})
     full_adjoint = bench.adjoint_section
     monkeypatch.setattr(bench, "adjoint_section",
                         lambda device: full_adjoint(device, lps_count=3, shape=(60, 120),
@@ -120,7 +128,7 @@ def test_default_line(monkeypatch):
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
                 "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
                 "roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "fp64",
-                "batched", "adjoint"):
+                "batched", "adjoint", "reference_gpu"):
         assert key in line, key
     assert line["n_gpus"] == 1 and line["steps"] == 1 and line["warmup"] == 3
     assert line["higher_is_better"] is False and line["unit"] == "s"

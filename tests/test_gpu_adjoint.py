@@ -141,6 +141,89 @@ def test_torch_autograd_function():
         assert close(lo.grad[k].numpy(), dl) and close(up.grad[k].numpy(), du)
 
 
+def test_adjoint_of_a_maximisation_lp():
+    """max (-c)'x over the planted LP's feasible set has the same optimum x*; its reported
+    row duals are -y* and its objective -f*. With L' = w'x* + v'y' + f' the chain rule gives
+    dL'/dc' = -(the minimisation's dL/dc for upstream w, -v, -1), and every other gradient
+    equal to the minimisation's for that upstream."""
+    from sankhya_gb300.model import LP
+
+    lp = lpgen.planted_nondegenerate(60, 120, 5, seed=4242)
+    mx = LP(lp.rows, lp.cols, lp.col_starts, lp.row_index, lp.values, -lp.col_cost,
+            lp.col_lower, lp.col_upper, lp.row_lower, lp.row_upper, sense=-1.0)
+    rng = np.random.default_rng(11)
+    w, v = rng.standard_normal(lp.cols), rng.standard_normal(lp.rows)
+    with capi.BatchEngine(0) as eng:
+        eng.load([mx])
+        items, _ = eng.solve(tolerance=1e-7, stop_rule="relative", iteration_limit=1000000)
+        assert items[0].status_name in ("optimal", "feasible")
+        _, info = eng.polish()
+        assert info[0]["status"] == 0, info
+        x, _, y = eng.solution(0)
+        assert np.allclose(x, lp.x0, rtol=0, atol=1e-9)
+        assert np.allclose(y, -lp.lam, rtol=0, atol=1e-9)
+        r = eng.adjoint([w], [v], [1.0])[0]
+    assert r["status"] == 0, r
+    dc, db, dl, du = basis_gradients(lp, w, -v, -1.0)
+    assert close(r["dc"], -dc)
+    assert close(r["drl"] + r["dru"], db)
+    assert close(r["dl"], dl) and close(r["du"], du)
+
+
+def test_polish_from_a_set_point_matches_the_adjoint_at_step_1e6():
+    """Perturbed copies of a planted LP (costs and right-hand sides moved by +-1e-6) are
+    solved, then polished from the base LP's vertex (sankhya_gb300_batch_set_point): each
+    lands on its own vertex (the dense solve at the planted basis), and the central
+    differences of L = g_x'x* + g_y'y* + f* match the adjoint to 1e-5 relative."""
+    from sankhya_gb300.model import LP
+
+    lp = lpgen.planted_nondegenerate(80, 160, 5, seed=31)
+    rng = np.random.default_rng(8)
+    gx, gy = rng.standard_normal(lp.cols), rng.standard_normal(lp.rows)
+    h = 1e-6
+    with capi.BatchEngine(0) as eng:
+        eng.load([lp])
+        eng.solve(tolerance=1e-7, stop_rule="relative", iteration_limit=1000000)
+        eng.polish()
+        base = eng.solution(0)
+        r = eng.adjoint([gx], [gy], [1.0])[0]
+    assert r["status"] == 0, r
+    picks = [("c", int(j)) for j in rng.choice(lp.cols, 4, replace=False)]
+    picks += [("b", int(i)) for i in rng.choice(lp.rows, 4, replace=False)]
+    pert = []
+    for fam, j in picks:
+        for sign in (1.0, -1.0):
+            c, rl = lp.col_cost.copy(), lp.row_lower.copy()
+            if fam == "c":
+                c[j] += sign * h
+            else:
+                rl[j] += sign * h
+            pert.append(LP(lp.rows, lp.cols, lp.col_starts, lp.row_index, lp.values, c,
+                           lp.col_lower, lp.col_upper, rl, rl.copy()))
+    A = dense(lp)
+    B = (lp.x0 > lp.col_lower) & (lp.x0 < lp.col_upper)
+    with capi.BatchEngine(0) as eng:
+        eng.load(pert)
+        eng.solve(tolerance=1e-4, stop_rule="relative", iteration_limit=1000000)
+        for q in range(len(pert)):
+            eng.set_point(q, *base)
+        _, info = eng.polish()
+        assert all(i["status"] == 0 for i in info), info
+        sols = [eng.solution(q) for q in range(len(pert))]
+    for q, p in enumerate(pert):
+        x = np.where(lp.x0 <= lp.col_lower, lp.col_lower, lp.col_upper)
+        x[B] = np.linalg.solve(A[:, B], p.row_lower - A[:, ~B] @ x[~B])
+        assert np.allclose(sols[q][0], x, rtol=0, atol=1e-10), q
+    for t, (fam, j) in enumerate(picks):
+        (xp, _, yp), (xm, _, ym) = sols[2 * t], sols[2 * t + 1]
+        dl = (gx + lp.col_cost) @ (xp - xm) + gy @ (yp - ym)
+        if fam == "c":
+            dl += h * (xp[j] + xm[j])
+        fd = dl / (2 * h)
+        got = r["dc"][j] if fam == "c" else r["drl"][j] + r["dru"][j]
+        assert abs(got - fd) <= 1e-5 * max(1.0, abs(fd)), (fam, j, got, fd)
+
+
 def test_polish_leaves_degenerate_and_infeasible_lps_alone():
     degenerate = lpgen.planted_uniform(40, 80, 5, seed=3)  # more interior columns than rows
     with capi.BatchEngine(0) as eng:

@@ -9,7 +9,7 @@ objective; infeasible ones must be reported infeasible.
 import numpy as np
 import pytest
 
-from sankhya_gb300 import capi, lpgen
+from sankhya_gb300 import capi, certify, lpgen
 from sankhya_gb300.model import LP, from_dense
 
 pytestmark = pytest.mark.gpu
@@ -67,6 +67,7 @@ def test_batch_iteration_limit_and_reproducible():
     lps = [lpgen.planted_uniform(m, 2 * m, 5, seed=m) for m in (60, 80, 100)]
     with capi.BatchEngine(0) as eng:
         eng.load(lps)
+        eng.set_schedule(2, 256)  # a fixed schedule: bit-reproducible solves
         a, _ = eng.solve(tolerance=1e-12, iteration_limit=321)
         assert all(it.status_name == "iteration_limit" and it.iterations == 321 for it in a)
         b, _ = eng.solve(tolerance=1e-12, iteration_limit=321)
@@ -104,9 +105,9 @@ def test_batch_nodes_share_one_matrix_against_highs():
         nodes[k] = LP(base.rows, base.cols, base.col_starts, base.row_index, base.values,
                       base.col_cost, zero, zero.copy(), base.row_lower, base.row_upper)
     A = csc_matrix((base.values, base.row_index, base.col_starts), shape=(base.rows, base.cols))
-    with capi.BatchEngine(0) as eng:
-        eng.load(nodes)
-        items, _ = eng.solve(tolerance=1e-8, iteration_limit=200000)
+    eng = capi.BatchEngine(0)
+    eng.load(nodes)
+    items, _ = eng.solve(tolerance=1e-8, iteration_limit=200000)
     for k, (lp, it) in enumerate(zip(nodes, items)):
         h = scipy_opt.linprog(lp.col_cost, A_eq=A, b_eq=lp.row_lower,
                               bounds=list(zip(lp.col_lower, lp.col_upper)), method="highs")
@@ -115,10 +116,13 @@ def test_batch_nodes_share_one_matrix_against_highs():
         if h.status == 2:
             assert it.status_name == "infeasible", (k, it)
             assert it.farkas_value > 0.0
+            # The certificate itself, checked on the host in exactly rounded FP64.
+            assert certify.farkas_share(lp, eng.ray(k)) > 0.0, k
         else:
             assert h.status == 0
             assert it.status_name in ("optimal", "feasible"), (k, it)
             assert rel(it.objective, h.fun) <= 1e-6
+    eng.close()
 
 
 def test_batch_reports_infeasible_lps():
@@ -129,8 +133,11 @@ def test_batch_reports_infeasible_lps():
     with capi.BatchEngine(0) as eng:
         eng.load(bad + good)
         items, _ = eng.solve(tolerance=1e-8, iteration_limit=100000)
+        rays = [eng.ray(k) for k in range(2)]
     assert [it.status_name for it in items[:2]] == ["infeasible", "infeasible"]
     assert items[2].status_name == "optimal" and rel(items[2].objective, 1.0) <= 1e-6
+    for lp, d in zip(bad, rays):
+        assert certify.farkas_share(lp, d) > 0.0
 
 
 def test_batch_rejects_bad_lps():
@@ -175,5 +182,39 @@ def test_batch_mixed_reports_infeasible_lps():
         eng.load(bad + good)
         items, _ = eng.solve(tolerance=1e-6, iteration_limit=200000, precision="mixed",
                              stop_rule="relative")
+        ray = eng.ray(0)
     assert items[0].status_name == "infeasible"
+    assert certify.farkas_share(bad[0], ray) > 0.0
     assert items[1].status_name in ("optimal", "feasible")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_every_schedule_gives_the_same_answers(oracle, precision):
+    """Each fixed schedule (lanes per row or column x threads per LP) solves the batch to the
+    tolerance with the oracle's statuses and objectives; the autotuned solve reports the
+    schedule it picked, which is one of the candidates."""
+    lps = _mixed_batch()
+    tol = 1e-8
+    refs = [oracle.solve(lp, tolerance=tol, iteration_limit=400000) for lp in lps]
+    with capi.BatchEngine(0) as eng:
+        eng.load(lps)
+        for lanes, threads in [(1, 128), (2, 512), (4, 256), (8, 128), (16, 256), (32, 512)]:
+            eng.set_schedule(lanes, threads)
+            items, _ = eng.solve(tolerance=tol, iteration_limit=400000, precision=precision,
+                                 stop_rule="relative")
+            assert eng.last_schedule()[:2] == (lanes, threads)
+            for k, (lp, it, ref) in enumerate(zip(lps, items, refs)):
+                assert it.status_name in ("optimal", "feasible"), (lanes, threads, k, it)
+                assert rel(it.objective, ref.objective) <= 1e-6, (lanes, threads, k)
+                x, _, y = eng.solution(k)
+                res, _, _ = oracle.evaluate(lp, x, -lp.sense * y)
+                assert max(res["primal"], res["dual"], res["gap"]) <= tol, (lanes, threads, k)
+        eng.set_schedule(0, 0)
+        items, _ = eng.solve(tolerance=tol, iteration_limit=400000, precision=precision,
+                             stop_rule="relative")
+        lanes, threads, tune_s = eng.last_schedule()
+        assert lanes in (1, 2, 4, 8) and threads in (128, 256, 512) and tune_s > 0.0
+        assert all(rel(it.objective, ref.objective) <= 1e-6 for it, ref in zip(items, refs))
+        for bad in [(3, 256), (2, 100), (0, 256), (64, 512)]:
+            with pytest.raises(capi.EngineError):
+                eng.set_schedule(*bad)
