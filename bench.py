@@ -255,7 +255,7 @@ def profile_case(blocks, precision, iterations, zipf=False):
 BATCH_LPS = 4096
 BATCH_NODES = 1024
 BATCH_TOLERANCE = 1e-6
-BATCH_SEQUENTIAL_SAMPLE = (12, 3)  # LPs of each part solved one at a time for the baseline
+BATCH_SEQUENTIAL_SAMPLE = (64, 16)  # LPs of each part solved one at a time for the baseline
 
 
 def make_batch_lps(seed=2027):
@@ -290,9 +290,11 @@ def make_batch_nodes(seed=2028):
 
 def batched_section(device):
     """LPs/s of the batched engine (mixed precision: FP32 iterations on FP64 refinement
-    rounds) against the same LPs solved one at a time by the single-LP engine's plain FP64
-    method (a sample of each part, extrapolated); relative KKT <= 1e-6."""
-    from sankhya_gb300 import capi
+    rounds, the schedule autotuned per batch) against the same LPs solved one at a time by the
+    single-LP engine's plain FP64 method (a sample of each part, extrapolated); relative KKT
+    <= 1e-6. Every independent LP's objective is held to its planted optimum, and every node
+    relaxation reported infeasible has its Farkas certificate checked on the host."""
+    from sankhya_gb300 import capi, certify
 
     out = {}
     for name, make, sample in (("independent", make_batch_lps, BATCH_SEQUENTIAL_SAMPLE[0]),
@@ -304,6 +306,8 @@ def batched_section(device):
             t_load = time.perf_counter() - t0
             items, dev_s = eng.solve(tolerance=BATCH_TOLERANCE, stop_rule="relative",
                                      iteration_limit=200000, precision="mixed")
+            lanes, threads, tune_s = eng.last_schedule()
+            rays = {k: eng.ray(k) for k, it in enumerate(items) if it.status_name == "infeasible"}
         statuses = {}
         for it in items:
             statuses[it.status_name] = statuses.get(it.status_name, 0) + 1
@@ -317,12 +321,28 @@ def batched_section(device):
                               iteration_limit=200000)
                 seq_s += r.device_seconds
         seq_rate = len(picked) / seq_s
-        out[name] = {"lps": len(lps), "precision": "mixed", "device_s": dev_s, "load_s": t_load,
-                     "lps_per_s": len(lps) / dev_s, "statuses": statuses,
-                     "iterations_mean": sum(it.iterations for it in items) / len(items),
-                     "sequential_lps_per_s": seq_rate,
-                     "sequential_sample": len(picked),
-                     "speedup_vs_sequential": (len(lps) / dev_s) / seq_rate}
+        entry = {"lps": len(lps), "precision": "mixed", "device_s": dev_s, "load_s": t_load,
+                 "schedule": {"lanes": lanes, "threads": threads, "autotune_s": tune_s},
+                 "lps_per_s": len(lps) / dev_s, "statuses": statuses,
+                 "iterations_mean": sum(it.iterations for it in items) / len(items),
+                 "sequential_lps_per_s": seq_rate,
+                 "sequential_sample": len(picked),
+                 "speedup_vs_sequential": (len(lps) / dev_s) / seq_rate}
+        if name == "independent":
+            conv = [(it, lp) for it, lp in zip(items, lps) if it.converged]
+            entry["objective_max_rel_err_vs_planted"] = max(
+                (abs(it.objective - lp.fstar) / max(1.0, abs(lp.fstar)) for it, lp in conv),
+                default=None)
+        else:
+            # Every node reported infeasible carries a Farkas ray, checked here in FP64 on the
+            # host (exactly rounded sums); every other node must have converged.
+            shares = [certify.farkas_share(lps[k], rays[k]) for k in rays]
+            entry["infeasible_check"] = {
+                "reported": len(rays), "certified": sum(1 for sh in shares if sh > 0.0),
+                "min_share": min(shares, default=None),
+                "not_converged_other": sum(1 for it in items
+                                           if it.status_name != "infeasible" and not it.converged)}
+        out[name] = entry
     return out
 
 
@@ -337,7 +357,7 @@ ADJOINT_SHAPE = (5000, 10000)
 ADJOINT_FORWARD_TOLERANCE = 1e-4
 
 
-def adjoint_section(device, lps_count=ADJOINT_LPS, shape=ADJOINT_SHAPE, ref_lps=16, fd_lps=2,
+def adjoint_section(device, lps_count=ADJOINT_LPS, shape=ADJOINT_SHAPE, ref_lps=256, fd_lps=16,
                     fd_coords=64):
     """Forward + polish + adjoint times for the whole batch, and the gradients' agreement with
     (a) the basis solves of the planted optimum (sparse LU on the host, `ref_lps` LPs, every
@@ -366,10 +386,15 @@ def adjoint_section(device, lps_count=ADJOINT_LPS, shape=ADJOINT_SHAPE, ref_lps=
         res = eng.adjoint(gx, gy, np.ones(len(lps)))
         adj_s = time.perf_counter() - t0
         vertex_err = 0.0
-        for k in range(min(ref_lps, len(lps))):
-            x, _, y = eng.solution(k)
-            vertex_err = max(vertex_err, float(np.abs(x - lps[k].x0).max()),
-                             float(np.abs(y - lps[k].lam).max()))
+        base_points = {}
+        for k in range(len(lps)):
+            point = eng.solution(k)
+            if k < fd_lps:
+                base_points[k] = point
+            if k < ref_lps:
+                x, _, y = point
+                vertex_err = max(vertex_err, float(np.abs(x - lps[k].x0).max()),
+                                 float(np.abs(y - lps[k].lam).max()))
     out = {"lps": len(lps), "shape": [m, n], "forward_tolerance": ADJOINT_FORWARD_TOLERANCE,
            "forward_device_s": fwd_s, "polish_s": polish_s,
            "forward_iterations_mean": fwd_iterations,
@@ -437,9 +462,16 @@ def adjoint_section(device, lps_count=ADJOINT_LPS, shape=ADJOINT_SHAPE, ref_lps=
                     up[j] += sign * h
                 pert.append(LP(m, n, lp.col_starts, lp.row_index, lp.values, c, lo, up, rl, ru))
                 meta.append((k, fam, j, sign))
+    # Each perturbed LP is solved by PDHG and then polished from its base LP's vertex (a warm
+    # start, sankhya_gb300_batch_set_point): the polish re-solves the base's active sets for
+    # the perturbed data, so the +h and -h vertices carry the same rounding (the basis
+    # matrices' condition numbers reach 1e5 here, so two independently polished vertices
+    # differ by up to ~1e-9 of rounding, which a step of 1e-6 would turn into ~1e-3).
     with capi.BatchEngine(device) as eng:
         eng.load(pert)
         eng.solve(**solve_kw)
+        for q, (k, _, _, _) in enumerate(meta):
+            eng.set_point(q, *base_points[k])
         fitems, finfo = eng.polish()
         sols = [eng.solution(q) for q in range(len(meta))]
     fd_worst, fam_worst, fd_count = 0.0, {}, 0
@@ -469,7 +501,7 @@ def adjoint_section(device, lps_count=ADJOINT_LPS, shape=ADJOINT_SHAPE, ref_lps=
     out["fd_sample"] = (f"{min(fd_lps, len(lps))} LPs x {fd_count // max(1, min(fd_lps, len(lps)))} "
                         f"coordinates (costs, right-hand sides, active lower and upper bounds), "
                         f"central differences with step {h}; the {len(meta)} perturbed LPs "
-                        f"re-solved and polished in one batch")
+                        f"re-solved in one batch and polished from their base LP's vertex")
     return out
 
 
@@ -577,6 +609,74 @@ def cpu_time_limited(lp, threads, time_limit):
             "relative_kkt": relative_kkt(r.residuals), "objective": r.objective}
 
 
+# The reference's own CUDA PDHG (src/gpu/pdhg_gpu.cu, built from its sources by
+# `make -C oracle ref-gpu`): the existing-GPU bar. It runs in a child process, so that its
+# device memory and any failure of it stay out of this process.
+REFERENCE_GPU_TIME_LIMIT = 150.0
+REFERENCE_GPU_SAMPLE_ITERATIONS = 2000
+
+_REFERENCE_GPU_CHILD = r"""
+import json, sys, time
+sys.path[:0] = [sys.argv[1], sys.argv[2]]
+import bench, pyoracle
+lp = bench.make_workload()
+out = {}
+for key, kw in (("setup", dict(iteration_limit=0)),
+                ("sample", dict(iteration_limit=int(sys.argv[3]))),
+                ("to_1e8", dict(time_limit=float(sys.argv[4])))):
+    t0 = time.perf_counter()
+    r = pyoracle.reference_gpu_solve(lp, bench.TOLERANCE, **kw)
+    r["wall_s"] = time.perf_counter() - t0
+    r["objective_rel_err"] = abs(r["objective"] - lp.fstar) / max(1.0, abs(lp.fstar))
+    out[key] = r
+print("REFGPU " + json.dumps(out))
+"""
+
+
+def reference_gpu_section():
+    """The reference's CUDA PDHG on the 1M x 2M LP: its setup alone (iteration limit 0), a
+    fixed sample of iterations, and a run to tolerance 1e-8 under its own stopping rule and
+    REFERENCE_GPU_TIME_LIMIT; seconds per iteration from the first two."""
+    import pyoracle
+
+    t0 = time.perf_counter()
+    pyoracle.build_reference_gpu()
+    build_s = time.perf_counter() - t0
+    proc = subprocess.run([sys.executable, "-c", _REFERENCE_GPU_CHILD, os.path.dirname(
+        os.path.abspath(__file__)), os.path.dirname(os.path.abspath(pyoracle.__file__)),
+        str(REFERENCE_GPU_SAMPLE_ITERATIONS), str(REFERENCE_GPU_TIME_LIMIT)],
+        capture_output=True, text=True, timeout=REFERENCE_GPU_TIME_LIMIT + 600)
+    lines = [l for l in proc.stdout.splitlines() if l.startswith("REFGPU ")]
+    if proc.returncode != 0 or not lines:
+        return {"error": f"exit {proc.returncode}: {(proc.stderr or proc.stdout)[-400:]}"}
+    runs = json.loads(lines[-1][len("REFGPU "):])
+    setup, sample, full = runs["setup"], runs["sample"], runs["to_1e8"]
+    per_it = max(sample["solve_seconds"] - setup["solve_seconds"], 0.0) / max(
+        1, sample["iterations"])
+    statuses = {1: "optimal", 5: "feasible", 6: "iteration_limit", 7: "time_limit",
+                9: "numerical_error"}
+    # An unconverged run states its relative residuals in the message ("stopped at relative
+    # primal P, dual D, gap G ...", src/gpu/pdhg_gpu.cu:796-799); a converged one met the
+    # request (relative KKT <= the tolerance) by definition.
+    import re
+
+    rel = re.search(r"relative primal ([0-9.e+-]+), dual ([0-9.e+-]+), gap ([0-9.e+-]+)",
+                    full["message"])
+    full_kkt = max(float(v) for v in rel.groups()) if rel else None
+    return {"engine": "src/gpu/pdhg_gpu.cu (cuSPARSE SpMV + its elementwise kernels), FP64",
+            "ran_on_gpu": all(r["algorithm"] == "pdhg-cuda" for r in runs.values()),
+            "build_s": build_s, "setup_s": setup["solve_seconds"],
+            "s_per_iteration": per_it, "sample_iterations": sample["iterations"],
+            "to_1e8": {"status": statuses.get(full["status"], str(full["status"])),
+                       "seconds": full["solve_seconds"], "iterations": full["iterations"],
+                       "time_limit_s": REFERENCE_GPU_TIME_LIMIT,
+                       "met_request": full["status"] in (1, 5), "relative_kkt": full_kkt,
+                       "primal_infeasibility": full["primal_infeasibility"],
+                       "dual_infeasibility": full["dual_infeasibility"],
+                       "objective_rel_err": full["objective_rel_err"],
+                       "message": full["message"][:200]}}
+
+
 def kernel_roofline(eng, lp, precision, peak, staged=None):
     """Mean CUDA-event durations of the two step passes (on the engine's stream, 20 steps on
     the state the last solve left) and their achieved GB/s on the algorithmic bytes."""
@@ -604,6 +704,8 @@ def main():
     ap.add_argument("--cpu-iterations", type=int, default=REFERENCE_SAMPLE_ITERATIONS)
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-LP section")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint section")
+    ap.add_argument("--no-reference-gpu", action="store_true",
+                    help="skip timing the reference's own CUDA PDHG")
     ap.add_argument("--no-zipf", action="store_true",
                     help="skip the load-balance stress LP (Zipf row lengths)")
     ap.add_argument("--profile-case", type=int, metavar="PERIODS", default=0,
@@ -763,6 +865,13 @@ def main():
                "sample_relative_kkt": relative_kkt(sr.residuals) if sr is not None else None,
                "time_limited_run": limited, "single_thread": single}
 
+    reference_gpu = None
+    if not args.no_reference_gpu:
+        try:
+            reference_gpu = reference_gpu_section()
+        except Exception as exc:  # noqa: BLE001
+            reference_gpu = {"error": f"{type(exc).__name__}: {exc}"}
+
     dominant = "k_dual" if roof["k_dual_ms"] >= roof["k_primal_ms"] else "k_primal"
     kname = {"k_dual": "row pass (A xbar, A dx, dual update)",
              "k_primal": "column pass (A^T y, primal update)"}[dominant]
@@ -773,7 +882,7 @@ def main():
     # a reader that keeps only the end of the line still has the parity verdict.
     line = {
         "spmv_gbs": roof, "fp64_kernels": froof, "batched": batched, "adjoint": adjoint,
-        "zipf": zipf,
+        "zipf": zipf, "reference_gpu": reference_gpu,
         "metric": METRIC, "value": step_s, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None,

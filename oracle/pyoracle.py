@@ -23,6 +23,10 @@ REF_LIB = os.path.join(HERE, "_ref", "libsankhya_ref.so")
 REFERENCE_TREE = os.environ.get(
     "SANKHYA_REFERENCE_TREE",
     os.path.normpath(os.path.join(HERE, os.pardir, os.pardir, "reference")))
+# A copy of the reference files the checkers are built from (`make -C oracle stage`), made
+# where the reference tree exists, in the git-ignored _ref/ tree, for machines without it.
+STAGE_TREE = os.path.join(HERE, "_ref", "stage")
+REF_GPU_LIB = os.path.join(HERE, "_ref", "libsankhya_ref_gpu.so")
 
 STATUS_NAMES = {0: "not_solved", 1: "optimal", 2: "feasible", 3: "infeasible",
                 5: "iteration_limit", 6: "time_limit", 8: "numerical_error", 9: "model_error",
@@ -90,8 +94,55 @@ def build(reference: bool = False) -> None:
         subprocess.run(["gcc", "-O2", "-fPIC", "-std=c11", "-ffp-contract=off", "-fopenmp",
                         "-shared", "-o", ORACLE_LIB, src, "-lm"], check=True)
     if reference and os.path.isdir(os.path.join(REFERENCE_TREE, "src", "pdhg")):
-        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", f"REF={REFERENCE_TREE}"],
+        subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "stage", f"REF={REFERENCE_TREE}"],
                        check=True)
+
+
+def reference_tree():
+    """The reference checkout, else its staged copy, else None."""
+    for tree in (REFERENCE_TREE, STAGE_TREE):
+        if os.path.isdir(os.path.join(tree, "src", "pdhg")):
+            return tree
+    return None
+
+
+def build_reference_gpu() -> str:
+    """Compile the reference's own CUDA PDHG (`make -C oracle ref-gpu`) from the reference
+    tree or its staged copy; returns the library's path. Raises when neither is present."""
+    tree = reference_tree()
+    if tree is None:
+        raise RuntimeError("neither the reference tree nor its staged copy is present")
+    subprocess.run(["make", "-s", "-j16", "-C", HERE, "ref-gpu", f"REF={tree}"], check=True,
+                   stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    return REF_GPU_LIB
+
+
+def reference_gpu_solve(lp, tolerance, iteration_limit=-1, time_limit=None):
+    """The reference's CUDA PDHG (src/gpu/pdhg_gpu.cu) on one LP, through
+    ref/ref_gpu_capi.cpp. Returns a dict: status (the reference's SolveStatus value),
+    iterations, objective, solve_seconds, primal / dual infeasibility and relative gap,
+    algorithm ("pdhg-cuda" when the CUDA path ran to the end) and message."""
+    lib = ctypes.CDLL(REF_GPU_LIB)
+    f = lib.ref_gpu_solve_pdhg
+    f.argtypes = [ctypes.POINTER(CLp), ctypes.c_double, ctypes.c_int64, ctypes.c_double,
+                  ctypes.POINTER(ctypes.c_int64), _D, _D, _D, ctypes.c_char_p, ctypes.c_int32,
+                  ctypes.c_char_p, ctypes.c_int32]
+    f.restype = ctypes.c_int32
+    c, keep = Oracle._clp(lp)
+    its = ctypes.c_int64()
+    obj, sec = ctypes.c_double(), ctypes.c_double()
+    res = np.zeros(3)
+    alg = ctypes.create_string_buffer(64)
+    msg = ctypes.create_string_buffer(512)
+    status = f(ctypes.byref(c), tolerance, iteration_limit,
+               1e308 if time_limit is None else time_limit, ctypes.byref(its),
+               ctypes.byref(obj), ctypes.byref(sec), _ptr(res, ctypes.c_double), alg, 64, msg,
+               512)
+    del keep
+    return {"status": int(status), "iterations": int(its.value), "objective": obj.value,
+            "solve_seconds": sec.value, "primal_infeasibility": float(res[0]),
+            "dual_infeasibility": float(res[1]), "relative_gap": float(res[2]),
+            "algorithm": alg.value.decode(), "message": msg.value.decode()}
 
 
 def reference_available() -> bool:

@@ -63,9 +63,11 @@ def engine(built):
 
 
 def _reference_tree():
+    """The reference checkout, else its staged copy (oracle/_ref/stage), else the checkout's
+    expected path (where the tests that need it skip)."""
     import pyoracle
 
-    return pyoracle.REFERENCE_TREE
+    return pyoracle.reference_tree() or pyoracle.REFERENCE_TREE
 
 
 def core_link_args():

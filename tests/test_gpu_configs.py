@@ -1,0 +1,101 @@
+"""Both methods on reduced forms of the two large synthetic LPs, held to the oracle.
+
+* A 4-period slice of the block-angular multi-period LP (62,500 x 125,000, 1.25e6 nonzeros;
+  the full LP is 64 periods): each method to relative KKT 1e-8.
+* The load-balance stress family (Zipf(1.5) row lengths, values of log-uniform magnitude
+  over [1e-3, 1e3], badly scaled before the solver's own scaling), twice:
+  - at 300 x 600, each method to relative KKT 1e-6 against the oracle's own answer. The
+    reference algorithm converges slowly on this family: the oracle, which stops only by the
+    reference's rule (its request also asks an absolute primal residual of 1e-7), runs to its
+    2,000,000-iteration limit and ends at relative gap 1.6e-7, objective 2e-8 from the
+    planted optimum;
+  - at 1/20 of its size (25,000 x 50,000, about 1.5e6 nonzeros, rows up to 6,688 entries,
+    cut into pieces), each method for a fixed 60,000 iterations. At this size the reference's
+    restart rule does not reach 1e-6 in practical time (the FP64 method stood at relative gap
+    9.8e-5 after 1,000,000 iterations), so this case checks the product at scale instead of
+    convergence: the oracle's FP64 evaluation of each reported point must equal the engine's
+    own residuals, and both methods must have made the same progress (relative KKT below
+    1e-2, objectives within it of the planted optimum and of each other).
+
+The oracle's copy of the reference's evaluate() (src/pdhg/pdhg_evaluate.cpp) re-evaluates
+each returned point in FP64 and must find it within the tolerance; the objective must match
+the planted optimum c'x0 to 1e-6 relative, and the two methods each other to 1e-6. A solve
+of the oracle itself at the block-angular slice's size takes minutes on one CPU thread, so
+the planted optimum stands in for its answer there (it is the LP's optimal value by
+construction).
+"""
+import numpy as np
+import pytest
+
+from sankhya_gb300 import capi, lpgen
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return abs(a - b) / max(1.0, abs(b))
+
+
+def _check(oracle, lp, sol, tol):
+    assert sol.status in ("optimal", "feasible"), sol.message
+    assert rel(sol.objective, lp.fstar) <= 1e-6, (sol.objective, lp.fstar)
+    res, _, red = oracle.evaluate(lp, sol.col_value, -lp.sense * sol.row_dual)
+    assert max(res["primal"], res["dual"], res["gap"]) <= tol, res
+    assert np.allclose(lp.sense * red, sol.col_dual, rtol=1e-12, atol=1e-12)
+    for key in ("primal", "dual", "gap"):
+        assert abs(sol.result.residuals[key] - res[key]) <= 1e-12 + 1e-6 * res[key]
+
+
+def _both(engine, oracle, lp, tol, limit):
+    out = {}
+    for precision in ("fp64", "mixed"):
+        sol = capi.solve_pdhg_gpu(lp, {"pdhg_tolerance": tol, "pdhg_precision": precision,
+                                       "pdhg_stop_rule": "relative",
+                                       "iteration_limit": limit}, engine=engine)
+        print(f"{precision}: {sol.status} {sol.iterations} it, objective {sol.objective!r} "
+              f"vs planted {lp.fstar!r} (rel {rel(sol.objective, lp.fstar):.2e})")
+        _check(oracle, lp, sol, tol)
+        out[precision] = sol
+    assert rel(out["mixed"].objective, out["fp64"].objective) <= 1e-6
+    return out
+
+
+def test_block_angular_slice(engine, oracle):
+    lp = lpgen.planted_blocks(4, 15625, 31250, 9, seed=2026)
+    _both(engine, oracle, lp, 1e-8, 1000000)
+
+
+def test_zipf_rows_small_against_the_oracle(engine, oracle):
+    lp = lpgen.planted_zipf(300, 600, 6000, max_len=400, seed=4)
+    ref = oracle.solve(lp, tolerance=1e-6, iteration_limit=2000000)
+    print(f"oracle: {ref.status_name} {ref.iterations} it, objective {ref.objective!r}")
+    assert rel(ref.objective, lp.fstar) <= 1e-6
+    out = _both(engine, oracle, lp, 1e-6, 2000000)
+    for sol in out.values():
+        assert rel(sol.objective, ref.objective) <= 1e-6
+
+
+def test_zipf_rows_twentieth_at_fixed_iterations(engine, oracle):
+    lp = lpgen.planted_zipf(25000, 50000, 1500000, seed=3)
+    assert np.diff(lp.col_starts).max() < 2048 < _row_lengths(lp).max()  # long rows: pieces
+    out = {}
+    for precision in ("fp64", "mixed"):
+        sol = capi.solve_pdhg_gpu(lp, {"pdhg_tolerance": 1e-8, "pdhg_precision": precision,
+                                       "pdhg_stop_rule": "relative",
+                                       "iteration_limit": 60000}, engine=engine)
+        kkt = max(sol.result.residuals[k] for k in ("primal", "dual", "gap"))
+        print(f"{precision}: {sol.status} {sol.iterations} it, relative KKT {kkt:.3e}, "
+              f"objective {sol.objective!r} vs planted {lp.fstar!r}")
+        assert sol.status == "iteration_limit" and sol.iterations == 60000
+        res, _, red = oracle.evaluate(lp, sol.col_value, -lp.sense * sol.row_dual)
+        for key in ("primal", "dual", "gap"):
+            assert abs(sol.result.residuals[key] - res[key]) <= 1e-12 + 1e-6 * res[key], key
+        assert np.allclose(lp.sense * red, sol.col_dual, rtol=1e-12, atol=1e-12)
+        assert kkt <= 1e-2
+        assert rel(sol.objective, lp.fstar) <= 1e-2
+        out[precision] = sol
+    assert rel(out["mixed"].objective, out["fp64"].objective) <= 1e-2
+
+
+def _row_lengths(lp):
+    return np.bincount(lp.row_index, minlength=lp.rows)

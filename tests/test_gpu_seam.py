@@ -1,0 +1,61 @@
+"""SANKHYA's own solve() on the GB300 engine, checked by the reference's own verifier.
+
+`tests/host/gpu_write.cpp` is linked with the reference's whole core (`make -C oracle
+ref-core`: solve(), the MPS reader, the solution writer), the four seam files that replace
+src/gpu and the engine's real library, lib/libsankhya_gb300.so: the build a maintainer ships,
+with no stand-in. Each Netlib model is solved by solve() with algorithm=pdhg, gpu=true at
+1e-8 (src/core/solve.cpp:796-803 routes it to the seam), written by io::write_solution, and
+must pass tools/verify_solution.py (tools/verify_solution.py:601-610), which re-reads the
+model and recomputes feasibility, reduced costs, complementarity and strong duality from the
+written point. Uses the reference tree, or its copy staged by `make -C oracle stage` where
+the tree is absent; skips when neither is there.
+"""
+import os
+import subprocess
+import sys
+
+import pytest
+
+from conftest import core_link_args
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+MODELS = ["afiro", "sc50a", "sc50b", "adlittle", "blend", "sc105", "stocfor1", "israel"]
+
+
+@pytest.fixture(scope="module")
+def gpu_write(tmp_path_factory, built):
+    import pyoracle
+
+    flags, sources, core = core_link_args()
+    # The real engine stands where the C-ABI stand-in stands in the CPU front-end tests.
+    sources = [s for s in sources if not s.endswith("seam_standin.cpp")]
+    lib_dir = os.path.join(ROOT, "sih-26_gb300", "lib")
+    exe = str(tmp_path_factory.mktemp("gpu_write") / "gpu_write")
+    cmd = (["g++"] + flags + sources + [os.path.join(ROOT, "tests", "host", "gpu_write.cpp"),
+                                        core, f"-L{lib_dir}", "-lsankhya_gb300",
+                                        f"-Wl,-rpath,{lib_dir}", "-fopenmp", "-lz", "-o", exe])
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr[-3000:]
+    return exe, pyoracle.reference_tree()
+
+
+@pytest.mark.parametrize("name", MODELS)
+def test_gpu_answers_pass_the_reference_verifier(gpu_write, tmp_path, name):
+    exe, tree = gpu_write
+    model = os.path.join(tree, "data", "netlib", f"{name}.mps")
+    verifier = os.path.join(tree, "tools", "verify_solution.py")
+    if not (os.path.exists(model) and os.path.exists(verifier)):
+        pytest.skip("the Netlib model or tools/verify_solution.py is not present")
+    sol = str(tmp_path / f"{name}.sol")
+    run = subprocess.run([exe, model, sol], capture_output=True, text=True, timeout=600)
+    print(run.stdout[-600:])
+    assert run.returncode == 0, run.stdout[-2000:] + run.stderr[-2000:]
+    assert "algorithm pdhg-gpu" in run.stdout, run.stdout
+    assert ": optimal," in run.stdout, run.stdout
+    check = subprocess.run([sys.executable, verifier, model, sol], capture_output=True,
+                           text=True, timeout=600)
+    print(check.stdout[-600:])
+    assert check.returncode == 0, check.stdout[-3000:] + check.stderr[-2000:]
+    assert "VERIFIED" in check.stdout, check.stdout[-2000:]
