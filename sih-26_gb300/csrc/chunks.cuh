@@ -30,15 +30,9 @@
 // a chunk of 256 entries almost every warp-wide gather has a lane that misses when even 8% of
 // the entries fall outside. So where a window covers most but not all of a layout's entries,
 // the layout is split: the entries inside each row's window form the main matrix (gathered
-// from shared memory only), the rest an OUTER matrix of their own. The outer entries are
-// summed one of two ways:
-//   * FED (the row pass of the mixed method): the column pass, as it produces du_j, writes
-//     a_ij du_j of every outer entry (i, j) to that entry's slot, and the row pass reads each
-//     row's slots as a stream at chunk start (addresses known up front, nothing gathered)
-//     and adds them after the row's main entries;
-//   * by a PROLOGUE: each block first sums the outer entries of its own rows (plain L2
-//     gathers, while its first window copy is in flight) into outer[row], and the main loop
-//     adds outer[row] to each row's sum before its epilogue.
+// from shared memory only), the rest an OUTER matrix of their own. Each block first sums the
+// outer entries of its own rows (plain L2 gathers, while its first window copy is in flight)
+// into outer[row], and the main loop adds outer[row] to each row's sum before its epilogue.
 //
 // Every wait is bounded: a wait that gives up raises the block's abort flag, the remaining
 // chunks are skipped, the copy still in flight is given a bounded time to land, and the
@@ -93,24 +87,8 @@ struct ChunkSet {
   const T* oval;
   const int2* orounds;
   const int* oround_start;
-  T* outer;              // nullptr: not split, or split with fed outer products
-  // A split layout whose outer products another pass writes (FED): row r's outer products
-  // are oprod[optr[r] .. optr[r + 1]), read as a stream at chunk start.
-  const T* oprod;        // nullptr: not fed
-  // The feeds this layout writes for another layout's outer products: line r's feed entries
-  // [fptr[r], fptr[r + 1]) of (fslot, fval, fline) make fout[fslot] = fval * (the value line
-  // fline's epilogue produced).
-  const int* fptr;       // nullptr: this layout feeds nothing
-  const int* fslot;
-  const int* fline;
-  const T* fval;
-  T* fout;
+  T* outer;              // nullptr: not split
 };
-
-// Per chunk: at most kFeedsPerChunk feed entries (one per lane) and at most kOuterPerChunk
-// fed outer products (two per lane), staged beside the chunk's products.
-constexpr int kFeedsPerChunk = 32;
-constexpr int kOuterPerChunk = 64;
 
 // ---- PTX helpers ---------------------------------------------------------------------------
 __device__ __forceinline__ int ld_stream(const int* p) {
@@ -160,7 +138,7 @@ struct StageProducts {
 template <typename T, typename G, int NP, int CH>
 struct ChunkSmem {
   static constexpr int kBufBytes =
-      (CH * (StageProducts<T>::value ? NP : 1 + NP) + kOuterPerChunk) * static_cast<int>(sizeof(T));
+      CH * (StageProducts<T>::value ? NP : 1 + NP) * static_cast<int>(sizeof(T));
   __host__ __device__ static constexpr int bytes(int warps, int wmax) {
     return warps * kBufBytes + 128 + ((wmax * static_cast<int>(sizeof(G)) + 127) & ~127);
   }
@@ -175,25 +153,18 @@ __device__ __forceinline__ int chunk_lanes(int R) {
 // One chunk: stream, gather, stage, sum, epilogue (all lanes of the warp call it).
 //   gather(col) -> G          the vector element of column col
 //   load(row, ops)            the row's NR epilogue operands (lane-per-row, at chunk start)
-//   epi(row, sums, ops) -> T  once per row, on the row's first lane; returns the value the
-//                             row produces for the feeds (used when FEED)
-// OUTER: 0 = every entry in the main layout; 1 = plus outer[row] (summed by the block's
-// prologue); 2 = plus the row's fed outer products (oprod), staged after the products and
-// summed after the row's main entries. FEED: the chunk's lines write their feed entries.
-template <int NP, int NR, typename T, typename G, int CH, int OUTER, bool FEED, typename Gather,
+//   epi(row, sums, ops)       once per row, on the row's first lane
+template <int NP, int NR, typename T, typename G, int CH, bool OUTER, typename Gather,
           typename Load, typename Epi>
-__device__ __forceinline__ void chunk_step(const ChunkSet<T>& cs, const Tile& ch, T* buf,
-                                           double* piece_part, Gather gather, Load load,
-                                           Epi epi) {
-  static_assert((OUTER != 2 && !FEED) || (NP == 1 && StageProducts<T>::value),
-                "fed outer products and feeds are single FP32 products");
+__device__ __forceinline__ void chunk_step(const int* __restrict__ ptr, const int* __restrict__ idx,
+                                           const T* __restrict__ val, const Tile& ch, T* buf,
+                                           const T* __restrict__ outer, double* piece_part,
+                                           Gather gather, Load load, Epi epi) {
   constexpr int J = CH / 32;
   const int lane = static_cast<int>(threadIdx.x) & 31;
   const bool piece = ch.r1 < 0;
   const int R = piece ? 0 : ch.r1 - ch.r0;
   const int n = ch.k1 - ch.k0;
-  const int* __restrict__ idx = cs.idx;
-  const T* __restrict__ val = cs.val;
   int col[J];
   T a[J];
 #pragma unroll
@@ -203,52 +174,25 @@ __device__ __forceinline__ void chunk_step(const ChunkSet<T>& cs, const Tile& ch
     col[j] = in ? ld_stream(idx + k) : -1;
     a[j] = in ? ld_stream(val + k) : T(0);
   }
-  int pr = 0, op = 0, fp = 0;
+  int pr = 0;
   T ops[NR > 0 ? NR : 1];
   T out[NP];
 #pragma unroll
   for (int q = 0; q < NP; ++q) out[q] = T(0);
   if (!piece) {
-    if (lane <= R) {
-      pr = __ldg(cs.ptr + ch.r0 + lane);
-      if (OUTER == 2) op = __ldg(cs.optr + ch.r0 + lane);
-      if (FEED) fp = __ldg(cs.fptr + ch.r0 + lane);
-    }
+    if (lane <= R) pr = __ldg(ptr + ch.r0 + lane);
     if (lane < R) {
       load(ch.r0 + lane, ops);
-      if (OUTER == 1) {
+      if (OUTER) {
 #pragma unroll
-        for (int q = 0; q < NP; ++q) out[q] = cs.outer[(ch.r0 + lane) * NP + q];
+        for (int q = 0; q < NP; ++q) out[q] = outer[(ch.r0 + lane) * NP + q];
       }
-    }
-  }
-  // Fed outer products: the chunk's rows own slots [op0, op0 + ocount), read as a stream.
-  int op0 = 0, ocount = 0;
-  T o_lo = T(0), o_hi = T(0);
-  if (OUTER == 2 && !piece) {
-    op0 = __shfl_sync(0xffffffffu, op, 0);
-    ocount = __shfl_sync(0xffffffffu, op, R) - op0;
-    if (lane < ocount) o_lo = ld_stream(cs.oprod + op0 + lane);
-    if (lane + 32 < ocount) o_hi = ld_stream(cs.oprod + op0 + 32 + lane);
-  }
-  // Feed entries of the chunk's lines: lane l holds entry f0 + l.
-  int fcount = 0, fslot = 0, fsrc = 0;
-  T fval = T(0);
-  if (FEED && !piece) {
-    const int f0 = __shfl_sync(0xffffffffu, fp, 0);
-    fcount = __shfl_sync(0xffffffffu, fp, R) - f0;
-    if (lane < fcount) {
-      fslot = __ldg(cs.fslot + f0 + lane);
-      fval = __ldg(cs.fval + f0 + lane);
-      fsrc = __ldg(cs.fline + f0 + lane) - ch.r0;
     }
   }
   constexpr bool kProducts = StageProducts<T>::value;
   // Pairs: bv holds the values, bg the NP gathered components; products: bg the NP products.
-  // bo holds the fed outer products.
   T* bv = buf;
   T* bg = kProducts ? buf : buf + CH;
-  T* bo = buf + CH * (kProducts ? NP : 1 + NP);
 #pragma unroll
   for (int j = 0; j < J; ++j) {
     T c[NP];
@@ -264,10 +208,6 @@ __device__ __forceinline__ void chunk_step(const ChunkSet<T>& cs, const Tile& ch
 #pragma unroll
       for (int q = 0; q < NP; ++q) bg[q * CH + lane + 32 * j] = c[q];
     }
-  }
-  if (OUTER == 2) {
-    bo[lane] = o_lo;
-    bo[lane + 32] = o_hi;
   }
   __syncwarp();
   // The sum of entry k's term q in order: an add of the staged product, or an FMA of the
@@ -297,13 +237,6 @@ __device__ __forceinline__ void chunk_step(const ChunkSet<T>& cs, const Tile& ch
         for (int q = 0; q < NP; ++q) s[q] = term(q, k, s[q]);
       }
     }
-    if (OUTER == 2) {
-      const int oa = __shfl_sync(0xffffffffu, op, g & 31) - op0;
-      const int oe = __shfl_sync(0xffffffffu, op, (g + 1) & 31) - op0;
-      if (g < R) {
-        for (int k = oa + sub; k < oe; k += L) s[0] += bo[k];
-      }
-    }
     for (int o = L >> 1; o > 0; o >>= 1) {
 #pragma unroll
       for (int q = 0; q < NP; ++q) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
@@ -311,18 +244,11 @@ __device__ __forceinline__ void chunk_step(const ChunkSet<T>& cs, const Tile& ch
     T og[NR > 0 ? NR : 1];
 #pragma unroll
     for (int q = 0; q < NR; ++q) og[q] = __shfl_sync(0xffffffffu, ops[q], g & 31);
-    if (OUTER == 1) {
+    if (OUTER) {
 #pragma unroll
       for (int q = 0; q < NP; ++q) s[q] += __shfl_sync(0xffffffffu, out[q], g & 31);
     }
-    T produced = T(0);
-    if (g < R && sub == 0) produced = epi(ch.r0 + g, s, og);
-    if (FEED) {
-      // A feed entry's line is summed by the lanes of group fsrc; its first lane produced
-      // the value.
-      const T v = __shfl_sync(0xffffffffu, produced, (fsrc * L) & 31);
-      if (lane < fcount) cs.fout[fslot] = fval * v;
-    }
+    if (g < R && sub == 0) epi(ch.r0 + g, s, og);
   }
   __syncwarp();
 }
@@ -376,8 +302,7 @@ __device__ __forceinline__ void outer_sums(const ChunkSet<T>& cs, const G* __res
   }
 }
 
-template <int OUTER, bool FEED, int NP, int NR, typename T, typename G, int CH, typename Load,
-          typename Epi>
+template <bool OUTER, int NP, int NR, typename T, typename G, int CH, typename Load, typename Epi>
 __device__ __forceinline__ bool run_chunks_impl(const ChunkSet<T>& cs, const G* __restrict__ vec,
                                                 unsigned char* dsmem, double* piece_part,
                                                 Load load, Epi epi) {
@@ -407,7 +332,7 @@ __device__ __forceinline__ bool run_chunks_impl(const ChunkSet<T>& cs, const G* 
     bulk_copy_g2s(win, vec + sg.lo, static_cast<uint32_t>(sg.len) * sizeof(G), winbar);
     pending = true;
   }
-  if (OUTER == 1) outer_sums<NP>(cs, vec, reinterpret_cast<T*>(dsmem));
+  if (OUTER) outer_sums<NP>(cs, vec, reinterpret_cast<T*>(dsmem));
 
   for (int s = s0; s < s1; ++s) {
     const ChunkSeg sg = cs.segs[s];
@@ -442,7 +367,8 @@ __device__ __forceinline__ bool run_chunks_impl(const ChunkSet<T>& cs, const G* 
       if (s_abort) break;
       const Tile ch = next;
       if (c + W < sg.c1) next = cs.chunks[c + W];
-      chunk_step<NP, NR, T, G, CH, OUTER, FEED>(cs, ch, buf, piece_part, gather, load, epi);
+      chunk_step<NP, NR, T, G, CH, OUTER>(cs.ptr, cs.idx, cs.val, ch, buf, cs.outer, piece_part,
+                                          gather, load, epi);
     }
   }
   __syncthreads();
@@ -454,31 +380,14 @@ __device__ __forceinline__ bool run_chunks_impl(const ChunkSet<T>& cs, const G* 
 }
 
 // Visit this block's chunks (kernel launched with a multiple of 32 threads, every thread
-// calls it). Returns false -- in every thread -- if a wait gave up. FEEDER: whether this pass
-// may write feeds (the FP32 column pass, which feeds the row pass's outer products; it does
-// when its layout has feed entries). A feeder's own layout is unsplit or split with a
-// prologue; a non-feeder's may also consume fed outer products.
-template <bool FEEDER, int NP, int NR, typename T, typename G, int CH, typename Load,
-          typename Epi>
+// calls it). Returns false -- in every thread -- if a wait gave up.
+template <int NP, int NR, typename T, typename G, int CH, typename Load, typename Epi>
 __device__ __forceinline__ bool run_chunks(const ChunkSet<T>& cs, const G* __restrict__ vec,
                                            unsigned char* dsmem, double* piece_part, Load load,
                                            Epi epi) {
-  if constexpr (FEEDER) {
-    if (cs.fptr != nullptr) {
-      return cs.outer != nullptr
-                 ? run_chunks_impl<1, true, NP, NR, T, G, CH>(cs, vec, dsmem, piece_part, load,
-                                                              epi)
-                 : run_chunks_impl<0, true, NP, NR, T, G, CH>(cs, vec, dsmem, piece_part, load,
-                                                              epi);
-    }
-  } else {
-    if (cs.oprod != nullptr) {
-      return run_chunks_impl<2, false, NP, NR, T, G, CH>(cs, vec, dsmem, piece_part, load, epi);
-    }
-  }
   return cs.outer != nullptr
-             ? run_chunks_impl<1, false, NP, NR, T, G, CH>(cs, vec, dsmem, piece_part, load, epi)
-             : run_chunks_impl<0, false, NP, NR, T, G, CH>(cs, vec, dsmem, piece_part, load, epi);
+             ? run_chunks_impl<true, NP, NR, T, G, CH>(cs, vec, dsmem, piece_part, load, epi)
+             : run_chunks_impl<false, NP, NR, T, G, CH>(cs, vec, dsmem, piece_part, load, epi);
 }
 
 // Last block only: each long row combined from its piece partials in piece order (double),
@@ -501,12 +410,7 @@ __device__ __forceinline__ void run_chunk_long_rows(const ChunkSet<T>& cs,
     for (int q = 0; q < NP; ++q) s[q] = static_cast<T>(acc[q]);
     T ops[NR > 0 ? NR : 1];
     load(lr.row, ops);
-    const T produced = epi(lr.row, s, ops);
-    if (cs.fptr != nullptr) {
-      for (int f = cs.fptr[lr.row]; f < cs.fptr[lr.row + 1]; ++f) {
-        cs.fout[cs.fslot[f]] = cs.fval[f] * produced;
-      }
-    }
+    epi(lr.row, s, ops);
   }
 }
 

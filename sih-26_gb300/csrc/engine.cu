@@ -365,9 +365,7 @@ void Engine::allocate_mixed() {
     D->fval.allocate_padded(static_cast<size_t>(D->nmain), kPad, s);
     D->foval.allocate_padded(static_cast<size_t>(D->nouter), kPad, s);
     D->fouter.allocate_padded(static_cast<size_t>(D->nrows), kPad, s);
-    if (D->fed) D->oprod.allocate_padded(static_cast<size_t>(D->nouter), kPad, s);
   }
-  if (ck_csc_f_.nfeeds > 0) ck_csc_f_.feed_val.allocate(static_cast<size_t>(ck_csc_f_.nfeeds));
   fill_mixed_buffers();
   mixed_ready_ = true;
 }
@@ -409,7 +407,6 @@ void Engine::fill_mixed_buffers() {
   b.part_dual = part_dual_.ptr;
   b.csc_k = chunk_set(ck_csc_f_, csc_ptr_.ptr, csc_idx_.ptr, csc_f_.ptr);
   b.csr_k = chunk_set(ck_csr_f_, csr_ptr_.ptr, csr_idx_.ptr, csr_f_.ptr);
-  if (ck_csc_f_.nfeeds > 0) b.csc_k.fout = ck_csr_f_.oprod.ptr;
   b.piece_primal = ck_csc_f_.pieces.ptr;
   b.piece_dual = ck_csr_f_.pieces.ptr;
   b.part_rows0 = part_rows0_.ptr;
@@ -632,43 +629,8 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   };
   make_layout(step_csc_, ctiles, lp.row_index, m, 0);
   make_layout(step_csr_, rtiles, ridx.data(), n, 1);
-  // The FP32 row layout first: where it is split, the column pass feeds its outer products
-  // (a_ij du_j of every out-of-window entry, written as du_j is produced), so the column
-  // layout is planned with the feed lists of its columns.
-  const ChunkPlan prow = plan_layout(ck_csr_f_, rptr, ridx.data(), m, n, 1, cap, nullptr,
-                                     kOuterPerChunk);
-  std::vector<int> feed_ptr, feed_slot, feed_map;
-  if (prow.split) {
-    feed_ptr.assign(static_cast<size_t>(n) + 1, 0);
-    for (int j : prow.oidx) ++feed_ptr[static_cast<size_t>(j) + 1];
-    for (int j = 0; j < n; ++j) feed_ptr[j + 1] += feed_ptr[j];
-    feed_slot.resize(prow.oidx.size());
-    feed_map.resize(prow.oidx.size());
-    std::vector<int> at(feed_ptr.begin(), feed_ptr.end() - 1);
-    for (size_t slot = 0; slot < prow.oidx.size(); ++slot) {
-      const int f = at[static_cast<size_t>(prow.oidx[slot])]++;
-      feed_slot[static_cast<size_t>(f)] = static_cast<int>(slot);
-      feed_map[static_cast<size_t>(f)] = prow.omap[slot];
-    }
-  }
-  plan_layout(ck_csc_f_, cptr, lp.row_index, n, m, 0, cap, prow.split ? &feed_ptr : nullptr);
-  ck_csr_f_.fed = prow.split;
-  ck_csc_f_.nfeeds = static_cast<long long>(feed_slot.size());
-  if (prow.split) {
-    std::vector<int> feed_line(feed_slot.size());
-    for (int j = 0; j < n; ++j) {
-      for (int f = feed_ptr[j]; f < feed_ptr[j + 1]; ++f) feed_line[static_cast<size_t>(f)] = j;
-    }
-    ck_csc_f_.fptr.upload(feed_ptr.data(), feed_ptr.size(), s);
-    ck_csc_f_.fslot.upload(feed_slot.data(), feed_slot.size(), s);
-    ck_csc_f_.fline.upload(feed_line.data(), feed_line.size(), s);
-    ck_csc_f_.fmap.upload(feed_map.data(), feed_map.size(), s);
-  } else {
-    for (DeviceArray<int>* a : {&ck_csc_f_.fptr, &ck_csc_f_.fslot, &ck_csc_f_.fline,
-                                &ck_csc_f_.fmap}) {
-      a->release();
-    }
-  }
+  plan_layout(ck_csc_f_, cptr, lp.row_index, n, m, 0, cap);
+  plan_layout(ck_csr_f_, rptr, ridx.data(), m, n, 1, cap);
   grid_c = std::max({grid_c, step_csc_.grid, ck_csc_f_.grid});
   grid_r = std::max({grid_r, step_csr_.grid, ck_csr_f_.grid});
 
@@ -731,9 +693,8 @@ void Engine::load(const sankhya_gb300_lp& lp) {
 // piece and split buffers allocated. Windows are kept over every entry when they hold at least
 // 99.9% of them and the layout is split from 50% up; a capacity set through
 // SANKHYA_GB300_WINDOW_CAP (window_cap >= 0) splits any layout whose windows hold an entry.
-ChunkPlan Engine::plan_layout(ChunkDev& D, const std::vector<int>& lptr, const int* lidx,
-                              int lines, int extent, int pass, int window_cap,
-                              const std::vector<int>* feed_ptr, int outer_chunk_cap) {
+void Engine::plan_layout(ChunkDev& D, const std::vector<int>& lptr, const int* lidx, int lines,
+                         int extent, int pass, int window_cap) {
   cudaStream_t s = stream_;
   int wmax = mixed_window_capacity(pass);
   if (window_cap >= 0) wmax = std::min(wmax, window_cap);
@@ -741,8 +702,7 @@ ChunkPlan Engine::plan_layout(ChunkDev& D, const std::vector<int>& lptr, const i
   // The outer sums stage their products in the block's warp buffers.
   const int round_cap = (kChunkThreads / 32) * kChunkCapF;
   ChunkPlan P = plan_chunks(lptr, lidx, lines, extent, kChunkCapF, wmax, num_sms_,
-                            static_cast<int>(sizeof(float)), split_min, 0.999, round_cap,
-                            feed_ptr, kFeedsPerChunk, outer_chunk_cap);
+                            static_cast<int>(sizeof(float)), split_min, 0.999, round_cap);
   if (P.error) throw EngineError{SANKHYA_GB300_ERROR_DEVICE, "chunk layout planning failed"};
   D.nrows = lines;
   D.split = P.split;
@@ -778,11 +738,6 @@ ChunkPlan Engine::plan_layout(ChunkDev& D, const std::vector<int>& lptr, const i
   D.fval.release();
   D.foval.release();
   D.fouter.release();
-  D.oprod.release();
-  D.feed_val.release();
-  D.fed = false;
-  D.nfeeds = 0;
-  return P;
 }
 
 ChunkSet<float> Engine::chunk_set(const ChunkDev& D, const int* full_ptr, const int* full_idx,
@@ -805,22 +760,12 @@ ChunkSet<float> Engine::chunk_set(const ChunkDev& D, const int* full_ptr, const 
     c.oround_start = D.oround_start.ptr;
     c.val = D.fval.ptr;
     c.oval = D.foval.ptr;
-    if (D.fed) {
-      c.oprod = D.oprod.ptr;  // written by the column pass, read as a stream
-    } else {
-      c.outer = D.fouter.ptr;
-    }
+    c.outer = D.fouter.ptr;
   } else {
     c.ptr = full_ptr;
     c.idx = full_idx;
     c.val = full_val;
     c.outer = nullptr;
-  }
-  if (D.nfeeds > 0) {
-    c.fptr = D.fptr.ptr;
-    c.fslot = D.fslot.ptr;
-    c.fline = D.fline.ptr;
-    c.fval = D.feed_val.ptr;
   }
   return c;
 }
@@ -937,11 +882,6 @@ void Engine::fill_split_values() {
     if (!D.split) continue;
     launch_gather_values(l.second, D.map.ptr, D.fval.ptr, D.nmain, s);
     launch_gather_values(l.second, D.omap.ptr, D.foval.ptr, D.nouter, s);
-  }
-  // The feed values: the row layout's scaled values at its outer entries.
-  if (ck_csc_f_.nfeeds > 0) {
-    launch_gather_values(csr_s_.ptr, ck_csc_f_.fmap.ptr, ck_csc_f_.feed_val.ptr,
-                         ck_csc_f_.nfeeds, s);
   }
 }
 

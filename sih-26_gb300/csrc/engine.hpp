@@ -49,27 +49,6 @@ struct DeviceArray {
   void release();
 };
 
-// The step passes' chunk layout of one matrix layout (layout.cu): `ptr` / `idx` its lines
-// and indices over a gathered vector of `extent` elements, `cap` entries per chunk, `wmax`
-// the window capacity, `grid` blocks, `elem_bytes` the gathered element's size. Windows are
-// kept over every entry when they hold at least `full_min` of them; between `split_min` and
-// that, the layout is split into main and outer parts; below it, nothing is staged. A split
-// layout's outer entries are summed in rounds of at most `outer_round_cap` entries. A layout
-// that FEEDS another's outer products (feed_ptr: a prefix array over its lines) keeps at most
-// `feed_cap` feed entries per chunk; a layout that CONSUMES fed outer products
-// (outer_chunk_cap > 0) keeps at most that many outer entries per chunk.
-struct ChunkPlan {
-  int cap = 0, grid = 1, wmax = 0, npieces = 0;
-  bool split = false, error = false;
-  double coverage = 0.0, staged = 0.0;
-  std::vector<Tile> chunks;
-  std::vector<int2> orounds;
-  std::vector<LongRow> longs;
-  std::vector<ChunkSeg> segs;
-  std::vector<int> seg_start, oround_start;
-  std::vector<int> ptr, idx, map, optr, oidx, omap;  // split layouts only
-};
-
 class Engine {
  public:
   explicit Engine(int device);
@@ -161,14 +140,6 @@ class Engine {
     DeviceArray<int> seg_start, oround_start;
     DeviceArray<int> ptr, idx, map, optr, oidx, omap;
     DeviceArray<float> fval, foval, fouter;
-    // Fed outer products (a split row layout that the column pass feeds): one per outer entry.
-    DeviceArray<float> oprod;
-    // The feeds this layout writes (the column layout): per line, slots in the fed layout's
-    // outer products, the line, the full-CSR position of the value, and the FP32 values.
-    DeviceArray<int> fptr, fslot, fline, fmap;
-    DeviceArray<float> feed_val;
-    long long nfeeds = 0;
-    bool fed = false;
     DeviceArray<double> pieces;  // piece partials (NP per piece)
     int nlong = 0, npieces = 0, wmax = 0, grid = 1, smem = 0, nrows = 0;
     bool split = false;
@@ -177,9 +148,8 @@ class Engine {
     double coverage = 0.0;  // share the windows would hold over the whole layout
   };
   ChunkDev ck_csc_f_, ck_csr_f_;
-  ChunkPlan plan_layout(ChunkDev& D, const std::vector<int>& ptr, const int* idx, int lines,
-                        int extent, int pass, int window_cap,
-                        const std::vector<int>* feed_ptr = nullptr, int outer_chunk_cap = 0);
+  void plan_layout(ChunkDev& D, const std::vector<int>& ptr, const int* idx, int lines,
+                   int extent, int pass, int window_cap);
   void fill_split_values();
   ChunkSet<float> chunk_set(const ChunkDev& D, const int* full_ptr, const int* full_idx,
                             const float* full_val) const;
@@ -237,11 +207,26 @@ class Engine {
 
 size_t estimate_memory(long long rows, long long cols, long long nnz, int precision);
 
-// The chunk plan of one matrix layout (see ChunkPlan).
+// The step passes' chunk layout of one matrix layout (layout.cu): `ptr` / `idx` its lines
+// and indices over a gathered vector of `extent` elements, `cap` entries per chunk, `wmax`
+// the window capacity, `grid` blocks, `elem_bytes` the gathered element's size. Windows are
+// kept over every entry when they hold at least `full_min` of them; between `split_min` and
+// that, the layout is split into main and outer parts; below it, nothing is staged. A split
+// layout's outer entries are summed in rounds of at most `outer_round_cap` entries.
+struct ChunkPlan {
+  int cap = 0, grid = 1, wmax = 0, npieces = 0;
+  bool split = false, error = false;
+  double coverage = 0.0, staged = 0.0;
+  std::vector<Tile> chunks;
+  std::vector<int2> orounds;
+  std::vector<LongRow> longs;
+  std::vector<ChunkSeg> segs;
+  std::vector<int> seg_start, oround_start;
+  std::vector<int> ptr, idx, map, optr, oidx, omap;  // split layouts only
+};
 ChunkPlan plan_chunks(const std::vector<int>& ptr, const int* idx, int lines, int extent, int cap,
                       int wmax, int grid, int elem_bytes, double split_min, double full_min,
-                      int outer_round_cap, const std::vector<int>* feed_ptr = nullptr,
-                      int feed_cap = 0, int outer_chunk_cap = 0);
+                      int outer_round_cap);
 
 // The status a tile product's error word maps to: 0 = ok, otherwise a device error.
 int product_error_status(unsigned int word);

@@ -21,14 +21,12 @@ namespace sgb {
 
 namespace {
 
-// Consecutive rows while the chunk has at most kChunkRows rows and `cap` entries, every row
-// of it shares `row_win` (nullptr: no window constraint), and the rows' counts in `extra` (a
-// prefix array over the rows, nullptr: none) sum to at most `extra_cap`; a row longer than
-// `cap` becomes pieces of `cap` entries, listed as a LongRow.
+// Consecutive rows while the chunk has at most kChunkRows rows and `cap` entries, and every
+// row of it shares `row_win` (nullptr: no window constraint); a row longer than `cap` becomes
+// pieces of `cap` entries, listed as a LongRow.
 void cut_chunks(const std::vector<int>& ptr, int r_begin, int r_end, int cap,
                 const std::vector<int>* row_win, std::vector<Tile>* chunks,
-                std::vector<LongRow>* longs, int* npieces, const std::vector<int>* extra = nullptr,
-                int extra_cap = 0) {
+                std::vector<LongRow>* longs, int* npieces) {
   int r = r_begin;
   while (r < r_end) {
     const int len = ptr[r + 1] - ptr[r];
@@ -48,8 +46,7 @@ void cut_chunks(const std::vector<int>& ptr, int r_begin, int r_end, int cap,
     const int w = row_win ? (*row_win)[r] : 0;
     ++r;
     while (r < r_end && r - begin < kChunkRows && ptr[r + 1] - ptr[r] <= cap &&
-           ptr[r + 1] - ptr[begin] <= cap && (row_win == nullptr || (*row_win)[r] == w) &&
-           (extra == nullptr || (*extra)[r + 1] - (*extra)[begin] <= extra_cap)) {
+           ptr[r + 1] - ptr[begin] <= cap && (row_win == nullptr || (*row_win)[r] == w)) {
       ++r;
     }
     chunks->push_back(Tile{begin, r, ptr[begin], ptr[r]});
@@ -173,14 +170,8 @@ long long plan_windows(const std::vector<Tile>& chunks, const int* idx, int exte
 
 ChunkPlan plan_chunks(const std::vector<int>& ptr, const int* idx, int lines, int extent, int cap,
                       int wmax, int grid, int elem_bytes, double split_min, double full_min,
-                      int outer_round_cap, const std::vector<int>* feed_ptr, int feed_cap,
-                      int outer_chunk_cap) {
+                      int outer_round_cap) {
   ChunkPlan p;
-  if (feed_ptr != nullptr && outer_chunk_cap > 0) {
-    std::fprintf(stderr, "plan_chunks: a layout cannot both feed and consume fed products\n");
-    p.error = true;
-    return p;
-  }
   p.cap = cap;
   p.grid = std::max(1, grid);
   const long long nnz = lines > 0 ? ptr[lines] : 0;
@@ -188,7 +179,7 @@ ChunkPlan plan_chunks(const std::vector<int>& ptr, const int* idx, int lines, in
   std::vector<Tile> base;
   std::vector<LongRow> base_longs;
   int base_pieces = 0;
-  cut_chunks(ptr, 0, lines, cap, nullptr, &base, &base_longs, &base_pieces, feed_ptr, feed_cap);
+  cut_chunks(ptr, 0, lines, cap, nullptr, &base, &base_longs, &base_pieces);
   std::vector<int> tile_win;
   std::vector<int2> windows;
   long long covered = 0;
@@ -244,16 +235,7 @@ ChunkPlan plan_chunks(const std::vector<int>& ptr, const int* idx, int lines, in
       p.ptr[r + 1] = static_cast<int>(p.idx.size());
       p.optr[r + 1] = static_cast<int>(p.oidx.size());
     }
-    // A layout that consumes fed outer products keeps at most outer_chunk_cap of them per
-    // chunk (they are staged beside the chunk's products); a feeding layout keeps its feed
-    // limit.
-    if (outer_chunk_cap > 0) {
-      cut_chunks(p.ptr, 0, lines, cap, &row_win, &p.chunks, &p.longs, &p.npieces, &p.optr,
-                 outer_chunk_cap);
-    } else {
-      cut_chunks(p.ptr, 0, lines, cap, &row_win, &p.chunks, &p.longs, &p.npieces, feed_ptr,
-                 feed_cap);
-    }
+    cut_chunks(p.ptr, 0, lines, cap, &row_win, &p.chunks, &p.longs, &p.npieces);
     chunk_win.resize(p.chunks.size());
     for (size_t c = 0; c < p.chunks.size(); ++c) {
       const Tile& tl = p.chunks[c];

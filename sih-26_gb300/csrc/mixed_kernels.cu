@@ -79,10 +79,9 @@ __global__ void __launch_bounds__(kChunkThreads, 1) k_primal_f(MixedBuffers b) {
     const float d = unj - uj;
     b.du[j] = d;
     mvf = fmaf(d, d, mvf);
-    return d;  // feeds the row pass's out-of-window products a_ij du_j
   };
-  if (!run_chunks<true, 1, 5, float, float, kChunkCapF>(b.csc_k, v, dsmem, b.piece_primal,
-                                                        load, epi) &&
+  if (!run_chunks<1, 5, float, float, kChunkCapF>(b.csc_k, v, dsmem, b.piece_primal, load,
+                                                  epi) &&
       threadIdx.x == 0) {
     raise_error(ctl);
   }
@@ -150,10 +149,9 @@ __global__ void __launch_bounds__(kChunkThreads, 1) k_dual_f(MixedBuffers b) {
     const float d = vni - vi;
     a0 = fmaf(d, d, a0);
     a1 = fmaf(d, adu, a1);
-    return 0.0f;
   };
-  if (!run_chunks<false, 1, 6, float, float, kChunkCapF>(b.csr_k, b.du, dsmem, b.piece_dual,
-                                                         load, epi) &&
+  if (!run_chunks<1, 6, float, float, kChunkCapF>(b.csr_k, b.du, dsmem, b.piece_dual, load,
+                                                  epi) &&
       threadIdx.x == 0) {
     raise_error(ctl);
   }

@@ -16,9 +16,7 @@
 //     cover its chunks in order with windows on 4-element bounds inside the padded vector;
 //     a split layout's main and outer parts partition the entries, every main entry of a
 //     windowed chunk lies in its window, and the outer rounds write every row exactly once,
-//     by the block whose chunks hold it, within the staging space; a row plan that consumes
-//     fed outer products keeps at most kOuterPerChunk of them per chunk, and the column plan
-//     that feeds it at most kFeedsPerChunk feeds per chunk;
+//     by the block whose chunks hold it, within the staging space;
 // plus the FP32 lane rule and the step graph's launch count. Given a file, it checks the
 // layouts the engine builds for that pattern instead (read_pattern).
 #include <cmath>
@@ -170,17 +168,12 @@ void check_windows(const Pattern& p, const std::vector<Tile>& tiles, int wmax) {
   if (count != covered) fail("staged count", covered, count);
 }
 
-// The chunk plan of an FP32 step pass for pattern p (see plan_chunks). With `consume`, the
-// plan is the row pass's, whose outer products are fed (at most kOuterPerChunk per chunk);
-// with `feed`, it writes feeds for the lines' counts in *feed (at most kFeedsPerChunk per
-// chunk).
-ChunkPlan check_chunk_plan(const Pattern& p, int wmax, int grid, double split_min,
-                           bool consume = false, const std::vector<int>* feed = nullptr) {
+// The chunk plan of an FP32 step pass for pattern p (see plan_chunks).
+void check_chunk_plan(const Pattern& p, int wmax, int grid, double split_min) {
   const int cap = kChunkCapF;
   const int round_cap = (kChunkThreads / 32) * kChunkCapF;
   const ChunkPlan P = plan_chunks(p.ptr, p.idx.data(), p.lines, p.extent, cap, wmax, grid, 4,
-                                  split_min, 0.999, round_cap, feed, kFeedsPerChunk,
-                                  consume ? kOuterPerChunk : 0);
+                                  split_min, 0.999, round_cap);
   if (P.error) fail("plan_chunks reported an error", p.lines, wmax);
   const long long nnz = p.ptr[p.lines];
   const std::vector<int>& ptr = P.split ? P.ptr : p.ptr;
@@ -208,13 +201,6 @@ ChunkPlan check_chunk_plan(const Pattern& p, int wmax, int grid, double split_mi
     if (ch.r0 != row) fail("chunks out of order", ch.r0, row);
     if (ch.r1 <= ch.r0 || ch.r1 - ch.r0 > kChunkRows) fail("chunk rows", ch.r0, ch.r1);
     if (ch.k0 != ptr[static_cast<size_t>(ch.r0)] || ch.k1 != ptr[static_cast<size_t>(ch.r1)]) fail("chunk entries do not match its rows", ch.k0, ch.k1);
-    // Feeds (one per lane) and fed outer products (two per lane) per chunk.
-    if (feed != nullptr && (*feed)[static_cast<size_t>(ch.r1)] - (*feed)[static_cast<size_t>(ch.r0)] > kFeedsPerChunk) {
-      fail("feeds per chunk", ch.r0, (*feed)[static_cast<size_t>(ch.r1)] - (*feed)[static_cast<size_t>(ch.r0)]);
-    }
-    if (consume && P.split && P.optr[static_cast<size_t>(ch.r1)] - P.optr[static_cast<size_t>(ch.r0)] > kOuterPerChunk) {
-      fail("fed outer products per chunk", ch.r0, P.optr[static_cast<size_t>(ch.r1)] - P.optr[static_cast<size_t>(ch.r0)]);
-    }
     row = ch.r1;
   }
   if (row != p.lines) fail("chunks do not cover every line", row, p.lines);
@@ -252,7 +238,7 @@ ChunkPlan check_chunk_plan(const Pattern& p, int wmax, int grid, double split_mi
   }
   if (!P.split) {
     if (!P.orounds.empty() || !P.oidx.empty()) fail("outer part of an unsplit layout", static_cast<long long>(P.oidx.size()), 0);
-    return P;
+    return;
   }
   // Split: main and outer entries partition the layout's entries, in row order.
   if (static_cast<long long>(P.map.size() + P.omap.size()) != nnz) fail("split entry count", static_cast<long long>(P.map.size() + P.omap.size()), nnz);
@@ -291,43 +277,6 @@ ChunkPlan check_chunk_plan(const Pattern& p, int wmax, int grid, double split_mi
       if (row_block[static_cast<size_t>(r)] != chunk_block[static_cast<size_t>(c)]) fail("outer sum written by another block", r, chunk_block[static_cast<size_t>(c)]);
     }
   }
-  return P;
-}
-
-// A row plan that consumes fed outer products and the column plan that feeds it: every outer
-// entry of the row plan is fed by exactly one column line, the one its index names.
-void check_fed_pair(const Pattern& rows, const Pattern& cols, int wmax) {
-  const ChunkPlan pr = check_chunk_plan(rows, wmax, 152, 0.0, true);
-  if (!pr.split) return;
-  std::vector<int> feed(static_cast<size_t>(cols.lines) + 1, 0);
-  for (int j : pr.oidx) {
-    if (j < 0 || j >= cols.lines) {
-      fail("outer entry's column", j, cols.lines);
-      return;
-    }
-    ++feed[static_cast<size_t>(j) + 1];
-  }
-  for (int j = 0; j < cols.lines; ++j) feed[static_cast<size_t>(j) + 1] += feed[static_cast<size_t>(j)];
-  if (feed[static_cast<size_t>(cols.lines)] != static_cast<int>(pr.oidx.size())) fail("feed count", feed[static_cast<size_t>(cols.lines)], static_cast<long long>(pr.oidx.size()));
-  check_chunk_plan(cols, wmax, 152, 0.5, false, &feed);
-}
-
-// The transpose of a pattern (CSR <-> CSC).
-Pattern transpose(const Pattern& p) {
-  Pattern t;
-  t.lines = p.extent;
-  t.extent = p.lines;
-  t.ptr.assign(static_cast<size_t>(t.lines) + 1, 0);
-  for (int c : p.idx) ++t.ptr[static_cast<size_t>(c) + 1];
-  for (int r = 0; r < t.lines; ++r) t.ptr[static_cast<size_t>(r) + 1] += t.ptr[static_cast<size_t>(r)];
-  std::vector<int> at(t.ptr.begin(), t.ptr.end() - 1);
-  t.idx.assign(p.idx.size(), 0);
-  for (int r = 0; r < p.lines; ++r) {
-    for (int k = p.ptr[static_cast<size_t>(r)]; k < p.ptr[static_cast<size_t>(r) + 1]; ++k) {
-      t.idx[static_cast<size_t>(at[static_cast<size_t>(p.idx[static_cast<size_t>(k)])]++)] = r;
-    }
-  }
-  return t;
 }
 
 // A pattern from a file: int32 lines, int32 extent, int32 ptr[lines + 1], int32 idx[nnz].
@@ -421,12 +370,6 @@ int main(int argc, char** argv) {
           for (double split_min : {0.0, 0.5}) check_chunk_plan(p, wmax, grid, split_min);
           ++layouts;
         }
-      }
-      // Fed pairs: the row plan consuming, the column plan of the transpose feeding it.
-      const Pattern t = transpose(p);
-      for (int wmax : {1024, 4096, 8192}) {
-        check_fed_pair(p, t, wmax);
-        ++layouts;
       }
     }
   }
