@@ -25,19 +25,55 @@ __device__ inline void clear_evaluation_flags(Ctl* c) {
   }
 }
 
+// The primal half of the movement for the row pass's decision (every thread of the last
+// block calls it; thread 0 gets the value). When the column pass had no long column to
+// finish, its blocks only published their partials and the sum is taken here, in block
+// order as the column pass's own last block would have (`published` true); otherwise that
+// block already left it in the control block. Either way ctl->mv_primal holds it after.
+__device__ __forceinline__ double primal_movement(bool published, const double* part,
+                                                  int nblocks, double omega, Ctl* ctl,
+                                                  double* scratch) {
+  if (!published) return ctl->mv_primal;
+  double tp[1];
+  sum_partials<1>(part, nblocks, scratch, tp);
+  const double mv = 0.5 * omega * tp[0];
+  if (threadIdx.x == 0) ctl->mv_primal = mv;
+  return mv;
+}
+
 // Adaptive step, src/pdhg/pdhg.cpp:252-335: accept iff eta <= movement / interaction, then
 // eta <- clamp(min(shrink * limit, grow * eta), 1e-12, ceiling) unless the step carried no
 // information; an accepted step flips the current buffer and counts an iteration.
-__device__ inline void step_decision(Ctl* c, double movement, double interaction) {
+//
+// The two factors depend only on the iteration count: shrink = 1 - e^-0.3 and grow = 1 + e^-0.6
+// with e = max(iteration + 1, 2). step_factors() gives them; a kernel whose decision sits on
+// its critical path (the last block's) reads them from a table filled once by the same pow
+// (k_step_factors), so the decision does not wait on two FP64 pow calls on one thread.
+__device__ inline long long step_factor_index(long long iteration) {
+  return iteration + 1 > 2 ? iteration + 1 : 2;
+}
+
+__device__ inline double2 step_factors(long long e) {
+  const double exponent = static_cast<double>(e);
+  return make_double2(1.0 - pow(exponent, -0.3), 1.0 + pow(exponent, -0.6));
+}
+
+// The factors of iteration count `iteration` from `table` (n entries, indexed by e) where it
+// covers e, else computed.
+__device__ inline double2 step_factors(long long iteration, const double2* table, long long n) {
+  const long long e = step_factor_index(iteration);
+  return (table != nullptr && e < n) ? table[e] : step_factors(e);
+}
+
+__device__ inline void step_decision(Ctl* c, double movement, double interaction,
+                                     double2 factors) {
   c->movement = movement;
   c->interaction = interaction;
   const bool no_information = interaction <= 0.0;
   const double limit = no_information ? __longlong_as_double(0x7ff0000000000000LL)
                                       : movement / interaction;
-  const long long e = c->iteration + 1 > 2 ? c->iteration + 1 : 2;
-  const double exponent = static_cast<double>(e);
-  const double shrink = 1.0 - pow(exponent, -0.3);
-  const double grow = 1.0 + pow(exponent, -0.6);
+  const double shrink = factors.x;
+  const double grow = factors.y;
   const double proposed = dmin(shrink * limit, grow * c->eta);
   const bool accept = c->eta <= limit;
   if (accept) {
@@ -57,6 +93,10 @@ __device__ inline void step_decision(Ctl* c, double movement, double interaction
   c->accepted = accept;
   c->no_information = no_information;
   c->eval_now = (c->iteration > 0) && ((c->iteration % 40) == 0 || no_information);
+}
+
+__device__ inline void step_decision(Ctl* c, double movement, double interaction) {
+  step_decision(c, movement, interaction, step_factors(step_factor_index(c->iteration)));
 }
 
 // The evaluation-tick decisions of src/pdhg/pdhg.cpp:349-483 given the assembled residuals

@@ -280,8 +280,10 @@ size_t estimate_memory(long long rows, long long cols, long long nnz, int precis
     bytes += 2 * z * sizeof(float) + (10 * n + 8 * m) * sizeof(float);
   }
   // Fixed: the kernels' device code (a 5.8 MB fatbin, loaded at the first launch, after a
-  // caller's memory check), the partial-sum buffers and the control block.
+  // caller's memory check), the partial-sum buffers and the control block; and the 16 MB
+  // table of step-size factors.
   bytes += 16u << 20;
+  bytes += static_cast<size_t>(kStepFactorTable) * sizeof(double2);
   return bytes;
 }
 
@@ -403,6 +405,8 @@ void Engine::fill_mixed_buffers() {
   b.vc[1] = vc1_.ptr;
   b.u_best = ubest_.ptr;
   b.v_best = vbest_.ptr;
+  b.step_factors = step_factors_.ptr;
+  b.step_factors_n = kStepFactorTable;
   b.part_primal = part_primal_.ptr;
   b.part_dual = part_dual_.ptr;
   b.csc_k = chunk_set(ck_csc_f_, csc_ptr_.ptr, csc_idx_.ptr, csc_f_.ptr);
@@ -682,6 +686,10 @@ void Engine::load(const sankhya_gb300_lp& lp) {
   chunk_spmv_.allocate(static_cast<size_t>(std::max(nchunks_csc_, nchunks_csr_)) + 1);
   scalars_.allocate(static_cast<size_t>(pgrid) * 2 + 16);
   power_norms_.allocate(64);
+  if (step_factors_.ptr == nullptr) {
+    step_factors_.allocate(static_cast<size_t>(kStepFactorTable));
+    launch_step_factors(step_factors_.ptr, kStepFactorTable, s);
+  }
   tickets_.allocate(4);
   SGB_CUDA(cudaMemsetAsync(tickets_.ptr, 0, 4 * sizeof(unsigned int), s));
   SGB_CUDA(cudaStreamSynchronize(s));
@@ -793,6 +801,8 @@ void Engine::fill_buffers() {
   b.u = us_.ptr;
   b.rl = rls_.ptr;
   b.ru = rus_.ptr;
+  b.step_factors = step_factors_.ptr;
+  b.step_factors_n = kStepFactorTable;
   b.part_primal = part_primal_.ptr;
   b.part_dual = part_dual_.ptr;
   b.chunk_primal = chunk_primal_.ptr;

@@ -49,6 +49,9 @@ struct DeviceArray {
   void release();
 };
 
+// Entries of the step-size factor table (decisions.cuh, step_factors): 16 MB of double2.
+constexpr long long kStepFactorTable = 1LL << 20;
+
 class Engine {
  public:
   explicit Engine(int device);
@@ -162,6 +165,8 @@ class Engine {
   DeviceArray<double> csc_raw_, csr_raw_, csc_s_, csr_s_;
   // Unscaled vectors.
   DeviceArray<double> cost_, col_cost_, l_, u_, rl_, ru_;
+  // The step-size factors for iteration counts below kStepFactorTable (filled once).
+  DeviceArray<double2> step_factors_;
   // Scaled vectors and scaling.
   DeviceArray<double> cs_, ls_, us_, rls_, rus_, dr_, dc_, row_acc_, col_acc_;
   // Iterates.

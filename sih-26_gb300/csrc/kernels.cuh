@@ -110,6 +110,9 @@ struct StepBuffers {
   double* chunk_dual;    // [csr.nchunks * 2]
   int grid_primal, grid_dual;
   int smem_primal, smem_dual;  // dynamic shared memory: pipeline + staged window
+  // The step-size factors by iteration count (decisions.cuh, step_factors).
+  const double2* step_factors;
+  long long step_factors_n;
 };
 
 struct EvalBuffers {
@@ -179,6 +182,8 @@ cudaError_t noalloc_scratch(int device, cudaStream_t s, double** chunks, unsigne
 // doubles; ticket is one device counter that is zero on entry and on exit. A bounded wait
 // that gives up sets *error (which the caller clears and reads) and leaves NaN in the rows
 // the product could not finish.
+// table[e] = step_factors(e) for e < n (decisions.cuh).
+void launch_step_factors(double2* table, long long n, cudaStream_t s);
 void launch_spmv(TileSet<double> a, const double* x, double* y, double* chunk,
                  unsigned int* ticket, unsigned int* error, cudaStream_t s, int grid);
 // out[0] = sum v^2, deterministic; part holds grid doubles.

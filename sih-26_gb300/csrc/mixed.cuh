@@ -63,6 +63,8 @@ struct MixedBuffers {
   int grid_step_primal, grid_step_dual;  // step passes (one block of kChunkThreads per SM)
   int smem_primal, smem_dual;     // step passes' dynamic shared memory
   int m, n;
+  const double2* step_factors;    // the step-size factors by iteration count
+  long long step_factors_n;
 };
 
 // FP64 buffers of the refinement rounds.

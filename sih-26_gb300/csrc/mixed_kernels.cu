@@ -86,6 +86,15 @@ __global__ void __launch_bounds__(kChunkThreads, 1) k_primal_f(MixedBuffers b) {
     raise_error(ctl);
   }
   double mv[1] = {static_cast<double>(mvf)};
+  if (b.csc_k.nlong == 0) {
+    // No long column to finish: each block publishes its partial, and the row pass's last
+    // block sums them in block order (primal_movement) when it takes the step decision. No
+    // block of this pass waits for another.
+    double out[1];
+    block_sum<1>(mv, scratch, out);
+    if (threadIdx.x == 0) b.part_primal[blockIdx.x] = out[0];
+    return;
+  }
   if (!arrive_last<1>(mv, scratch, b.part_primal, &ctl->ticket[kTicketPrimal])) return;
   mvf = 0.0f;
   run_chunk_long_rows<1, 5, float>(b.csc_k, b.piece_primal, load, epi);
@@ -107,6 +116,10 @@ __global__ void __launch_bounds__(kChunkThreads, 1) k_dual_f(MixedBuffers b) {
   const bool add = ctl->pending_add != 0;
   const double omega = ctl->omega, eta = ctl->eta;
   if (done != kRunning || eval_now != 0) return;
+  // The step-size factors of this step, loaded now for the decision the last block takes.
+  const double2 factors = threadIdx.x == 0
+                              ? step_factors(ctl->iteration, b.step_factors, b.step_factors_n)
+                              : make_double2(0.0, 0.0);
   const float* __restrict__ v = b.v[cur];
   float* __restrict__ vn = b.v[cur ^ 1];
   const float* __restrict__ au = b.au[cur];
@@ -164,11 +177,13 @@ __global__ void __launch_bounds__(kChunkThreads, 1) k_dual_f(MixedBuffers b) {
   double longs[2], total[2];
   block_sum<2>(acc2, scratch, longs);
   sum_partials<2>(b.part_dual, gridDim.x, scratch, total);
+  const double mv_primal = primal_movement(b.csc_k.nlong == 0, b.part_primal,
+                                           b.grid_step_primal, omega, ctl, scratch);
   if (threadIdx.x == 0) {
     ctl->ticket[kTicketDual] = 0;
     if (ctl->done == kRunning) {
-      const double movement = ctl->mv_primal + (0.5 * (total[0] + longs[0])) / omega;
-      step_decision(ctl, movement, fabs(total[1] + longs[1]));
+      const double movement = mv_primal + (0.5 * (total[0] + longs[0])) / omega;
+      step_decision(ctl, movement, fabs(total[1] + longs[1]), factors);
     }
   }
 }

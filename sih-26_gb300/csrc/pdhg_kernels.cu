@@ -134,6 +134,14 @@ __global__ void __launch_bounds__(kBlockThreads) k_primal(StepBuffers b) {
       threadIdx.x == 0) {
     raise_error(ctl);
   }
+  if (b.csc.nlong == 0) {
+    // No long column to finish: each block publishes its partial, and k_dual's last block
+    // sums them in block order (primal_movement). No block of this pass waits for another.
+    double out[1];
+    block_sum<1>(mv, scratch, out);
+    if (threadIdx.x == 0) b.part_primal[blockIdx.x] = out[0];
+    return;
+  }
   if (!arrive_last<1>(mv, scratch, b.part_primal, &ctl->ticket[kTicketPrimal])) return;
   mv[0] = 0.0;
   run_long_rows<1>(b.csc, b.chunk_primal, epi);
@@ -153,6 +161,10 @@ __global__ void __launch_bounds__(kBlockThreads) k_dual(StepBuffers b) {
   Ctl* ctl = b.ctl;
   if (ctl->done != kRunning || ctl->eval_now != 0) return;
   const int cur = ctl->cur;
+  // The step-size factors of this step, loaded now for the decision the last block takes.
+  const double2 factors = threadIdx.x == 0
+                              ? step_factors(ctl->iteration, b.step_factors, b.step_factors_n)
+                              : make_double2(0.0, 0.0);
   const double* __restrict__ y = b.y[cur];
   double* __restrict__ yn = b.y[cur ^ 1];
   const double2* __restrict__ xd = b.xd;
@@ -198,11 +210,13 @@ __global__ void __launch_bounds__(kBlockThreads) k_dual(StepBuffers b) {
   double longs[2], total[2];
   block_sum<2>(acc2, scratch, longs);
   sum_partials<2>(b.part_dual, gridDim.x, scratch, total);
+  const double mv_primal =
+      primal_movement(b.csc.nlong == 0, b.part_primal, b.grid_primal, omega, ctl, scratch);
   if (threadIdx.x == 0) {
     ctl->ticket[kTicketDual] = 0;
     if (ctl->done == kRunning) {
-      const double movement = ctl->mv_primal + (0.5 * (total[0] + longs[0])) / omega;
-      step_decision(ctl, movement, fabs(total[1] + longs[1]));
+      const double movement = mv_primal + (0.5 * (total[0] + longs[0])) / omega;
+      step_decision(ctl, movement, fabs(total[1] + longs[1]), factors);
     }
   }
 }
@@ -812,6 +826,19 @@ void launch_scale_vectors(int m, int n, const double* cost, const double* l, con
   ++g_launches;
   k_scale_vectors<<<elementwise_grid(m > n ? m : n), 256, 0, s>>>(m, n, cost, l, u, rl, ru, dr, dc,
                                                                   cs, ls, us, rls, rus);
+}
+
+__global__ void k_step_factors(double2* table, long long n) {
+  for (long long e = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; e < n;
+       e += static_cast<long long>(gridDim.x) * blockDim.x) {
+    table[e] = step_factors(step_factor_index(e - 1));
+  }
+}
+
+void launch_step_factors(double2* table, long long n, cudaStream_t s) {
+  if (n <= 0) return;
+  ++g_launches;
+  k_step_factors<<<std::max(1, device_sms()) * 8, 256, 0, s>>>(table, n);
 }
 
 void launch_spmv(TileSet<double> a, const double* x, double* y, double* chunk,

@@ -4,11 +4,12 @@
 // Linked with the reference's whole core (solve(), the readers, the writer; oracle/Makefile
 // `ref-core`), the seam files that replace src/gpu and the engine's real library
 // (lib/libsankhya_gb300.so): the path a maintainer ships, with no stand-in anywhere.
-// `gpu_write model.mps out.sol` solves the model with algorithm=pdhg, gpu=true (tolerance
-// 1e-8, no interior-point polish) and writes the answer with io::write_solution
-// (src/io/writer.cpp), which tools/verify_solution.py reads. It exits 1 unless the answer came
+// `gpu_write model.mps out.sol [tolerance]` solves the model with algorithm=pdhg, gpu=true
+// (tolerance 1e-8 unless given, no interior-point polish) and writes the answer with
+// io::write_solution (src/io/writer.cpp), which tools/verify_solution.py reads. It exits 1 unless the answer came
 // through the seam ("pdhg-gpu"), 2 when the model cannot be read or the answer written.
 #include <cstdio>
+#include <cstdlib>
 #include <string>
 
 #include "sankhya/io.hpp"
@@ -16,8 +17,8 @@
 #include "sankhya/options.hpp"
 
 int main(int argc, char** argv) {
-  if (argc != 3) {
-    std::printf("usage: gpu_write model.mps out.sol\n");
+  if (argc < 3 || argc > 4) {
+    std::printf("usage: gpu_write model.mps out.sol [tolerance]\n");
     return 2;
   }
   sankhya::Model model;
@@ -31,7 +32,7 @@ int main(int argc, char** argv) {
   o.set_string("algorithm", "pdhg");
   o.set_bool("gpu", true);
   o.set_bool("pdhg_polish", false);
-  o.set_double("pdhg_tolerance", 1e-8);
+  o.set_double("pdhg_tolerance", argc >= 4 ? std::atof(argv[3]) : 1e-8);
   o.set_int("iteration_limit", 1000000);
   const sankhya::Solution s = sankhya::solve(model, o);
   std::string error;

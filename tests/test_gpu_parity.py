@@ -216,3 +216,22 @@ def test_iteration_log_every_40(engine):
     assert sol.status == "optimal"
     assert rows and all(it % 40 == 0 for it, *_ in rows[:-1])
     assert abs(rows[-1][1] - sol.objective) <= 1e-6 * max(1.0, abs(sol.objective))
+
+
+def test_engines_on_two_devices_in_one_process(oracle):
+    """Each device gets its own kernel configuration (the shared-memory opt-ins are per
+    device): engines on devices 0 and 1 in one process each run a product and a solve. It
+    uses no peer memory. Skips where fewer than two GPUs are visible."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.device_count() < 2:
+        pytest.skip("fewer than two GPUs are visible")
+    lp = lpgen.planted_uniform(200, 500, 5, seed=3)
+    x = np.random.default_rng(4).normal(size=lp.cols)
+    ref = oracle.solve(lp, tolerance=1e-8)
+    for device in (0, 1):
+        with capi.PdhgEngine(device) as eng:
+            eng.load(lp)
+            assert_spmv_close(oracle, lp, eng.spmv(0, x), x, False)
+            r = eng.solve(tolerance=1e-8)
+            assert r.status_name == ref.status_name
+            assert rel(r.objective, ref.objective) <= OBJ_TOL
