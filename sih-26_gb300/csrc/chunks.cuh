@@ -268,18 +268,36 @@ __device__ __forceinline__ void outer_sums(const ChunkSet<T>& cs, const G* __res
     const int2 rr = cs.orounds[q0];
     const int e0 = __ldg(cs.optr + rr.x), e1 = __ldg(cs.optr + rr.y);
     const int count = e1 - e0;
-    // Stage: pairs put the value at [k] and component q at [(1 + q) * count + k].
-    for (int k = t; k < count; k += B) {
-      const T a = ld_stream(cs.oval + e0 + k);
-      T c[NP];
-      split_gathered(__ldg(vec + ld_stream(cs.oidx + e0 + k)), c);
-      if (kProducts) {
+    // Stage: pairs put the value at [k] and component q at [(1 + q) * count + k]. A thread
+    // takes kOuterBatch entries at a time and issues all their index and value loads, then
+    // all their gathers, so it waits for two latencies per batch, not two per entry.
+    constexpr int kOuterBatch = 8;
+    for (int k0 = t; k0 < count; k0 += B * kOuterBatch) {
+      int ix[kOuterBatch];
+      T av[kOuterBatch];
 #pragma unroll
-        for (int q = 0; q < NP; ++q) stage[q * count + k] = a * c[q];
-      } else {
-        stage[k] = a;
+      for (int u = 0; u < kOuterBatch; ++u) {
+        const int k = k0 + u * B;
+        ix[u] = k < count ? ld_stream(cs.oidx + e0 + k) : -1;
+        av[u] = k < count ? ld_stream(cs.oval + e0 + k) : T(0);
+      }
+      G g[kOuterBatch];
 #pragma unroll
-        for (int q = 0; q < NP; ++q) stage[(1 + q) * count + k] = c[q];
+      for (int u = 0; u < kOuterBatch; ++u) g[u] = ix[u] >= 0 ? __ldg(vec + ix[u]) : G{};
+#pragma unroll
+      for (int u = 0; u < kOuterBatch; ++u) {
+        const int k = k0 + u * B;
+        if (k >= count) break;
+        T c[NP];
+        split_gathered(g[u], c);
+        if (kProducts) {
+#pragma unroll
+          for (int q = 0; q < NP; ++q) stage[q * count + k] = av[u] * c[q];
+        } else {
+          stage[k] = av[u];
+#pragma unroll
+          for (int q = 0; q < NP; ++q) stage[(1 + q) * count + k] = c[q];
+        }
       }
     }
     __syncthreads();

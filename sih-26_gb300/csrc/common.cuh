@@ -29,6 +29,36 @@ __host__ __device__ __forceinline__ T project(T v, T lo, T hi) {
 
 // Projection onto [lo, hi] when an absent side is an IEEE infinity (lo <= hi): the same
 // value as project() for every non-NaN input, in two min/max instructions.
+// Programmatic dependent launch: a kernel launched with programmatic stream serialization
+// (launch_after, below) may have its blocks placed while the previous kernel in the stream is
+// still finishing. Before it reads anything that kernel wrote, it waits here for that kernel's
+// completion and the visibility of its memory. In a kernel launched the ordinary way the wait
+// returns at once.
+__device__ __forceinline__ void grid_dependency_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// Launches kernel<<<grid, threads, smem, s>>>(args...) with programmatic stream
+// serialization: its blocks are placed on the SMs as the previous kernel's blocks leave them,
+// instead of after the whole kernel and its launch; the kernel must call
+// grid_dependency_wait() before its first read of the previous kernel's results. Returns the
+// launch's error.
+template <typename... Params, typename... Args>
+inline cudaError_t launch_after(void (*kernel)(Params...), int grid, int threads, int smem,
+                                cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(static_cast<unsigned>(grid));
+  cfg.blockDim = dim3(static_cast<unsigned>(threads));
+  cfg.dynamicSmemBytes = static_cast<size_t>(smem);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 __device__ __forceinline__ double clamp_box(double v, double lo, double hi) {
   return fmin(fmax(v, lo), hi);
 }

@@ -46,6 +46,7 @@ __device__ __forceinline__ int grid_stride_begin() {
 __global__ void __launch_bounds__(kChunkThreads, 1) k_primal_f(MixedBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kChunkScratch];
+  grid_dependency_wait();  // the previous kernel's results (launch_after)
   Ctl* ctl = b.ctl;
   // Every control field the pass reads, loaded together before the first test.
   const int done = ctl->done, eval_now = ctl->eval_now, cur = ctl->cur;
@@ -111,6 +112,7 @@ __global__ void __launch_bounds__(kChunkThreads, 1) k_primal_f(MixedBuffers b) {
 __global__ void __launch_bounds__(kChunkThreads, 1) k_dual_f(MixedBuffers b) {
   extern __shared__ __align__(16) unsigned char dsmem[];
   __shared__ double scratch[kChunkScratch];
+  grid_dependency_wait();  // the previous kernel's results (launch_after)
   Ctl* ctl = b.ctl;
   const int done = ctl->done, eval_now = ctl->eval_now, cur = ctl->cur;
   const bool add = ctl->pending_add != 0;
@@ -609,12 +611,15 @@ int mixed_step_smem(int pass, int wmax) {
   return StepSmemF::bytes(kChunkThreads / 32, wmax);
 }
 
+// The two step passes are launched with programmatic stream serialization (launch_after):
+// each occupies a whole SM, and its blocks are placed as the previous kernel's leave, so the
+// launch and the SM's reconfiguration overlap that kernel's last blocks.
 void launch_mixed_primal(const MixedBuffers& b, cudaStream_t s) {
-  k_primal_f<<<b.grid_step_primal, kChunkThreads, b.smem_primal, s>>>(b);
+  launch_after(k_primal_f, b.grid_step_primal, kChunkThreads, b.smem_primal, s, b);
 }
 
 void launch_mixed_dual(const MixedBuffers& b, cudaStream_t s) {
-  k_dual_f<<<b.grid_step_dual, kChunkThreads, b.smem_dual, s>>>(b);
+  launch_after(k_dual_f, b.grid_step_dual, kChunkThreads, b.smem_dual, s, b);
 }
 
 void launch_mixed_step(const MixedBuffers& b, cudaStream_t s) {
