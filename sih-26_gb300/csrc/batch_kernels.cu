@@ -1522,6 +1522,7 @@ __device__ int pcg_sf(const Lines& S, const Lines& F, int nb, const double* h, d
 }
 
 constexpr int kRefinePasses = 3;
+constexpr double kPassReduction = 1e-12;
 
 // S u = h (F = S') by refinement passes around pcg_sf; u holds the starting point on entry
 // and the solution on exit, w.kw[2..6] are used as scratch. Returns the conjugate-gradient
@@ -1558,7 +1559,12 @@ __device__ int solve_square(const Lines& S, const Lines& F, int nb, const double
     const double rnorm = sqrt(rs[0]);
     *rel = hnorm > 0.0 ? rnorm / hnorm : 0.0;
     if (*rel <= tol || pass == kRefinePasses) break;
-    its += pcg_sf(S, F, nb, res, z, r, wv, diag, p, t, scratch, max_it, tol * hnorm / rnorm);
+    // A pass reduces its own residual to the final target, and by kPassReduction at least:
+    // a solve started next to the answer (a polish from the PDHG point, or from a neighbour's
+    // vertex, sankhya_gb300_batch_set_point) must still solve its small correction to full
+    // accuracy, or two neighbouring solves carry different errors of the correction's size.
+    its += pcg_sf(S, F, nb, res, z, r, wv, diag, p, t, scratch, max_it,
+                  fmin(tol * hnorm / rnorm, kPassReduction));
     for (int k = th; k < nb; k += T) u[k] += line_dot(F, k, z);
     __syncthreads();
   }

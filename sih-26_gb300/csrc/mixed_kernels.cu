@@ -33,6 +33,15 @@ constexpr int kSmemF = EvalPipeF::bytes();
 // the column pass, du in the row pass).
 using StepSmemF = ChunkSmem<float, float, 1, kChunkCapF>;
 
+// A value formed by thread 0 and handed to every thread of the block (all threads call it).
+template <typename F>
+__device__ __forceinline__ float block_scalar(F f) {
+  __shared__ float s_value;
+  if (threadIdx.x == 0) s_value = f();
+  __syncthreads();
+  return s_value;
+}
+
 __device__ __forceinline__ void raise_error(Ctl* c) {
   c->error = 1;
   c->done = kFault;
@@ -61,7 +70,10 @@ __global__ void __launch_bounds__(kChunkThreads, 1) k_primal_f(MixedBuffers b) {
   const float* __restrict__ u = b.u[cur];
   float* __restrict__ un = b.u[cur ^ 1];
   const float* __restrict__ v = b.v[cur];
-  const float tau = static_cast<float>(eta / omega);
+  // The step's FP32 scalar, formed once per block: GB300 runs FP64 at 1/64 of the FP32 rate,
+  // so an FP64 division in each of 1,024 threads would hold the FP64 pipe for thousands of
+  // cycles per SM at the start of every launch.
+  const float tau = block_scalar([&] { return static_cast<float>(eta / omega); });
   float mvf = 0.0f;
   // Operands of column j: u, cf, lf, uf and (when the last step is still to be added) u_sum.
   auto load = [&](int j, float* o) {
@@ -126,7 +138,7 @@ __global__ void __launch_bounds__(kChunkThreads, 1) k_dual_f(MixedBuffers b) {
   float* __restrict__ vn = b.v[cur ^ 1];
   const float* __restrict__ au = b.au[cur];
   float* __restrict__ aun = b.au[cur ^ 1];
-  const float sigma = static_cast<float>(eta * omega);
+  const float sigma = block_scalar([&] { return static_cast<float>(eta * omega); });
   const float inv_sigma = 1.0f / sigma;
   float a0 = 0.0f, a1 = 0.0f;  // sum dv^2, sum dv (A du)
   // Operands of row i: v, gu, gl, yhat, A u and (when the last step is still to be added)

@@ -104,7 +104,11 @@ __global__ void __launch_bounds__(kBlockThreads) k_primal(StepBuffers b) {
   double* __restrict__ xn = b.x[cur ^ 1];
   const double* __restrict__ y = b.y[cur];
   const double omega = ctl->omega;
-  const double tau = ctl->eta / omega;
+  // Formed once per block: an FP64 division per thread would hold GB300's slow FP64 pipe.
+  __shared__ double s_tau;
+  if (threadIdx.x == 0) s_tau = ctl->eta / omega;
+  __syncthreads();
+  const double tau = s_tau;
   const bool add = ctl->pending_add != 0;
   double mv[1] = {0.0};  // sum of dx^2
   PrimalPipe pipe;

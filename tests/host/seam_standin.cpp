@@ -14,13 +14,20 @@
 // (standin_set_device), and counts the solves it ran (standin_solve_count), so a test can
 // tell whether SANKHYA's solve() reached the seam or took its own CPU path. Test
 // infrastructure only; nothing here is part of the engine.
+//
+// The batched calls seam/node_batch.cpp makes (batch create, load, solve, solution, ray) are
+// answered the same way, one reference solve per LP. The reference's PDHG detects no
+// infeasibility, so a test marks an LP infeasible itself, with the direction the stand-in
+// returns as its certificate (standin_batch_mark_infeasible).
 #include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <string>
+#include <vector>
 
 #include "sankhya/logging.hpp"
 #include "sankhya/model.hpp"
@@ -34,9 +41,16 @@ struct sankhya_gb300_pdhg {
   bool solved = false;
 };
 
+struct sankhya_gb300_batch {
+  std::vector<sankhya::Model> models;
+  std::vector<sankhya::Solution> solutions;
+  bool solved = false;
+};
+
 namespace {
 
 thread_local std::string g_error;
+std::map<int, std::vector<double>> g_infeasible;  // LP index -> its certificate
 int g_fail_create = 0;
 std::atomic<long long> g_solves{0};
 
@@ -63,6 +77,38 @@ int32_t to_code(sankhya::SolveStatus s) {
     case S::kModelError: return SANKHYA_GB300_MODEL_ERROR;
     default: return SANKHYA_GB300_NUMERICAL_ERROR;
   }
+}
+
+sankhya::Options options_of(const sankhya_gb300_params* p) {
+  sankhya::Options o;
+  o.set_double("pdhg_tolerance", p->tolerance);
+  o.set_int("iteration_limit", p->iteration_limit);
+  o.set_double("time_limit", p->time_limit);
+  o.set_bool("pdhg_restart", p->restart != 0);
+  o.set_bool("pdhg_stop_at_request", p->stop_at_request != 0);
+  o.set_int("random_seed", p->random_seed);
+  return o;
+}
+
+void to_model(const sankhya_gb300_lp* lp, sankhya::Model& m) {
+  m = sankhya::Model();
+  const auto n = static_cast<std::size_t>(lp->cols);
+  const auto rows = static_cast<std::size_t>(lp->rows);
+  m.sense = lp->sense < 0.0 ? sankhya::ObjSense::kMaximize : sankhya::ObjSense::kMinimize;
+  m.objective_offset = lp->objective_offset;
+  m.col_cost.assign(lp->col_cost, lp->col_cost + n);
+  m.col_lower.assign(lp->col_lower, lp->col_lower + n);
+  m.col_upper.assign(lp->col_upper, lp->col_upper + n);
+  m.col_type.assign(n, sankhya::VarType::kContinuous);
+  m.row_lower.assign(lp->row_lower, lp->row_lower + rows);
+  m.row_upper.assign(lp->row_upper, lp->row_upper + rows);
+  m.matrix.reset(lp->rows, lp->cols);
+  for (int32_t j = 0; j < lp->cols; ++j) {
+    for (int32_t k = lp->col_starts[j]; k < lp->col_starts[j + 1]; ++k) {
+      m.matrix.add_entry(lp->row_index[k], j, lp->values[k]);
+    }
+  }
+  m.matrix.finalize(0.0);
 }
 
 }  // namespace
@@ -122,25 +168,7 @@ int sankhya_gb300_pdhg_create(int32_t device, sankhya_gb300_pdhg** out) {
 }
 
 int sankhya_gb300_pdhg_load(sankhya_gb300_pdhg* e, const sankhya_gb300_lp* lp) {
-  sankhya::Model& m = e->model;
-  m = sankhya::Model();
-  const auto n = static_cast<std::size_t>(lp->cols);
-  const auto rows = static_cast<std::size_t>(lp->rows);
-  m.sense = lp->sense < 0.0 ? sankhya::ObjSense::kMaximize : sankhya::ObjSense::kMinimize;
-  m.objective_offset = lp->objective_offset;
-  m.col_cost.assign(lp->col_cost, lp->col_cost + n);
-  m.col_lower.assign(lp->col_lower, lp->col_lower + n);
-  m.col_upper.assign(lp->col_upper, lp->col_upper + n);
-  m.col_type.assign(n, sankhya::VarType::kContinuous);
-  m.row_lower.assign(lp->row_lower, lp->row_lower + rows);
-  m.row_upper.assign(lp->row_upper, lp->row_upper + rows);
-  m.matrix.reset(lp->rows, lp->cols);
-  for (int32_t j = 0; j < lp->cols; ++j) {
-    for (int32_t k = lp->col_starts[j]; k < lp->col_starts[j + 1]; ++k) {
-      m.matrix.add_entry(lp->row_index[k], j, lp->values[k]);
-    }
-  }
-  m.matrix.finalize(0.0);
+  to_model(lp, e->model);
   e->solved = false;
   return SANKHYA_GB300_OK;
 }
@@ -160,13 +188,7 @@ int sankhya_gb300_pdhg_solve(sankhya_gb300_pdhg* e, const sankhya_gb300_params* 
     g_error = "the stand-in runs the reference method only";
     return SANKHYA_GB300_ERROR_OPTION;
   }
-  sankhya::Options o;
-  o.set_double("pdhg_tolerance", p->tolerance);
-  o.set_int("iteration_limit", p->iteration_limit);
-  o.set_double("time_limit", p->time_limit);
-  o.set_bool("pdhg_restart", p->restart != 0);
-  o.set_bool("pdhg_stop_at_request", p->stop_at_request != 0);
-  o.set_int("random_seed", p->random_seed);
+  const sankhya::Options o = options_of(p);
   sankhya::Logger quiet(nullptr);
   e->solution = sankhya::pdhg::solve_pdhg(e->model, o, quiet, nullptr);
   e->solved = true;
@@ -204,6 +226,91 @@ int sankhya_gb300_pdhg_solution(sankhya_gb300_pdhg* e, double* col_value, double
   for (std::size_t i = 0; i < s.row_dual.size(); ++i) {
     if (row_dual) row_dual[i] = s.row_dual[i];
   }
+  return SANKHYA_GB300_OK;
+}
+
+void standin_batch_mark_infeasible(int index, const double* ray, int rows) {
+  g_infeasible[index] = std::vector<double>(ray, ray + rows);
+}
+
+void standin_batch_clear_marks(void) { g_infeasible.clear(); }
+
+int sankhya_gb300_batch_create(int32_t device, sankhya_gb300_batch** out) {
+  (void)device;
+  if (g_fail_create) {
+    g_error = "no usable CUDA device (stand-in)";
+    return SANKHYA_GB300_ERROR_DEVICE;
+  }
+  *out = new sankhya_gb300_batch();
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_batch_destroy(sankhya_gb300_batch* b) {
+  delete b;
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_batch_load(sankhya_gb300_batch* b, int32_t count, const sankhya_gb300_lp* lps) {
+  b->models.assign(static_cast<std::size_t>(count), sankhya::Model());
+  for (int32_t k = 0; k < count; ++k) to_model(&lps[k], b->models[static_cast<std::size_t>(k)]);
+  b->solved = false;
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_batch_solve(sankhya_gb300_batch* b, const sankhya_gb300_params* p,
+                              sankhya_gb300_batch_item* items, double* device_seconds) {
+  if (p->precision != SANKHYA_GB300_FP64 || p->stop_rule != SANKHYA_GB300_STOP_STANDARD) {
+    g_error = "the stand-in runs the reference method only";
+    return SANKHYA_GB300_ERROR_OPTION;
+  }
+  const sankhya::Options o = options_of(p);
+  sankhya::Logger quiet(nullptr);
+  b->solutions.clear();
+  for (std::size_t k = 0; k < b->models.size(); ++k) {
+    b->solutions.push_back(sankhya::pdhg::solve_pdhg(b->models[k], o, quiet, nullptr));
+    ++g_solves;
+    const sankhya::Solution& s = b->solutions.back();
+    sankhya_gb300_batch_item& it = items[k];
+    std::memset(&it, 0, sizeof(it));
+    it.status = g_infeasible.count(static_cast<int>(k)) ? SANKHYA_GB300_INFEASIBLE
+                                                        : to_code(s.status);
+    it.converged = s.status == sankhya::SolveStatus::kOptimal ||
+                   s.status == sankhya::SolveStatus::kFeasible;
+    it.iterations = s.iterations;
+    it.attempts = s.iterations;
+    it.objective = s.objective;
+    it.dual_bound = s.dual_bound;
+  }
+  if (device_seconds != nullptr) *device_seconds = 0.0;
+  b->solved = true;
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_batch_solution(sankhya_gb300_batch* b, int32_t index, double* col_value,
+                                 double* col_dual, double* row_dual) {
+  if (!b->solved || index < 0 || static_cast<std::size_t>(index) >= b->solutions.size()) {
+    g_error = "no such solved LP";
+    return SANKHYA_GB300_ERROR_ARGUMENT;
+  }
+  const auto& s = b->solutions[static_cast<std::size_t>(index)];
+  for (std::size_t j = 0; j < s.col_value.size(); ++j) {
+    if (col_value) col_value[j] = s.col_value[j];
+    if (col_dual) col_dual[j] = s.col_dual[j];
+  }
+  for (std::size_t i = 0; i < s.row_dual.size(); ++i) {
+    if (row_dual) row_dual[i] = s.row_dual[i];
+  }
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_batch_ray(sankhya_gb300_batch* b, int32_t index, double* ray) {
+  if (!b->solved || index < 0 || static_cast<std::size_t>(index) >= b->models.size()) {
+    g_error = "no such solved LP";
+    return SANKHYA_GB300_ERROR_ARGUMENT;
+  }
+  const std::size_t m = static_cast<std::size_t>(b->models[static_cast<std::size_t>(index)].num_rows());
+  const auto found = g_infeasible.find(index);
+  for (std::size_t i = 0; i < m; ++i) ray[i] = found != g_infeasible.end() ? found->second[i] : 0.0;
   return SANKHYA_GB300_OK;
 }
 

@@ -67,3 +67,32 @@ def test_gpu_answers_pass_the_reference_verifier(gpu_write, tmp_path, name):
     print(check.stdout[-600:])
     assert check.returncode == 0, check.stdout[-3000:] + check.stderr[-2000:]
     assert "VERIFIED" in check.stdout, check.stdout[-2000:]
+
+
+def test_node_relaxations_on_the_gpu(tmp_path, built):
+    """`seam/node_batch.cpp` with the engine's real library: the branching nodes of afiro's
+    root (and one node whose fixed columns break a row) solved together by the batched engine.
+    Every node the reference's CPU PDHG solves comes back solved with its objective within
+    1e-6 relative; the broken node never comes back solved: infeasible with a Farkas
+    certificate that checked on the host, or at the iteration limit, since afiro's one-sided
+    rows and columns keep the engine's certificate test from proving it
+    (`tests/host/node_batch_check.cpp`, gpu mode)."""
+    import pyoracle
+
+    flags, sources, core = core_link_args()
+    sources = [s for s in sources if not s.endswith("seam_standin.cpp")]
+    tree = pyoracle.reference_tree()
+    model = os.path.join(tree, "data", "netlib", "afiro.mps")
+    lib_dir = os.path.join(ROOT, "sih-26_gb300", "lib")
+    exe = str(tmp_path / "node_batch_check")
+    cmd = (["g++"] + flags + sources +
+           [os.path.join(ROOT, "sih-26_gb300", "seam", "node_batch.cpp"),
+            os.path.join(ROOT, "tests", "host", "node_batch_check.cpp"), core,
+            f"-L{lib_dir}", "-lsankhya_gb300", f"-Wl,-rpath,{lib_dir}", "-fopenmp", "-lz",
+            "-o", exe])
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr[-3000:]
+    run = subprocess.run([exe, model, "gpu"], capture_output=True, text=True, timeout=900)
+    print(run.stdout[-3000:])
+    assert run.returncode == 0, run.stdout[-3000:] + run.stderr[-2000:]
+    assert run.stdout.strip().endswith("OK"), run.stdout

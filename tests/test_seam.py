@@ -20,7 +20,8 @@ SEAM = os.path.join(ROOT, "sih-26_gb300", "seam")
 REF = pyoracle.REFERENCE_TREE
 
 
-@pytest.mark.parametrize("name", ["pdhg_gpu", "pdhg_multi_gpu", "gpu_memory", "device"])
+@pytest.mark.parametrize("name", ["pdhg_gpu", "pdhg_multi_gpu", "gpu_memory", "device",
+                                  "node_batch"])
 def test_seam_compiles_against_reference_headers(name):
     if not os.path.isdir(os.path.join(REF, "src", "gpu")) or shutil.which("g++") is None:
         pytest.skip("the reference tree (or g++) is not present here")
@@ -173,5 +174,25 @@ def test_reference_unit_tests_of_the_replaced_pieces(tmp_path):
     proc = subprocess.run(cmd, capture_output=True, text=True)
     assert proc.returncode == 0, proc.stderr[-2000:]
     run = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert run.returncode == 0, run.stdout[-2000:] + run.stderr[-2000:]
+    assert run.stdout.strip().endswith("OK"), run.stdout
+
+
+def test_node_relaxations_through_the_seam(tmp_path):
+    """`tests/host/node_batch_check.cpp` on afiro, through `seam/node_batch.cpp` and the C-ABI
+    stand-in: twelve branching nodes on the root's fractional columns come back as the
+    reference's solve_pdhg of each node, bit for bit; a node with a checked Farkas certificate
+    is infeasible, one whose certificate does not check is a numerical error; wrong bounds are
+    a model error; no engine is a numerical error for every node."""
+    flags, sources, core = core_link_args()
+    model = os.path.join(REF, "data", "netlib", "afiro.mps")
+    exe = str(tmp_path / "node_batch_check")
+    cmd = (["g++"] + flags + sources +
+           [os.path.join(SEAM, "node_batch.cpp"),
+            os.path.join(ROOT, "tests", "host", "node_batch_check.cpp"), core, "-fopenmp",
+            "-lz", "-o", exe])
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr[-2000:]
+    run = subprocess.run([exe, model, "standin"], capture_output=True, text=True, timeout=600)
     assert run.returncode == 0, run.stdout[-2000:] + run.stderr[-2000:]
     assert run.stdout.strip().endswith("OK"), run.stdout
