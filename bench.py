@@ -164,8 +164,10 @@ def host_cpu():
 # What the CPU baseline runs: the C restatement of the reference's PDHG, which the tests hold
 # bit-identical to the reference's own sources compiled on x86-64.
 CPU_BASELINE_PORT_OF = ("sankhya::pdhg::solve_pdhg (src/pdhg/pdhg.cpp) restated in C; "
-                        "bit-identical to the reference's own build on x86-64 "
+                        "bit-identical to the reference's own build "
                         "(tests/test_oracle_vs_reference.py)")
+CPU_BASELINE_REFERENCE = ("sankhya::pdhg::solve_pdhg (src/pdhg/pdhg.cpp), the reference's own "
+                          "sources compiled on this host (oracle/_ref/libsankhya_ref.so)")
 
 
 def pinned_lp(lp):
@@ -599,6 +601,9 @@ def workload_config(lp, precision):
 
 
 def _oracle(threads):
+    """The CPU implementation the baselines time: the reference's own PDHG compiled from its
+    sources (oracle/_ref, built by __graft_entry__.build from the reference tree or its staged
+    copy) where it is built, else the oracle's C restatement of it."""
     import ctypes
     import pyoracle
 
@@ -608,7 +613,16 @@ def _oracle(threads):
         ctypes.CDLL("libgomp.so.1").omp_set_num_threads(int(threads))
     except (OSError, AttributeError):
         pass
-    return pyoracle.Oracle()
+    return pyoracle.Oracle(reference=pyoracle.reference_available())
+
+
+def cpu_kind():
+    """("reference", what it is) when the reference's own build is there, else ("port", ...)."""
+    import pyoracle
+
+    if pyoracle.reference_available():
+        return "reference", CPU_BASELINE_REFERENCE
+    return "port", CPU_BASELINE_PORT_OF
 
 
 def relative_kkt(residuals):
@@ -773,9 +787,10 @@ def main():
                 "ms_per_step": 1e3 * value, "higher_is_better": False, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                 "config": workload_config(lp, "fp64"),
-                "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
-                                 "port_of": CPU_BASELINE_PORT_OF, "host": host_cpu(),
-                                 "sample": f"per timed step: oracle setup + "
+                "cpu_baseline": {"value": value, "unit": "s", "cores": threads,
+                                 "kind": cpu_kind()[0], "port_of": cpu_kind()[1],
+                                 "host": host_cpu(),
+                                 "sample": f"per timed step: {cpu_kind()[0]} setup + "
                                            f"{REFERENCE_SAMPLE_ITERATIONS} FP64 iterations on "
                                            f"{threads} threads; warm-up steps: setup only",
                                  "measured": {"setup_s": setup, "s_per_iteration": per_it,
@@ -889,9 +904,9 @@ def main():
             limited = cpu_time_limited(lp, threads, CPU_TIME_LIMIT)
         except Exception as exc:  # noqa: BLE001
             limited = {"error": f"{type(exc).__name__}: {exc}"}
-        cpu = {"value": setup + per_it * its, "unit": "s", "cores": threads, "kind": "port",
-               "port_of": CPU_BASELINE_PORT_OF, "host": host_cpu(),
-               "sample": f"oracle setup + {args.cpu_iterations} FP64 iterations on {threads} "
+        cpu = {"value": setup + per_it * its, "unit": "s", "cores": threads,
+               "kind": cpu_kind()[0], "port_of": cpu_kind()[1], "host": host_cpu(),
+               "sample": f"{cpu_kind()[0]} setup + {args.cpu_iterations} FP64 iterations on {threads} "
                          f"threads ({sample_s:.1f} s of CPU work), extrapolated to {its} "
                          f"iterations ({its_from})",
                "extrapolated": True, "setup_s": setup, "s_per_iteration": per_it,

@@ -138,7 +138,7 @@ def test_default_line(monkeypatch):
     assert roof["frac"] == pytest.approx(roof["achieved"] / roof["peak"])
     assert roof["traffic"] is None or roof["traffic"] > 0
     cpu = line["cpu_baseline"]
-    assert cpu["kind"] == "port" and cpu["cores"] >= 1 and cpu["value"] > 0
+    assert cpu["kind"] in ("port", "reference") and cpu["cores"] >= 1 and cpu["value"] > 0
     assert cpu["single_thread"].get("cores") == 1
     assert cpu["host"]["machine"] and cpu["host"]["logical_cpus"] >= cpu["cores"]
     e2e = line["e2e"]
