@@ -318,12 +318,13 @@ SGB_API int sankhya_gb300_batch_ray(sankhya_gb300_batch* batch, int32_t index, d
  * dl_dx[k] (cols), dl_dy[k] (rows) and dl_df[k], returns dL/dc, dL/d(row_lower),
  * dL/d(row_upper), dL/d(col_lower), dL/d(col_upper) by implicit differentiation of the
  * optimum: at the active set the PDHG fixed point reduces to two square linear systems with
- * the basis matrix A_RB, solved on the device by preconditioned conjugate gradients on the
- * normal equations (masked SpMVs). An equality row's dL/db is dl_drl + dl_dru (only the side
- * its multiplier's sign names is nonzero). Any upstream pointer may be NULL (zero); any
- * output pointer may be NULL. Minimisation LPs only (status 3 otherwise). */
+ * the basis matrix A_RB, solved on the device on a compact copy of A_RB by preconditioned
+ * conjugate gradients on its normal equations, with refinement passes. An equality row's
+ * dL/db is dl_drl + dl_dru (only the side its multiplier's sign names is nonzero). Any
+ * upstream pointer may be NULL (zero); any output pointer may be NULL. Minimisation and
+ * maximisation LPs alike (the sense is folded as src/pdhg/pdhg.cpp:95-111 folds it). */
 typedef struct sankhya_gb300_adjoint_info {
-  int32_t status;      /* 0 ok, 1 degenerate optimum (|B| != |R|), 2 CG not converged, 3 max */
+  int32_t status;      /* 0 ok, 1 degenerate optimum (|B| != |R|), 2 CG not converged */
   int32_t basic_cols;  /* |B| */
   int32_t active_rows; /* |R| */
   int32_t iterations[2];
@@ -333,11 +334,11 @@ typedef struct sankhya_gb300_adjoint_info {
 /* Active-set polish of the last batch solve (no reference counterpart; it plays the part
  * of the reference's PDHG -> interior-point polish hand-off, src/core/solve.cpp:239-308, for
  * nondegenerate LPs): at each converged LP's active sets, x_B and the multipliers are
- * re-solved from the basis matrix A_RB (masked conjugate gradients on the device); the
- * polished point replaces the reported one when it is primal and dual feasible within 1e-9,
- * and items (may be NULL) receive the new status, objective and residuals. info[k].status:
- * 0 polished, 1 degenerate optimum, 2 CG not converged, 3 maximisation, 4 LP not converged,
- * 5 polished point rejected. Minimisation LPs only. */
+ * re-solved from the basis matrix A_RB (the adjoint's square solves, started from the
+ * reported point); the polished point replaces the reported one when it is primal and dual
+ * feasible within 1e-9, and items (may be NULL) receive the new status, objective and
+ * residuals. info[k].status: 0 polished, 1 degenerate optimum, 2 CG not converged, 4 LP not
+ * converged, 5 polished point rejected. */
 SGB_API int sankhya_gb300_batch_polish(sankhya_gb300_batch* batch,
                                        sankhya_gb300_batch_item* items,
                                        sankhya_gb300_adjoint_info* info);

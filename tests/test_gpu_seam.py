@@ -96,3 +96,27 @@ def test_node_relaxations_on_the_gpu(tmp_path, built):
     print(run.stdout[-3000:])
     assert run.returncode == 0, run.stdout[-3000:] + run.stderr[-2000:]
     assert run.stdout.strip().endswith("OK"), run.stdout
+
+
+def test_gradients_through_the_seam(tmp_path, built):
+    """`seam/lp_gradients.cpp` with the engine's real library (`tests/host/gradients_check.cpp`):
+    a planted LP with a unique, nondegenerate optimum, minimised and (with its cost negated)
+    maximised; for L = f* the gradients are known exactly (dL/dc = x*, dL/db = y*, dL/dbound =
+    the active bounds' reduced costs) and must hold to 1e-8, and the gradient file written by
+    write_gradients has one line per column and per row."""
+    flags, sources, core = core_link_args()
+    sources = [s for s in sources if not s.endswith("seam_standin.cpp")]
+    lib_dir = os.path.join(ROOT, "sih-26_gb300", "lib")
+    exe = str(tmp_path / "gradients_check")
+    cmd = (["g++"] + flags + sources +
+           [os.path.join(ROOT, "sih-26_gb300", "seam", "lp_gradients.cpp"),
+            os.path.join(ROOT, "tests", "host", "gradients_check.cpp"), core,
+            f"-L{lib_dir}", "-lsankhya_gb300", f"-Wl,-rpath,{lib_dir}", "-fopenmp", "-lz",
+            "-o", exe])
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr[-3000:]
+    run = subprocess.run([exe, str(tmp_path / "gradients.txt")], capture_output=True, text=True,
+                         timeout=900)
+    print(run.stdout[-3000:])
+    assert run.returncode == 0, run.stdout[-3000:] + run.stderr[-2000:]
+    assert run.stdout.strip().endswith("OK"), run.stdout
