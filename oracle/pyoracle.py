@@ -231,10 +231,14 @@ class Oracle:
         else:
             self._solve(*args)
         del keep
+        residuals = res.final_residuals.as_dict()
+        if self.reference:
+            # The reference's Solution carries no residuals: evaluate its reported point with
+            # its own evaluate (row_dual = -sense * y, src/pdhg/pdhg.cpp:495-499).
+            residuals = self.evaluate(lp, x, -lp.sense * y)[0]
         return OracleSolution(res.status, STATUS_NAMES.get(res.status, str(res.status)),
                               res.iterations, res.restarts, res.objective, res.dual_bound,
-                              res.final_residuals.as_dict(), x, d, y, res.solve_seconds,
-                              res.spectral_norm, message)
+                              residuals, x, d, y, res.solve_seconds, res.spectral_norm, message)
 
     def build_scaling(self, lp, ruiz_iterations=10):
         c, keep = self._clp(lp)

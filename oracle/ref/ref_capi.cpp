@@ -28,8 +28,11 @@
 #include "sankhya/model.hpp"
 #include "sankhya/options.hpp"
 #include "sankhya/pdhg.hpp"
+#include "sankhya/qp.hpp"
+#include "qp/convexity.hpp"
 
 #include "../pdhg_oracle.h"
+#include "../qp_oracle.h"
 
 namespace {
 
@@ -55,6 +58,22 @@ sankhya::Model to_model(const orc_lp* lp) {
   // Drop tolerance zero keeps every entry the caller passed, explicit zeros included, so the
   // pattern matches the CSC arrays one for one.
   model.matrix.finalize(0.0);
+  return model;
+}
+
+// The Model of a QP: the LP part as to_model builds it, and the Hessian's stored triangle as
+// Model::hessian (n x n CSC), entries kept one for one.
+sankhya::Model to_qp_model(const orc_qp* qp) {
+  sankhya::Model model = to_model(&qp->lp);
+  model.hessian.reset(qp->lp.cols, qp->lp.cols);
+  if (qp->hessian_starts != nullptr) {
+    for (int32_t j = 0; j < qp->lp.cols; ++j) {
+      for (int32_t k = qp->hessian_starts[j]; k < qp->hessian_starts[j + 1]; ++k) {
+        model.hessian.add_entry(qp->hessian_index[k], j, qp->hessian_values[k]);
+      }
+    }
+  }
+  model.hessian.finalize(0.0);
   return model;
 }
 
@@ -136,6 +155,59 @@ int32_t ref_solve_pdhg(const orc_lp* lp, const orc_params* params, orc_result* r
     std::snprintf(message, static_cast<std::size_t>(message_capacity), "%s", s.message.c_str());
   }
   return result->status;
+}
+
+// The reference's convex-QP engine, convexity gate included (src/qp/qp_condat_vu.cpp:164-362).
+// result->primal_residual / dual_residual are not Solution fields and stay -1.
+int32_t ref_solve_qp(const orc_qp* qp, const orc_qp_params* params, orc_qp_result* result,
+                     double* col_value, double* col_dual, double* row_dual, char* message,
+                     int32_t message_capacity) {
+  std::memset(result, 0, sizeof(*result));
+  result->primal_residual = -1.0;
+  result->dual_residual = -1.0;
+  const sankhya::Model model = to_qp_model(qp);
+  sankhya::Options options;
+  options.set_bool("log_to_console", false);
+  options.set_double("qp_tolerance", params->tolerance);
+  options.set_int("iteration_limit", params->iteration_limit);
+  if (params->time_limit < 1e300) options.set_double("time_limit", params->time_limit);
+  options.set_int("random_seed", params->random_seed);
+  sankhya::Logger logger(nullptr);
+  const sankhya::Solution s = sankhya::qp::solve_convex_qp(model, options, logger, nullptr);
+  result->status = status_code(s.status);
+  result->iterations = s.iterations;
+  result->objective = s.objective;
+  result->solve_seconds = s.solve_seconds;
+  const auto n = static_cast<std::size_t>(qp->lp.cols);
+  const auto m = static_cast<std::size_t>(qp->lp.rows);
+  if (col_value != nullptr && s.col_value.size() == n) {
+    std::memcpy(col_value, s.col_value.data(), n * sizeof(double));
+  }
+  if (col_dual != nullptr && s.col_dual.size() == n) {
+    std::memcpy(col_dual, s.col_dual.data(), n * sizeof(double));
+  }
+  if (row_dual != nullptr && s.row_dual.size() == m) {
+    std::memcpy(row_dual, s.row_dual.data(), m * sizeof(double));
+  }
+  if (message != nullptr && message_capacity > 0) {
+    std::snprintf(message, static_cast<std::size_t>(message_capacity), "%s", s.message.c_str());
+  }
+  return result->status;
+}
+
+// The reference's convexity decision (src/qp/convexity.cpp:177-210): 0 convex, 1 indefinite,
+// 2 unverified; `detail` receives its text.
+int32_t ref_check_convexity(const orc_qp* qp, char* detail, int32_t detail_capacity) {
+  const sankhya::Model model = to_qp_model(qp);
+  const sankhya::qp::ConvexityResult r = sankhya::qp::check_convexity(model);
+  if (detail != nullptr && detail_capacity > 0) {
+    std::snprintf(detail, static_cast<std::size_t>(detail_capacity), "%s", r.detail.c_str());
+  }
+  switch (r.verdict) {
+    case sankhya::qp::Convexity::kConvex: return 0;
+    case sankhya::qp::Convexity::kIndefinite: return 1;
+    default: return 2;
+  }
 }
 
 void ref_build_scaling(const orc_lp* lp, const double* min_space_cost, int32_t ruiz_iterations,
@@ -266,6 +338,30 @@ void ref_model_arrays(const void* handle, int32_t* col_starts, int32_t* row_inde
   std::memcpy(col_upper, m.col_upper.data(), m.col_upper.size() * sizeof(double));
   std::memcpy(row_lower, m.row_lower.data(), m.row_lower.size() * sizeof(double));
   std::memcpy(row_upper, m.row_upper.data(), m.row_upper.size() * sizeof(double));
+}
+
+// The Hessian of a read Model (its stored lower triangle, CSC): the count of stored entries,
+// then the arrays (cols + 1 starts, that many row indices and values).
+int64_t ref_model_hessian_nonzeros(const void* handle) {
+  return static_cast<const ref_model*>(handle)->model.hessian.num_nonzeros();
+}
+
+void ref_model_hessian(const void* handle, int32_t* starts, int32_t* index, double* values) {
+  const sankhya::Model& m = static_cast<const ref_model*>(handle)->model;
+  const int32_t n = m.num_cols();
+  int32_t at = 0;
+  for (int32_t j = 0; j < n; ++j) {
+    starts[j] = at;
+    if (j < m.hessian.num_cols()) {
+      const sankhya::ColumnView c = m.hessian.column(j);
+      for (sankhya::Index k = 0; k < c.size; ++k) {
+        index[at] = static_cast<int32_t>(c.rows[k]);
+        values[at] = c.values[k];
+        ++at;
+      }
+    }
+  }
+  starts[n] = at;
 }
 
 void ref_model_free(void* handle) { delete static_cast<ref_model*>(handle); }
