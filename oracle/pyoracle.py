@@ -1,6 +1,7 @@
 """ctypes binding of the checker libraries (TEST INFRASTRUCTURE ONLY).
 
-``Oracle()`` loads oracle/liboracle.so, the C restatement of the reference PDHG;
+``Oracle()`` loads oracle/liboracle.so, the C restatements of the reference PDHG and of its
+convex-QP engine;
 ``Oracle(reference=True)`` loads oracle/_ref/libsankhya_ref.so, the reference's own sources
 compiled by ``make -C oracle ref`` (only where the reference tree exists). Both expose the
 same calls, so a test can run them side by side. Only tests/, __graft_entry__.smoke() and
@@ -84,17 +85,53 @@ class OracleSolution:
     message: str = ""
 
 
+class CQp(ctypes.Structure):
+    _fields_ = [("lp", CLp), ("hessian_starts", _I), ("hessian_index", _I),
+                ("hessian_values", _D)]
+
+
+class CQpParams(ctypes.Structure):
+    _fields_ = [("tolerance", ctypes.c_double), ("iteration_limit", ctypes.c_int64),
+                ("time_limit", ctypes.c_double), ("random_seed", ctypes.c_int64)]
+
+
+class CQpResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("ceiling", ctypes.c_int32),
+                ("iterations", ctypes.c_int64)] + [(k, ctypes.c_double) for k in (
+                    "primal_residual", "dual_residual", "norm_a", "norm_q", "tau", "sigma",
+                    "objective", "solve_seconds")]
+
+
+@dataclass
+class QpSolution:
+    status: int
+    status_name: str
+    iterations: int
+    objective: float
+    col_value: np.ndarray
+    col_dual: np.ndarray
+    row_dual: np.ndarray
+    solve_seconds: float
+    primal_residual: float = float("nan")  # restatement only (the last check's)
+    dual_residual: float = float("nan")
+    norm_a: float = float("nan")
+    norm_q: float = float("nan")
+    tau: float = float("nan")
+    sigma: float = float("nan")
+    message: str = ""
+
+
 def build(reference: bool = False) -> None:
     """Compile the restatement (always) and the reference library (when asked, from the
     reference tree or, on a machine without it, from its staged copy). A failure to build the
     reference from the staged copy is reported and left: the tests that need it skip, and the
     CPU baseline falls back to the restatement."""
-    src = os.path.join(HERE, "pdhg_oracle.c")
+    srcs = [os.path.join(HERE, f) for f in ("pdhg_oracle.c", "qp_oracle.c")]
+    deps = srcs + [s[:-1] + "h" for s in srcs]
     if (not os.path.exists(ORACLE_LIB)
-            or os.path.getmtime(ORACLE_LIB) < max(os.path.getmtime(src),
-                                                   os.path.getmtime(src[:-1] + "h"))):
+            or os.path.getmtime(ORACLE_LIB) < max(os.path.getmtime(d) for d in deps)):
         subprocess.run(["gcc", "-O2", "-fPIC", "-std=c11", "-ffp-contract=off", "-fopenmp",
-                        "-shared", "-o", ORACLE_LIB, src, "-lm"], check=True)
+                        "-shared", "-o", ORACLE_LIB] + srcs + ["-lm"], check=True)
     if not reference:
         return
     if os.path.isdir(os.path.join(REFERENCE_TREE, "src", "pdhg")):
@@ -240,6 +277,76 @@ class Oracle:
                               res.iterations, res.restarts, res.objective, res.dual_bound,
                               residuals, x, d, y, res.solve_seconds, res.spectral_norm, message)
 
+    # ---- Convex QP (src/qp/qp_condat_vu.cpp; the restatement in qp_oracle.c) ----
+
+    @staticmethod
+    def _cqp(qp):
+        qp = qp.contiguous()
+        c, keep = Oracle._clp(qp.lp)
+        cq = CQp(c, _ptr(qp.hessian_starts, ctypes.c_int32), _ptr(qp.hessian_index, ctypes.c_int32),
+                 _ptr(qp.hessian_values, ctypes.c_double))
+        return cq, (qp, keep)
+
+    def solve_qp(self, qp, tolerance=1e-8, iteration_limit=-1, time_limit=None,
+                 random_seed=0) -> QpSolution:
+        """The reference's solve_convex_qp (reference=True: its own build, convexity gate
+        included) or the restatement orc_solve_qp (which has no convexity gate)."""
+        cq, keep = self._cqp(qp)
+        params = CQpParams(tolerance, iteration_limit,
+                           1e308 if time_limit is None else time_limit, random_seed)
+        res = CQpResult()
+        x = np.zeros(qp.cols)
+        d = np.zeros(qp.cols)
+        y = np.zeros(qp.rows)
+        f = getattr(self.lib, ("ref_" if self.reference else "orc_") + "solve_qp")
+        args = [ctypes.byref(cq), ctypes.byref(params), ctypes.byref(res),
+                _ptr(x, ctypes.c_double), _ptr(d, ctypes.c_double), _ptr(y, ctypes.c_double)]
+        message = ""
+        if self.reference:
+            f.argtypes = [ctypes.POINTER(CQp), ctypes.POINTER(CQpParams),
+                          ctypes.POINTER(CQpResult), _D, _D, _D, ctypes.c_char_p, ctypes.c_int32]
+            f.restype = ctypes.c_int32
+            buf = ctypes.create_string_buffer(4096)
+            f(*args, buf, 4096)
+            message = buf.value.decode(errors="replace")
+        else:
+            f.argtypes = [ctypes.POINTER(CQp), ctypes.POINTER(CQpParams),
+                          ctypes.POINTER(CQpResult), _D, _D, _D]
+            f.restype = ctypes.c_int32
+            f(*args)
+        del keep
+        out = QpSolution(res.status, STATUS_NAMES.get(res.status, str(res.status)),
+                         res.iterations, res.objective, x, d, y, res.solve_seconds,
+                         message=message)
+        if not self.reference:
+            for k in ("primal_residual", "dual_residual", "norm_a", "norm_q", "tau", "sigma"):
+                setattr(out, k, getattr(res, k))
+        return out
+
+    def qp_norms(self, qp, seed=0):
+        """(||A||, ||Q||) by the QP engine's two power iterations (restatement only)."""
+        cq, keep = self._cqp(qp)
+        q = keep[0]
+        self.lib.orc_qp_spectral_norm.argtypes = [ctypes.c_int32, ctypes.c_int32, _I, _I, _D,
+                                                  ctypes.c_uint32]
+        self.lib.orc_qp_spectral_norm.restype = ctypes.c_double
+        self.lib.orc_qp_hessian_norm.argtypes = [ctypes.POINTER(CQp), ctypes.c_uint32]
+        self.lib.orc_qp_hessian_norm.restype = ctypes.c_double
+        a = self.lib.orc_qp_spectral_norm(q.rows, q.cols, cq.lp.col_starts, cq.lp.row_index,
+                                          cq.lp.values, seed)
+        return a, self.lib.orc_qp_hessian_norm(ctypes.byref(cq), seed)
+
+    def check_convexity(self, qp):
+        """(verdict, detail) of the reference's check_convexity (src/qp/convexity.cpp:177):
+        0 convex, 1 indefinite, 2 unverified. Reference only."""
+        cq, keep = self._cqp(qp)
+        f = self.lib.ref_check_convexity
+        f.argtypes = [ctypes.POINTER(CQp), ctypes.c_char_p, ctypes.c_int32]
+        f.restype = ctypes.c_int32
+        buf = ctypes.create_string_buffer(1024)
+        verdict = f(ctypes.byref(cq), buf, 1024)
+        return verdict, buf.value.decode(errors="replace")
+
     def build_scaling(self, lp, ruiz_iterations=10):
         c, keep = self._clp(lp)
         m, n = lp.rows, lp.cols
@@ -362,6 +469,34 @@ class Oracle:
         if not handle:
             raise ValueError(f"{path}: {err.value.decode(errors='replace')}")
         return self._model_from_handle(handle, os.path.basename(path))[0]
+
+    def read_qp(self, path):
+        """The QP in an MPS file with a QUADOBJ section, as the reference's reader builds it:
+        the LP part and Model::hessian's stored triangle."""
+        from sankhya_gb300.model import QP
+
+        lib = self._model_api()
+        lib.ref_model_hessian_nonzeros.argtypes = [ctypes.c_void_p]
+        lib.ref_model_hessian_nonzeros.restype = ctypes.c_int64
+        lib.ref_model_hessian.argtypes = [ctypes.c_void_p, _I, _I, _D]
+        lib.ref_model_hessian.restype = None
+        err = ctypes.create_string_buffer(1024)
+        handle = lib.ref_model_read(os.fsencode(path), err, 1024)
+        if not handle:
+            raise ValueError(f"{path}: {err.value.decode(errors='replace')}")
+        rows, cols = ctypes.c_int32(), ctypes.c_int32()
+        nnz, optimum = ctypes.c_int64(), ctypes.c_int64()
+        sense, offset = ctypes.c_double(), ctypes.c_double()
+        lib.ref_model_shape(handle, ctypes.byref(rows), ctypes.byref(cols), ctypes.byref(nnz),
+                            ctypes.byref(sense), ctypes.byref(offset), ctypes.byref(optimum))
+        hz = lib.ref_model_hessian_nonzeros(handle)
+        hs = np.zeros(cols.value + 1, np.int32)
+        hi = np.zeros(hz, np.int32)
+        hv = np.zeros(hz)
+        lib.ref_model_hessian(handle, _ptr(hs, ctypes.c_int32), _ptr(hi, ctypes.c_int32),
+                              _ptr(hv, ctypes.c_double))
+        lp = self._model_from_handle(handle, os.path.basename(path))[0]
+        return QP(lp, hs, hi, hv, os.path.basename(path))
 
     def kkt_lp(self, seed, trial, max_rows=8, max_cols=8):
         """(LP, exact optimal objective): the trial-th instance of the reference's generator
