@@ -350,6 +350,88 @@ SGB_API int sankhya_gb300_batch_adjoint(sankhya_gb300_batch* batch,
                                         double* const* dl_dl, double* const* dl_du,
                                         sankhya_gb300_adjoint_info* info);
 
+/* ---- Convex QP --------------------------------------------------------------------------
+ * The reference's convex-QP engine on the device: Condat-Vu's primal-dual splitting with a
+ * forward step on the quadratic term (src/qp/qp_condat_vu.cpp:164-362), every iterate
+ * resident on the GPU. It replaces the body of
+ *     Solution sankhya::qp::solve_convex_qp(const Model&, const Options&, Logger&,
+ *                                           SolveControl*)          (include/sankhya/qp.hpp:20)
+ * behind the seam sankhya::gpu::solve_convex_qp_gpu (sih-26_gb300/seam/qp_gpu.cpp), which runs
+ * the reference's own convexity test (src/qp/convexity.cpp:177) before it calls these
+ * functions. The engine itself refuses only what it can decide cheaply: a Hessian with a
+ * diagonal entry that is negative in minimisation sense (sense * Q_jj below -1e-10 times the
+ * largest |Q_jj|, or -1e-10 when that is under 1; the first certificate check_convexity_dense
+ * looks for, src/qp/convexity.cpp:89-100) fails to load with SANKHYA_GB300_ERROR_MODEL. A
+ * caller that bypasses the seam owns the rest of the convexity decision. */
+typedef struct sankhya_gb300_qp sankhya_gb300_qp; /* opaque engine handle */
+
+/* A QP in sankhya::Model's layout: the LP part as sankhya_gb300_lp, and Model::hessian, the
+ * stored lower triangle of the symmetric Q as a cols x cols CSC (int32 indices, FP64
+ * values), so that the objective is objective_offset + c'x + 0.5 x'Qx and a stored
+ * off-diagonal entry (i, j) stands for both Q_ij and Q_ji. hessian_starts may be NULL for no
+ * quadratic term. */
+typedef struct sankhya_gb300_qp_problem {
+  sankhya_gb300_lp lp;
+  const int32_t* hessian_starts; /* cols + 1, or NULL */
+  const int32_t* hessian_index;
+  const double* hessian_values;
+} sankhya_gb300_qp_problem;
+
+typedef struct sankhya_gb300_qp_params {
+  double tolerance;         /* qp_tolerance: primal and dual residual bound */
+  int64_t iteration_limit;  /* iteration_limit; < 0: the engine's ceiling of 1,000,000 */
+  double time_limit;        /* seconds; <= 0 is a zero budget, >= 1e300 means none */
+  int64_t random_seed;      /* random_seed (both power-iteration starts) */
+  int32_t periods_per_poll; /* 50-iteration check periods per CUDA-graph launch; 0 = auto */
+  int32_t column_lanes;     /* threads per column in the column pass: 1..32, 0 = auto */
+  int32_t row_lanes;        /* threads per row in the row pass: 1..32, 0 = auto */
+  int32_t reserved;
+  const volatile int32_t* interrupt; /* an interrupt flag, polled; may be NULL */
+  sankhya_gb300_log_fn log;  /* every 5,000 iterations, as the reference logs; may be NULL */
+  void* log_user;
+  sankhya_gb300_poll_fn poll; /* may be NULL */
+  void* poll_user;
+} sankhya_gb300_qp_params;
+
+typedef struct sankhya_gb300_qp_result {
+  int32_t status;  /* OPTIMAL, ITERATION_LIMIT, TIME_LIMIT or INTERRUPTED */
+  int32_t ceiling; /* 1 when the iteration limit was the engine's own ceiling */
+  int64_t iterations;
+  double primal_residual; /* max row-bound violation at the last check; -1 before the first */
+  double dual_residual;   /* max |x - proj(x - gradient)| at the last check; -1 before it */
+  double norm_a, norm_q;  /* the power-iteration estimates of ||A|| and ||Q|| */
+  double tau, sigma;      /* the step sizes */
+  double objective;       /* objective_offset + c'x + 0.5 x'Qx at the reported point */
+  double setup_seconds;   /* norms and step sizes, on the device */
+  double loop_seconds;    /* the iterations */
+  double solve_seconds;   /* the whole call, host clock */
+  double device_seconds;  /* the whole solve, CUDA events on the engine's stream */
+  int64_t kernel_launches; /* engine kernels launched by this solve (graph nodes included) */
+  int32_t column_lanes, row_lanes; /* the lanes the passes ran with */
+  char message[256];
+} sankhya_gb300_qp_result;
+
+SGB_API int sankhya_gb300_qp_create(int32_t device, sankhya_gb300_qp** out);
+SGB_API int sankhya_gb300_qp_destroy(sankhya_gb300_qp* engine);
+/* Copies the QP to the device: A as CSC and CSR, Q as the full symmetric matrix by rows.
+ * Fails with SANKHYA_GB300_ERROR_MODEL on the LP part's defects (as sankhya_gb300_pdhg_load,
+ * an infinite cost included), on a Hessian whose structure is not well formed or whose values
+ * are not finite, and on a negative diagonal entry as above. */
+SGB_API int sankhya_gb300_qp_load(sankhya_gb300_qp* engine,
+                                  const sankhya_gb300_qp_problem* problem);
+SGB_API int sankhya_gb300_qp_solve(sankhya_gb300_qp* engine,
+                                   const sankhya_gb300_qp_params* params,
+                                   sankhya_gb300_qp_result* result);
+/* The reported point of the last solve, filled as solve_convex_qp fills Solution
+ * (src/qp/qp_condat_vu.cpp:343-353): col_value = x, col_dual = c + Qx + sense * A'y,
+ * row_dual = -sense * y. Any pointer may be NULL. */
+SGB_API int sankhya_gb300_qp_solution(sankhya_gb300_qp* engine, double* col_value,
+                                      double* col_dual, double* row_dual);
+/* Measurement hook: `reps` iterations on the state the last solve left, each pass bracketed
+ * by CUDA events on the engine's stream; ms[0] = mean column pass, ms[1] = mean row pass, in
+ * milliseconds. The solve's point is restored afterwards. */
+SGB_API int sankhya_gb300_qp_time_kernels(sankhya_gb300_qp* engine, int32_t reps, double* ms);
+
 #ifdef __cplusplus
 }
 #endif

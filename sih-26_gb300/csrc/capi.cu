@@ -13,6 +13,7 @@
 
 #include "batch_engine.hpp"
 #include "engine.hpp"
+#include "qp_engine.hpp"
 #include "sankhya_gb300.h"
 
 struct sankhya_gb300_pdhg {
@@ -21,6 +22,10 @@ struct sankhya_gb300_pdhg {
 
 struct sankhya_gb300_batch {
   sgb::BatchEngine* engine;
+};
+
+struct sankhya_gb300_qp {
+  sgb::QpEngine* engine;
 };
 
 namespace {
@@ -268,6 +273,55 @@ SGB_API int sankhya_gb300_batch_polish(sankhya_gb300_batch* batch,
                                        sankhya_gb300_adjoint_info* info) {
   if (batch == nullptr) return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null batch");
   return guarded([&] { batch->engine->polish(items, info); });
+}
+
+// ---- Convex QP ----
+
+SGB_API int sankhya_gb300_qp_create(int32_t device, sankhya_gb300_qp** out) {
+  if (out == nullptr) return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null output handle");
+  *out = nullptr;
+  return guarded([&] {
+    sgb::QpEngine* e = new sgb::QpEngine(device);
+    *out = new sankhya_gb300_qp{e};
+  });
+}
+
+SGB_API int sankhya_gb300_qp_destroy(sankhya_gb300_qp* engine) {
+  if (engine == nullptr) return SANKHYA_GB300_OK;
+  return guarded([&] {
+    delete engine->engine;
+    delete engine;
+  });
+}
+
+SGB_API int sankhya_gb300_qp_load(sankhya_gb300_qp* engine,
+                                  const sankhya_gb300_qp_problem* problem) {
+  if (engine == nullptr || problem == nullptr) {
+    return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null engine or QP");
+  }
+  return guarded([&] { engine->engine->load(*problem); });
+}
+
+SGB_API int sankhya_gb300_qp_solve(sankhya_gb300_qp* engine,
+                                   const sankhya_gb300_qp_params* params,
+                                   sankhya_gb300_qp_result* result) {
+  if (engine == nullptr || params == nullptr || result == nullptr) {
+    return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null engine, parameters or result");
+  }
+  return guarded([&] { engine->engine->solve(*params, result); });
+}
+
+SGB_API int sankhya_gb300_qp_solution(sankhya_gb300_qp* engine, double* col_value,
+                                      double* col_dual, double* row_dual) {
+  if (engine == nullptr) return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null engine");
+  return guarded([&] { engine->engine->solution(col_value, col_dual, row_dual); });
+}
+
+SGB_API int sankhya_gb300_qp_time_kernels(sankhya_gb300_qp* engine, int32_t reps, double* ms) {
+  if (engine == nullptr || ms == nullptr) {
+    return fail(SANKHYA_GB300_ERROR_ARGUMENT, "null engine or output");
+  }
+  return guarded([&] { engine->engine->time_kernels(reps, ms); });
 }
 
 }  // extern "C"

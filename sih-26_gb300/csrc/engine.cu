@@ -16,6 +16,7 @@
 #include "engine.hpp"
 
 #include "batch.cuh"
+#include "qp.cuh"
 
 #include <algorithm>
 #include <cstdarg>
@@ -101,6 +102,9 @@ template struct DeviceArray<AdjointOutcome>;
 template struct DeviceArray<signed char>;
 template struct DeviceArray<long long>;
 template struct DeviceArray<ChunkSeg>;
+template struct DeviceArray<QpChunk>;
+template struct DeviceArray<QpCtl>;
+template struct DeviceArray<QpHist>;
 
 namespace {
 

@@ -96,6 +96,31 @@ class CBatchItem(ctypes.Structure):
                 ("farkas_value", ctypes.c_double), ("refinements", ctypes.c_int64)]
 
 
+class CQpProblem(ctypes.Structure):
+    _fields_ = [("lp", CLp), ("hessian_starts", _I), ("hessian_index", _I),
+                ("hessian_values", _D)]
+
+
+class CQpParams(ctypes.Structure):
+    _fields_ = [("tolerance", ctypes.c_double), ("iteration_limit", ctypes.c_int64),
+                ("time_limit", ctypes.c_double), ("random_seed", ctypes.c_int64),
+                ("periods_per_poll", ctypes.c_int32), ("column_lanes", ctypes.c_int32),
+                ("row_lanes", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("interrupt", ctypes.POINTER(ctypes.c_int32)), ("log", LOG_FN),
+                ("log_user", ctypes.c_void_p), ("poll", POLL_FN),
+                ("poll_user", ctypes.c_void_p)]
+
+
+class CQpResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("ceiling", ctypes.c_int32),
+                ("iterations", ctypes.c_int64)] + [(k, ctypes.c_double) for k in (
+                    "primal_residual", "dual_residual", "norm_a", "norm_q", "tau", "sigma",
+                    "objective", "setup_seconds", "loop_seconds", "solve_seconds",
+                    "device_seconds")] + [
+                ("kernel_launches", ctypes.c_int64), ("column_lanes", ctypes.c_int32),
+                ("row_lanes", ctypes.c_int32), ("message", ctypes.c_char * 256)]
+
+
 EXPORTS = [
     "sankhya_gb300_last_error", "sankhya_gb300_device_available",
     "sankhya_gb300_device_free_memory", "sankhya_gb300_device_compute_capability",
@@ -107,6 +132,8 @@ EXPORTS = [
     "sankhya_gb300_batch_solution", "sankhya_gb300_batch_adjoint", "sankhya_gb300_batch_polish",
     "sankhya_gb300_batch_schedule", "sankhya_gb300_batch_last_schedule",
     "sankhya_gb300_batch_ray", "sankhya_gb300_batch_set_point",
+    "sankhya_gb300_qp_create", "sankhya_gb300_qp_destroy", "sankhya_gb300_qp_load",
+    "sankhya_gb300_qp_solve", "sankhya_gb300_qp_solution", "sankhya_gb300_qp_time_kernels",
 ]
 
 _lib = None
@@ -168,6 +195,13 @@ def load_library():
         lib.sankhya_gb300_pdhg_spmv_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int32,
                                                         ctypes.c_int32, ctypes.c_void_p,
                                                         ctypes.c_void_p, ctypes.c_void_p]
+        lib.sankhya_gb300_qp_create.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_void_p)]
+        lib.sankhya_gb300_qp_destroy.argtypes = [ctypes.c_void_p]
+        lib.sankhya_gb300_qp_load.argtypes = [ctypes.c_void_p, ctypes.POINTER(CQpProblem)]
+        lib.sankhya_gb300_qp_solve.argtypes = [ctypes.c_void_p, ctypes.POINTER(CQpParams),
+                                               ctypes.POINTER(CQpResult)]
+        lib.sankhya_gb300_qp_solution.argtypes = [ctypes.c_void_p, _D, _D, _D]
+        lib.sankhya_gb300_qp_time_kernels.argtypes = [ctypes.c_void_p, ctypes.c_int32, _D]
         for name in EXPORTS:
             if name not in ("sankhya_gb300_last_error", "sankhya_gb300_estimate_memory"):
                 getattr(lib, name).restype = ctypes.c_int
@@ -324,6 +358,107 @@ class PdhgEngine:
         _check(self._lib.sankhya_gb300_pdhg_spmv_noalloc(
             self._h, op, int(scaled), ctypes.c_void_p(device_in), ctypes.c_void_p(device_out),
             ctypes.c_void_p(stream) if stream else None))
+
+
+@dataclass
+class QpResult:
+    status: int
+    status_name: str
+    ceiling: bool
+    iterations: int
+    primal_residual: float
+    dual_residual: float
+    norm_a: float
+    norm_q: float
+    tau: float
+    sigma: float
+    objective: float
+    setup_seconds: float
+    loop_seconds: float
+    solve_seconds: float
+    device_seconds: float
+    kernel_launches: int
+    column_lanes: int
+    row_lanes: int
+    message: str
+
+
+class QpEngine:
+    """The convex-QP engine (Condat-Vu, src/qp/qp_condat_vu.cpp) on one device: load a QP
+    once, solve it any number of times. The caller owns the convexity decision beyond the
+    engine's diagonal test (the seam runs the reference's check_convexity first)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load_library()
+        h = ctypes.c_void_p()
+        _check(self._lib.sankhya_gb300_qp_create(device, ctypes.byref(h)))
+        self._h = h
+        self._qp = None
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.sankhya_gb300_qp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def load(self, qp):
+        qp = qp.contiguous()
+        lp = qp.lp
+        c = CLp(lp.rows, lp.cols, _ptr(lp.col_starts, ctypes.c_int32),
+                _ptr(lp.row_index, ctypes.c_int32), _ptr(lp.values), _ptr(lp.col_cost),
+                _ptr(lp.col_lower), _ptr(lp.col_upper), _ptr(lp.row_lower), _ptr(lp.row_upper),
+                lp.sense, lp.objective_offset)
+        p = CQpProblem(c, _ptr(qp.hessian_starts, ctypes.c_int32),
+                       _ptr(qp.hessian_index, ctypes.c_int32), _ptr(qp.hessian_values))
+        _check(self._lib.sankhya_gb300_qp_load(self._h, ctypes.byref(p)))
+        self._qp = qp
+
+    def solve(self, tolerance: float = 1e-8, iteration_limit: int = -1,
+              time_limit: Optional[float] = None, random_seed: int = 0,
+              periods_per_poll: int = 0, column_lanes: int = 0, row_lanes: int = 0,
+              interrupt: Optional[np.ndarray] = None, log: Optional[Callable] = None,
+              poll: Optional[Callable] = None) -> QpResult:
+        cb = LOG_FN(lambda user, it, obj, p, d, s: log(it, obj, p, d, s)) if log else LOG_FN()
+        pcb = POLL_FN(lambda user, it, obj: int(bool(poll(it, obj)))) if poll else POLL_FN()
+        intr = (interrupt.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+                if interrupt is not None else ctypes.POINTER(ctypes.c_int32)())
+        params = CQpParams(tolerance, iteration_limit,
+                           1e308 if time_limit is None else float(time_limit), random_seed,
+                           periods_per_poll, column_lanes, row_lanes, 0, intr, cb, None, pcb,
+                           None)
+        r = CQpResult()
+        _check(self._lib.sankhya_gb300_qp_solve(self._h, ctypes.byref(params), ctypes.byref(r)))
+        return QpResult(r.status, STATUS_NAMES.get(r.status, str(r.status)), bool(r.ceiling),
+                        r.iterations, r.primal_residual, r.dual_residual, r.norm_a, r.norm_q,
+                        r.tau, r.sigma, r.objective, r.setup_seconds, r.loop_seconds,
+                        r.solve_seconds, r.device_seconds, r.kernel_launches, r.column_lanes,
+                        r.row_lanes, r.message.decode(errors="replace"))
+
+    def solution(self):
+        """(col_value, col_dual, row_dual) as solve_convex_qp fills Solution."""
+        qp = self._qp
+        x = np.zeros(qp.cols)
+        d = np.zeros(qp.cols)
+        y = np.zeros(qp.rows)
+        _check(self._lib.sankhya_gb300_qp_solution(self._h, _ptr(x), _ptr(d), _ptr(y)))
+        return x, d, y
+
+    def time_kernels(self, reps: int = 20):
+        """Mean device milliseconds of the column and the row pass on the last solve's state."""
+        ms = np.zeros(2)
+        _check(self._lib.sankhya_gb300_qp_time_kernels(self._h, reps, _ptr(ms)))
+        return float(ms[0]), float(ms[1])
 
 
 @dataclass

@@ -235,3 +235,26 @@ def random_qp(seed, rows, cols, per_column=4, hessian_band=2, equality_share=0.3
     lp = LP(m, n, starts, index, values, cost, lower, upper, row_lower, row_upper,
             sense=sense, name=name or f"random_qp_{seed}")
     return QP(lp, hs, hi, hv, lp.name)
+
+
+def banded_hessian(n, band=2, seed=0, scale=0.3):
+    """The stored lower triangle (CSC) of a positive definite banded Q of order n: entries
+    (j + b, j) for b = 1..band drawn from N(0, scale^2), and a diagonal raised above the sum of
+    each row's off-diagonal magnitudes by U(0.2, 2). Vectorised, for the QP workloads."""
+    rng = np.random.default_rng(seed)
+    j = np.arange(n)
+    vals = np.zeros((n, band + 1))
+    rowsum = np.zeros(n)
+    for b in range(1, band + 1):
+        v = scale * rng.normal(size=max(n - b, 0))
+        vals[: n - b, b] = v
+        rowsum[: n - b] += np.abs(v)
+        rowsum[b:] += np.abs(v)
+    vals[:, 0] = rowsum + rng.uniform(0.2, 2.0, size=n)
+    rows = j[:, None] + np.arange(band + 1)[None, :]
+    valid = rows < n
+    counts = valid.sum(axis=1)
+    starts = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(counts, out=starts[1:])
+    return (starts.astype(np.int32), rows[valid].astype(np.int32),
+            vals[valid].astype(np.float64))

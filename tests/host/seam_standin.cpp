@@ -15,6 +15,10 @@
 // tell whether SANKHYA's solve() reached the seam or took its own CPU path. Test
 // infrastructure only; nothing here is part of the engine.
 //
+// The QP calls seam/qp_gpu.cpp makes (qp create, load, solve, solution) hand the QP to the
+// reference's own CPU engine, sankhya::qp::solve_convex_qp, with the options rebuilt from the
+// params struct.
+//
 // The batched calls seam/node_batch.cpp makes (batch create, load, solve, solution, ray) are
 // answered the same way, one reference solve per LP. The reference's PDHG detects no
 // infeasibility, so a test marks an LP infeasible itself, with the direction the stand-in
@@ -33,6 +37,7 @@
 #include "sankhya/model.hpp"
 #include "sankhya/options.hpp"
 #include "sankhya/pdhg.hpp"
+#include "sankhya/qp.hpp"
 #include "sankhya_gb300.h"
 
 struct sankhya_gb300_pdhg {
@@ -44,6 +49,12 @@ struct sankhya_gb300_pdhg {
 struct sankhya_gb300_batch {
   std::vector<sankhya::Model> models;
   std::vector<sankhya::Solution> solutions;
+  bool solved = false;
+};
+
+struct sankhya_gb300_qp {
+  sankhya::Model model;
+  sankhya::Solution solution;
   bool solved = false;
 };
 
@@ -311,6 +322,80 @@ int sankhya_gb300_batch_ray(sankhya_gb300_batch* b, int32_t index, double* ray) 
   const std::size_t m = static_cast<std::size_t>(b->models[static_cast<std::size_t>(index)].num_rows());
   const auto found = g_infeasible.find(index);
   for (std::size_t i = 0; i < m; ++i) ray[i] = found != g_infeasible.end() ? found->second[i] : 0.0;
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_qp_create(int32_t device, sankhya_gb300_qp** out) {
+  (void)device;
+  if (g_fail_create) {
+    g_error = "no usable CUDA device (stand-in)";
+    return SANKHYA_GB300_ERROR_DEVICE;
+  }
+  *out = new sankhya_gb300_qp();
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_qp_destroy(sankhya_gb300_qp* e) {
+  delete e;
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_qp_load(sankhya_gb300_qp* e, const sankhya_gb300_qp_problem* p) {
+  to_model(&p->lp, e->model);
+  e->model.hessian.reset(p->lp.cols, p->lp.cols);
+  if (p->hessian_starts != nullptr) {
+    for (int32_t j = 0; j < p->lp.cols; ++j) {
+      for (int32_t k = p->hessian_starts[j]; k < p->hessian_starts[j + 1]; ++k) {
+        e->model.hessian.add_entry(p->hessian_index[k], j, p->hessian_values[k]);
+      }
+    }
+  }
+  e->model.hessian.finalize(0.0);
+  e->solved = false;
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_qp_solve(sankhya_gb300_qp* e, const sankhya_gb300_qp_params* p,
+                           sankhya_gb300_qp_result* r) {
+  std::memset(r, 0, sizeof(*r));
+  e->solution = sankhya::Solution();
+  e->solution.allocate_for(e->model);
+  e->solved = true;
+  if (p->poll != nullptr && p->poll(p->poll_user, 0, 0.0) != 0) {
+    r->status = SANKHYA_GB300_INTERRUPTED;
+    return SANKHYA_GB300_OK;
+  }
+  sankhya::Options o;
+  o.set_double("qp_tolerance", p->tolerance);
+  o.set_int("iteration_limit", p->iteration_limit);
+  o.set_double("time_limit", p->time_limit);
+  o.set_int("random_seed", p->random_seed);
+  sankhya::Logger quiet(nullptr);
+  e->solution = sankhya::qp::solve_convex_qp(e->model, o, quiet, nullptr);
+  ++g_solves;
+  if (p->log != nullptr) p->log(p->log_user, 5000, e->solution.objective, 1e-3, 2e-3, 0.25);
+  r->status = to_code(e->solution.status);
+  r->iterations = e->solution.iterations;
+  r->objective = e->solution.objective;
+  r->solve_seconds = e->solution.solve_seconds;
+  std::strncpy(r->message, e->solution.message.c_str(), sizeof(r->message) - 1);
+  return SANKHYA_GB300_OK;
+}
+
+int sankhya_gb300_qp_solution(sankhya_gb300_qp* e, double* col_value, double* col_dual,
+                              double* row_dual) {
+  if (!e->solved) {
+    g_error = "no solve has run";
+    return SANKHYA_GB300_ERROR_ARGUMENT;
+  }
+  const auto& s = e->solution;
+  for (std::size_t j = 0; j < s.col_value.size(); ++j) {
+    if (col_value) col_value[j] = s.col_value[j];
+    if (col_dual) col_dual[j] = s.col_dual[j];
+  }
+  for (std::size_t i = 0; i < s.row_dual.size(); ++i) {
+    if (row_dual) row_dual[i] = s.row_dual[i];
+  }
   return SANKHYA_GB300_OK;
 }
 

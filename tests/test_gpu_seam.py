@@ -120,3 +120,31 @@ def test_gradients_through_the_seam(tmp_path, built):
     print(run.stdout[-3000:])
     assert run.returncode == 0, run.stdout[-3000:] + run.stderr[-2000:]
     assert run.stdout.strip().endswith("OK"), run.stdout
+
+
+def test_convex_qp_on_the_gpu(tmp_path, built):
+    """`seam/qp_gpu.cpp` with the engine's real library (`tests/host/qp_seam_check.cpp`, gpu
+    mode): test_qp.cpp's convex QPs, seeded random QPs and the reference's two demo QPs give
+    the reference's status and iteration count with the point and duals within 1e-8; the
+    non-convex ones are refused with its message; the limits and the interrupt stop with its
+    messages."""
+    import pyoracle
+
+    flags, sources, core = core_link_args()
+    sources = [s for s in sources if not s.endswith("seam_standin.cpp")]
+    tree = pyoracle.reference_tree()
+    lib_dir = os.path.join(ROOT, "sih-26_gb300", "lib")
+    exe = str(tmp_path / "qp_seam_check")
+    cmd = (["g++"] + flags + sources +
+           [os.path.join(ROOT, "sih-26_gb300", "seam", "qp_gpu.cpp"),
+            os.path.join(ROOT, "tests", "host", "qp_seam_check.cpp"), core,
+            f"-L{lib_dir}", "-lsankhya_gb300", f"-Wl,-rpath,{lib_dir}", "-fopenmp", "-lz",
+            "-o", exe])
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr[-3000:]
+    demos = [os.path.join(tree, "demo", f) for f in ("qp_blend.mps", "crude_blend_qp.mps")]
+    run = subprocess.run([exe, "gpu"] + [d for d in demos if os.path.exists(d)],
+                         capture_output=True, text=True, timeout=900)
+    print(run.stdout[-3000:])
+    assert run.returncode == 0, run.stdout[-3000:] + run.stderr[-2000:]
+    assert run.stdout.strip().endswith("OK"), run.stdout

@@ -196,3 +196,24 @@ def test_node_relaxations_through_the_seam(tmp_path):
     run = subprocess.run([exe, model, "standin"], capture_output=True, text=True, timeout=600)
     assert run.returncode == 0, run.stdout[-2000:] + run.stderr[-2000:]
     assert run.stdout.strip().endswith("OK"), run.stdout
+
+
+def test_convex_qp_through_the_seam(tmp_path):
+    """`tests/host/qp_seam_check.cpp` through `seam/qp_gpu.cpp` and the C-ABI stand-in (the
+    reference's solve_convex_qp behind the engine's calls): test_qp.cpp's convex QPs, seeded
+    random QPs and the two demo QPs come back as the reference's Solution bit for bit; the
+    non-convex ones are refused with the reference's message word for word; the iteration and
+    time limits and the interrupt stop with its messages; no engine is a numerical error."""
+    flags, sources, core = core_link_args()
+    exe = str(tmp_path / "qp_seam_check")
+    cmd = (["g++"] + flags + sources +
+           [os.path.join(SEAM, "qp_gpu.cpp"),
+            os.path.join(ROOT, "tests", "host", "qp_seam_check.cpp"), core, "-fopenmp",
+            "-lz", "-o", exe])
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr[-2000:]
+    demos = [os.path.join(REF, "demo", f) for f in ("qp_blend.mps", "crude_blend_qp.mps")]
+    run = subprocess.run([exe, "standin"] + [d for d in demos if os.path.exists(d)],
+                         capture_output=True, text=True, timeout=600)
+    assert run.returncode == 0, run.stdout[-2000:] + run.stderr[-2000:]
+    assert run.stdout.strip().endswith("OK"), run.stdout
