@@ -219,6 +219,27 @@ def make_workload(blocks=None):
                                 WORKLOAD["cols_per_block"], WORKLOAD["k"], WORKLOAD["seed"])
 
 
+def profile_qp(blocks):
+    """The QP's small case for kernel captures: the same Hessian on a slice of `blocks`
+    periods (32 periods: 500,000 x 1,000,000, about 1e7 nonzeros of A and 5e6 of Q: matrix
+    copies of 120-180 MB), 200 iterations. Prints one line with the passes' CUDA-event times."""
+    from sankhya_gb300 import build, capi
+
+    build.build_lpgen()
+    build.build_engine()
+    qp = qp_workload(make_workload(blocks))
+    col_bytes, row_bytes = qp_bytes(qp)
+    with capi.QpEngine(0) as eng:
+        eng.load(qp)
+        r = eng.solve(tolerance=1e-30, iteration_limit=200)
+        col_ms, row_ms = eng.time_kernels(20)
+    print(json.dumps({"profile_qp": blocks, "status": r.status_name, "iterations": r.iterations,
+                      "lanes": [r.column_lanes, r.row_lanes],
+                      "column_pass_ms": col_ms, "row_pass_ms": row_ms,
+                      "column_pass_gbs": col_bytes / col_ms / 1e6,
+                      "row_pass_gbs": row_bytes / row_ms / 1e6}))
+
+
 def profile_case(blocks, precision, iterations, zipf=False):
     """The small case the kernel captures run on: the same generator with fewer periods
     (16 periods: 250,000 x 500,000, about 5M nonzeros, matrix copies of 40-120 MB), solved for
@@ -565,6 +586,99 @@ def zipf_section(device, peak):
     return out
 
 
+# The convex QP on the same kernels' terms (src/qp/qp_condat_vu.cpp): the 1M x 2M LP's rows,
+# columns and cost with a banded positive definite Hessian (two sub-diagonals, a dominant
+# diagonal; 6M stored entries, 10M in the full symmetric Q). Condat-Vu has a fixed step and
+# no restarts, so the GPU leg is a fixed QP_ITERATIONS at a tolerance no run meets, and the
+# reference's CPU engine is timed on QP_CPU_SAMPLE iterations of the same QP.
+QP_HESSIAN = dict(band=2, seed=7)
+QP_ITERATIONS = 2000
+QP_CPU_SAMPLE = 20
+
+
+def qp_workload(lp):
+    from sankhya_gb300.model import QP, banded_hessian
+
+    hs, hi, hv = banded_hessian(lp.cols, QP_HESSIAN["band"], seed=QP_HESSIAN["seed"])
+    return QP(lp, hs, hi, hv, "qp_" + lp.name)
+
+
+def qp_bytes(qp):
+    """Algorithmic bytes of one column and one row pass: matrix values and indices (A's
+    column and Q's full rows; A's rows), both passes' pointer arrays, each gathered vector
+    once, each streamed vector once (column pass: c, l, u, x read, x' and xbar written; row
+    pass: rl, ru, y read, y written)."""
+    m, n = qp.rows, qp.cols
+    za = qp.lp.nnz
+    zq = 2 * qp.hessian_nnz - n
+    col = 12 * (za + zq) + 8 * (n + 1) + 8 * n + 8 * m + 32 * n + 16 * n
+    row = 12 * za + 4 * (m + 1) + 8 * n + 24 * m + 8 * m
+    return col, row
+
+
+def qp_section(device, peak, lp, cpu=True):
+    """The convex QP: GPU iterations per second over QP_ITERATIONS, its column and row
+    passes' achieved bandwidth (CUDA events, 20 iterations), the reference's CPU engine per
+    iteration on QP_CPU_SAMPLE iterations, and the same-answer check at that count."""
+    import numpy as np
+    from sankhya_gb300 import capi
+
+    qp = qp_workload(lp)
+    col_bytes, row_bytes = qp_bytes(qp)
+    out = {"workload": f"QP {qp.rows:,} x {qp.cols:,}: the LP's rows and bounds, {lp.nnz:,} "
+                       f"nonzeros of A, a banded Hessian of {qp.hessian_nnz:,} stored "
+                       f"({2 * qp.hessian_nnz - qp.cols:,} full) entries",
+           "iterations": QP_ITERATIONS}
+    with capi.QpEngine(device) as eng:
+        t0 = time.perf_counter()
+        eng.load(qp)
+        out["load_s"] = time.perf_counter() - t0
+        eng.solve(tolerance=1e-30, iteration_limit=100)  # warm-up (graph capture)
+        r = eng.solve(tolerance=1e-30, iteration_limit=QP_ITERATIONS)
+        col_ms, row_ms = eng.time_kernels(20)
+        out.update({"status": r.status_name, "device_s": r.device_seconds,
+                    "setup_s": r.setup_seconds, "loop_s": r.loop_seconds,
+                    "us_per_iteration": 1e6 * r.loop_seconds / max(1, r.iterations),
+                    "iterations_per_s": r.iterations / r.loop_seconds if r.loop_seconds else None,
+                    "lanes": [r.column_lanes, r.row_lanes], "kernel_launches": r.kernel_launches,
+                    "primal_residual": r.primal_residual, "dual_residual": r.dual_residual,
+                    "column_pass_ms": col_ms, "row_pass_ms": row_ms,
+                    "column_pass_bytes": col_bytes, "row_pass_bytes": row_bytes,
+                    "column_pass_gbs": col_bytes / col_ms / 1e6,
+                    "row_pass_gbs": row_bytes / row_ms / 1e6,
+                    "column_pass_frac": col_bytes / col_ms / 1e6 / peak,
+                    "row_pass_frac": row_bytes / row_ms / 1e6 / peak})
+        if cpu:
+            threads = os.cpu_count() or 1
+            o = _oracle(threads)
+            t0 = time.perf_counter()
+            o.solve_qp(qp, tolerance=1e-30, iteration_limit=0)
+            setup = time.perf_counter() - t0
+            t0 = time.perf_counter()
+            c = o.solve_qp(qp, tolerance=1e-30, iteration_limit=QP_CPU_SAMPLE)
+            per_it = max(time.perf_counter() - t0 - setup, 0.0) / QP_CPU_SAMPLE
+            g = eng.solve(tolerance=1e-30, iteration_limit=QP_CPU_SAMPLE)
+            x, d, y = eng.solution()
+
+            def rel(a, b):
+                return float(np.max(np.abs(a - b))) / max(1.0, float(np.max(np.abs(b))))
+
+            out["cpu"] = {"kind": cpu_kind()[0],
+                          "engine": "sankhya::qp::solve_convex_qp (src/qp/qp_condat_vu.cpp)"
+                                    + (", the reference's own build" if cpu_kind()[0] ==
+                                       "reference" else ", the oracle's C restatement"),
+                          "cores": threads, "setup_s": setup, "s_per_iteration": per_it,
+                          "sample_iterations": QP_CPU_SAMPLE,
+                          "speedup_per_iteration": per_it / (1e-6 * out["us_per_iteration"])}
+            out["same_answer_at_sample"] = {
+                "iterations": [g.iterations, c.iterations],
+                "x_rel_diff": rel(x, c.col_value), "col_dual_rel_diff": rel(d, c.col_dual),
+                "row_dual_rel_diff": rel(y, c.row_dual),
+                "ok": bool(g.iterations == c.iterations and rel(x, c.col_value) <= 1e-9
+                           and rel(d, c.col_dual) <= 1e-9 and rel(y, c.row_dual) <= 1e-9)}
+    return out
+
+
 # The north star's "same answer": both methods' objectives within 1e-6 relative of each
 # other and of the planted optimum, and each at relative KKT <= 1e-8 by the exact FP64
 # evaluation of the reference's residuals (src/pdhg/pdhg_evaluate.hpp:48).
@@ -753,6 +867,9 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint section")
     ap.add_argument("--no-reference-gpu", action="store_true",
                     help="skip timing the reference's own CUDA PDHG")
+    ap.add_argument("--no-qp", action="store_true", help="skip the convex-QP section")
+    ap.add_argument("--profile-qp", type=int, metavar="PERIODS", default=0,
+                    help="profile case: the QP on a slice of this many periods, 200 iterations")
     ap.add_argument("--no-zipf", action="store_true",
                     help="skip the load-balance stress LP (Zipf row lengths)")
     ap.add_argument("--profile-case", type=int, metavar="PERIODS", default=0,
@@ -761,6 +878,9 @@ def main():
     ap.add_argument("--profile-zipf", action="store_true",
                     help="profile case on the 500,000 x 1,000,000 Zipf-row LP")
     args = ap.parse_args()
+    if args.profile_qp:
+        profile_qp(args.profile_qp)
+        return
     if args.profile_case or args.profile_zipf:
         profile_case(args.profile_case, args.precision, args.profile_iterations,
                      zipf=args.profile_zipf)
@@ -887,6 +1007,12 @@ def main():
             zipf = zipf_section(local, peak)
         except Exception as exc:  # noqa: BLE001
             zipf = {"error": f"{type(exc).__name__}: {exc}"}
+    qp = None
+    if not args.no_qp:
+        try:
+            qp = qp_section(local, peak, lp, cpu=not args.no_cpu_baseline)
+        except Exception as exc:  # noqa: BLE001
+            qp = {"error": f"{type(exc).__name__}: {exc}"}
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -930,7 +1056,7 @@ def main():
     # a reader that keeps only the end of the line still has the parity verdict.
     line = {
         "spmv_gbs": roof, "fp64_kernels": froof, "batched": batched, "adjoint": adjoint,
-        "zipf": zipf, "reference_gpu": reference_gpu,
+        "zipf": zipf, "qp": qp, "reference_gpu": reference_gpu,
         "metric": METRIC, "value": step_s, "unit": "s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None,

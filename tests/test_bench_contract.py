@@ -65,6 +65,46 @@ class StandInPdhgEngine:
         pass
 
 
+class StandInQpEngine:
+    """The QP engine's calls answered by the oracle's restatement (the answers the bench's
+    same-answer check compares are then the oracle's own, so the check must pass)."""
+
+    def __init__(self, device=0):
+        import pyoracle
+
+        self.oracle = pyoracle.Oracle()
+        self.last = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        return False
+
+    def load(self, qp):
+        self.qp = qp
+
+    def solve(self, tolerance=1e-8, iteration_limit=-1, **kw):
+        from types import SimpleNamespace
+
+        self.last = self.oracle.solve_qp(self.qp, tolerance=tolerance,
+                                         iteration_limit=iteration_limit)
+        return SimpleNamespace(status_name=self.last.status_name,
+                               iterations=self.last.iterations, device_seconds=0.2,
+                               setup_seconds=0.01, loop_seconds=0.19, column_lanes=1,
+                               row_lanes=2, kernel_launches=10, primal_residual=1e-3,
+                               dual_residual=1e-4)
+
+    def time_kernels(self, reps):
+        return 0.05, 0.04
+
+    def solution(self):
+        return self.last.col_value, self.last.col_dual, self.last.row_dual
+
+    def close(self):
+        pass
+
+
 def _batch_engine():
     from test_bench_adjoint_check import ExactBatchEngine, _Item
 
@@ -99,6 +139,9 @@ def _run(monkeypatch, argv):
     from sankhya_gb300 import capi
 
     monkeypatch.setattr(capi, "PdhgEngine", StandInPdhgEngine)
+    monkeypatch.setattr(capi, "QpEngine", StandInQpEngine)
+    monkeypatch.setattr(bench, "QP_ITERATIONS", 300)
+    monkeypatch.setattr(bench, "QP_CPU_SAMPLE", 7)
     monkeypatch.setattr(capi, "BatchEngine", _batch_engine())
     monkeypatch.setattr(bench, "WORKLOAD", dict(blocks=2, rows_per_block=300,
                                                 cols_per_block=600, k=9, seed=2026))
@@ -128,8 +171,13 @@ def test_default_line(monkeypatch):
     for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step",
                 "higher_is_better", "scaling", "vs_baseline", "dtype", "data", "config",
                 "roofline", "cpu_baseline", "e2e", "gpu_launches", "clocks", "fp64",
-                "batched", "adjoint", "reference_gpu"):
+                "batched", "adjoint", "reference_gpu", "qp"):
         assert key in line, key
+    qp = line["qp"]
+    assert "error" not in qp, qp
+    assert qp["iterations"] == 300 and qp["cpu"]["sample_iterations"] == 7
+    assert qp["same_answer_at_sample"]["ok"] is True
+    assert qp["column_pass_gbs"] == pytest.approx(qp["column_pass_bytes"] / 0.05 / 1e6)
     assert line["n_gpus"] == 1 and line["steps"] == 1 and line["warmup"] == 3
     assert line["higher_is_better"] is False and line["unit"] == "s"
     assert "workload" in line["config"]

@@ -43,7 +43,7 @@ def _rank_main(rank, world, port, out_path):
     capi.PdhgEngine = RankEngine
     bench.WORKLOAD = dict(blocks=2, rows_per_block=300, cols_per_block=600, k=9, seed=2026)
     sys.argv = ["bench.py", "--gpus", str(world), "--steps", "1", "--warmup", "3",
-                "--no-batch", "--no-adjoint", "--no-cpu-baseline", "--no-zipf",
+                "--no-batch", "--no-adjoint", "--no-cpu-baseline", "--no-zipf", "--no-qp",
                 "--no-reference-gpu"]
     with open(out_path, "w") as f:
         sys.stdout = f
