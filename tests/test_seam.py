@@ -21,7 +21,7 @@ REF = pyoracle.REFERENCE_TREE
 
 
 @pytest.mark.parametrize("name", ["pdhg_gpu", "pdhg_multi_gpu", "gpu_memory", "device",
-                                  "node_batch", "lp_gradients"])
+                                  "node_batch", "lp_gradients", "qp_gpu"])
 def test_seam_compiles_against_reference_headers(name):
     if not os.path.isdir(os.path.join(REF, "src", "gpu")) or shutil.which("g++") is None:
         pytest.skip("the reference tree (or g++) is not present here")
