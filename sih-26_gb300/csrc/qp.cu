@@ -40,13 +40,14 @@ std::string qp_format(const char* fmt, ...) {
 }
 
 // Lanes per item from the mean entries per item: the smallest power of two that leaves each
-// lane at most 16 entries of a typical item. The FP64 passes run fastest with few lanes (on the
-// 1M x 2M QP, 15 entries per column and 20 per row, one lane per column and two per row run
-// the passes 2.4 and 2.4 times faster than four and eight); items longer than 64 lanes' worth
-// go to the chunked path whatever the lanes.
+// lane at most 32 entries of a typical item. The passes are bound by the FP64 pipe, where a
+// lane that sits out the epilogue costs as much as a working one, so few lanes win: on the
+// 1M x 2M QP (15 entries per column, 20 per row) one lane per column and per row runs
+// 2.4 and 2.6 times faster than four and eight. Items longer than 64 lanes' worth go to the
+// chunked path whatever the lanes.
 int auto_lanes(double mean) {
   int g = 1;
-  while (g < 32 && 16.0 * g < mean) g *= 2;
+  while (g < 32 && 32.0 * g < mean) g *= 2;
   return g;
 }
 
@@ -208,11 +209,11 @@ void QpEngine::load(const sankhya_gb300_qp_problem& p) {
       const double v = p.hessian_values[k];
       int slot = qnext[i]++;
       qidx[slot] = j;
-      qval[slot] = v;
+      qval[slot] = sense * v;
       if (i != j) {
         slot = qnext[j]++;
         qidx[slot] = i;
-        qval[slot] = v;
+        qval[slot] = sense * v;
       }
     }
   }
@@ -249,11 +250,26 @@ void QpEngine::load(const sankhya_gb300_qp_problem& p) {
   q_rs_.upload(qptr.data(), qptr.size(), s);
   q_ci_.upload(qidx.data(), static_cast<size_t>(qz), s);
   q_v_.upload(qval.data(), static_cast<size_t>(qz), s);
-  cost_.upload(lp.col_cost, static_cast<size_t>(n), s);
-  col_lower_.upload(lp.col_lower, static_cast<size_t>(n), s);
-  col_upper_.upload(lp.col_upper, static_cast<size_t>(n), s);
-  row_lower_.upload(lp.row_lower, static_cast<size_t>(m), s);
-  row_upper_.upload(lp.row_upper, static_cast<size_t>(m), s);
+  // The kernels' forms (qp_kernels.cu): the cost times the sense (Q was stored so above), and
+  // every absent bound as an infinity on its side.
+  constexpr double kInf = std::numeric_limits<double>::infinity();
+  const auto finite = [](double v) { return !(std::isinf(v) || std::fabs(v) >= 1e30); };
+  std::vector<double> cmin(static_cast<size_t>(n)), lo(static_cast<size_t>(n)),
+      hi(static_cast<size_t>(n)), rlo(static_cast<size_t>(m)), rhi(static_cast<size_t>(m));
+  for (int j = 0; j < n; ++j) {
+    cmin[j] = sense * lp.col_cost[j];
+    lo[j] = finite(lp.col_lower[j]) ? lp.col_lower[j] : -kInf;
+    hi[j] = finite(lp.col_upper[j]) ? lp.col_upper[j] : kInf;
+  }
+  for (int i = 0; i < m; ++i) {
+    rlo[i] = finite(lp.row_lower[i]) ? lp.row_lower[i] : -kInf;
+    rhi[i] = finite(lp.row_upper[i]) ? lp.row_upper[i] : kInf;
+  }
+  cost_.upload(cmin.data(), cmin.size(), s);
+  col_lower_.upload(lo.data(), lo.size(), s);
+  col_upper_.upload(hi.data(), hi.size(), s);
+  row_lower_.upload(rlo.data(), rlo.size(), s);
+  row_upper_.upload(rhi.data(), rhi.size(), s);
   for (auto* a : {&x0_, &x1_, &xbar_, &col_dual_, &vec_n_}) a->allocate(static_cast<size_t>(n));
   for (auto* a : {&y_, &row_dual_, &vec_m_}) a->allocate(static_cast<size_t>(m));
   SGB_CUDA(cudaStreamSynchronize(s));
@@ -353,8 +369,10 @@ double QpEngine::spectral_norm(unsigned seed) {
     const double norm2 = dot(vec_n_.ptr, vec_n_.ptr, n_);
     if (std::sqrt(norm2) <= 0.0) return 0.0;
     qp_launch_scale(vec_n_.ptr, n_, dot_out_.ptr, stream_);
-    qp_launch_spmv(m_, a_rs_.ptr, a_ci_.ptr, a_rv_.ptr, vec_n_.ptr, vec_m_.ptr, stream_);
-    qp_launch_spmv(n_, a_cs_.ptr, a_ri_.ptr, a_cv_.ptr, vec_m_.ptr, vec_n_.ptr, stream_);
+    qp_launch_spmv(m_, a_rs_.ptr, a_ci_.ptr, a_rv_.ptr, vec_n_.ptr, vec_m_.ptr,
+                   auto_lanes(double(nnz_a_) / m_), stream_);
+    qp_launch_spmv(n_, a_cs_.ptr, a_ri_.ptr, a_cv_.ptr, vec_m_.ptr, vec_n_.ptr,
+                   auto_lanes(double(nnz_a_) / n_), stream_);
     estimate = std::sqrt(std::sqrt(dot(vec_n_.ptr, vec_n_.ptr, n_)));
   }
   return estimate;
@@ -377,7 +395,8 @@ double QpEngine::hessian_norm(unsigned seed) {
     const double norm2 = dot(a, a, n_);
     if (std::sqrt(norm2) <= 0.0) return 0.0;
     qp_launch_scale(a, n_, dot_out_.ptr, stream_);
-    qp_launch_spmv(n_, q_rs_.ptr, q_ci_.ptr, q_v_.ptr, a, b, stream_);
+    qp_launch_spmv(n_, q_rs_.ptr, q_ci_.ptr, q_v_.ptr, a, b, auto_lanes(double(nnz_q_) / n_),
+                   stream_);
     estimate = std::fabs(dot(b, a, n_));
     std::swap(a, b);
   }
@@ -481,6 +500,7 @@ void QpEngine::solve(const sankhya_gb300_qp_params& p, sankhya_gb300_qp_result* 
   QpCtl c{};
   c.tau = tau;
   c.sigma = sigma;
+  c.inv_sigma = sigma > 0.0 ? 1.0 / sigma : 0.0;
   c.tolerance = p.tolerance;
   c.limit = ceiling ? 1000000 : p.iteration_limit;
   SGB_CUDA(cudaMemcpyAsync(ctl_.ptr, &c, sizeof(QpCtl), cudaMemcpyHostToDevice, stream_));

@@ -50,6 +50,7 @@ struct QpCtl {
   int done;   // the stopping test held
   int error;  // unused by the kernels, cleared at load
   double tau, sigma, tolerance;  // the solve's step sizes and stopping tolerance
+  double inv_sigma;              // RN(1 / sigma), for the row pass's division
   long long base;        // iterations completed before the running graph
   long long limit;       // iteration limit in force (the ceiling when none was set)
   long long iterations;  // iteration at which the test held
@@ -77,9 +78,9 @@ struct QpDev {
   const double* a_rv;
   const int* q_rs;
   const int* q_ci;
-  const double* q_v;
-  const double* cost;
-  const double* col_lower;
+  const double* q_v;  // sense Q
+  const double* cost;       // sense c
+  const double* col_lower;  // bounds with absent sides as -inf / +inf
   const double* col_upper;
   const double* row_lower;
   const double* row_upper;
@@ -116,11 +117,12 @@ void qp_launch_decide(const QpDev& d, QpCtl* ctl, int k, int p, cudaStream_t s);
 // base += iterations of the graph (capped at the limit) unless done.
 void qp_launch_advance(QpCtl* ctl, int graph_iterations, cudaStream_t s);
 
-// Setup: out = M v over the rows of a CSR (one warp per row); sum of a[i] * b[i] into *out in
-// a fixed order (partials of kQpDotBlocks blocks, then one block); v /= sqrt(*norm2).
+// Setup: out = M v over the rows of a CSR (`lanes` threads per row, 1..32); sum of a[i] * b[i]
+// into *out in a fixed order (partials of kQpDotBlocks blocks, then one block);
+// v /= sqrt(*norm2).
 constexpr int kQpDotBlocks = 304;
 void qp_launch_spmv(int rows, const int* starts, const int* index, const double* values,
-                    const double* v, double* out, cudaStream_t s);
+                    const double* v, double* out, int lanes, cudaStream_t s);
 void qp_launch_dot(const double* a, const double* b, int n, double* partials, double* out,
                    cudaStream_t s);
 void qp_launch_scale(double* v, int n, const double* norm2, cudaStream_t s);

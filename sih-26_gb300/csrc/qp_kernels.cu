@@ -1,10 +1,25 @@
 // qp_kernels.cu -- kernels of the convex-QP engine (layout and schedule in qp.cuh).
 //
 // Arithmetic follows src/qp/qp_condat_vu.cpp:257-326 term by term. The element-wise steps
-// use explicitly rounded operations (no fused multiply-add), so they round as the
-// reference's do; the sums over a row or column accumulate with FMA in a fixed order (the
-// entries' order for one lane, then a fixed tree over the lanes and over the chunks of a long
-// item), which differs from the reference's sequential sums by a few ulps.
+// round as the reference's do; the sums over a row or column accumulate with FMA in a fixed
+// order (the entries' order for one lane, then a fixed tree over the lanes and over the chunks
+// of a long item), which differs from the reference's sequential sums by a few ulps.
+//
+// GB300 retires about two FP64 lane operations per clock per SM, and these passes are bound
+// by that pipe rather than by HBM: the per-item epilogue costs as much as a dozen entries of
+// the sums. So the epilogues are written for few FP64 instructions, each with the reference's
+// rounding:
+//   - absent bounds are stored as -inf / +inf (the load maps every bound that
+//     is_finite_bound calls absent), so the projection is two compares;
+//   - the cost and Q are stored times the sense (exact), so the gradient
+//     (sense c + sense Qx) + A'y is two additions with the same bits;
+//   - 2 x' - x is one FMA (2 x' is exact);
+//   - v / sigma is Markstein's correction of the product with the correctly rounded
+//     reciprocal (P. Markstein, "Computation of elementary functions on the IBM RISC
+//     System/6000 processor", IBM J. Res. Dev. 34(1), 1990): q = v (1/sigma), r = v - sigma q
+//     exactly by FMA, q + r (1/sigma) rounded once, which is the correctly rounded quotient
+//     for operands and results in the normal range (tests/host/qp_division_check.c holds it to
+//     IEEE division).
 #include "qp.cuh"
 
 #include <algorithm>
@@ -14,9 +29,24 @@ namespace {
 
 long long g_qp_launches = 0;
 
-// The gradient of the minimisation-space objective, (sense c + sense (Qx)_j) + (A'y)_j.
-__device__ __forceinline__ double qp_gradient(double sense, double c, double qx, double aty) {
-  return __dadd_rn(__dadd_rn(__dmul_rn(sense, c), __dmul_rn(sense, qx)), aty);
+// The gradient of the minimisation-space objective, (sense c + sense (Qx)_j) + (A'y)_j, from
+// the stored sense c and the sum over sense Q.
+__device__ __forceinline__ double qp_gradient(double cmin, double qxmin, double aty) {
+  return __dadd_rn(__dadd_rn(cmin, qxmin), aty);
+}
+
+// proj_[lo, hi](v) for bounds stored with absent sides as infinities: the reference's project
+// (src/qp/qp_condat_vu.cpp:60-64), a NaN left as it is.
+__device__ __forceinline__ double box(double v, double lo, double hi) {
+  return v < lo ? lo : (v > hi ? hi : v);
+}
+
+// v / sigma from inv = RN(1 / sigma) (Markstein's correction, see the file header); an exact
+// first product or a non-finite residual keeps the product.
+__device__ __forceinline__ double divide(double v, double sigma, double inv) {
+  const double q = __dmul_rn(v, inv);
+  const double r = fma(-q, sigma, v);
+  return (r == 0.0 || r != r) ? q : fma(r, inv, q);
 }
 
 // A residual into a running maximum held as the bit pattern of a non-negative double (the
@@ -42,22 +72,24 @@ __device__ __forceinline__ void column_epilogue(const QpDev& d, double tau, int 
                                                 const double* x, double* xn, double qx,
                                                 double aty, double* residual, double* obj) {
   const double xj = x[j];
-  const double c = d.cost[j];
+  const double c = d.cost[j];  // sense c; qx is (sense Q x)_j
   if (MODE == kQpStep) {
-    const double g = qp_gradient(d.sense, c, qx, aty);
+    const double g = qp_gradient(c, qx, aty);
     const double t = __dsub_rn(xj, __dmul_rn(tau, g));
-    const double xnj = project(t, d.col_lower[j], d.col_upper[j]);
+    const double xnj = box(t, d.col_lower[j], d.col_upper[j]);
     xn[j] = xnj;
-    d.xbar[j] = __dsub_rn(__dmul_rn(2.0, xnj), xj);
+    d.xbar[j] = fma(2.0, xnj, -xj);
   } else {
     if (MODE == kQpCheck) {
-      const double g = qp_gradient(d.sense, c, qx, aty);
-      const double stepped = project(__dsub_rn(xj, g), d.col_lower[j], d.col_upper[j]);
+      const double g = qp_gradient(c, qx, aty);
+      const double stepped = box(__dsub_rn(xj, g), d.col_lower[j], d.col_upper[j]);
       *residual = fabs(__dsub_rn(xj, stepped));
     } else {
-      d.col_dual[j] = __dadd_rn(__dadd_rn(c, qx), __dmul_rn(d.sense, aty));
+      // c + Qx = sense (sense c + sense Qx), exactly.
+      d.col_dual[j] =
+          __dadd_rn(__dmul_rn(d.sense, __dadd_rn(c, qx)), __dmul_rn(d.sense, aty));
     }
-    *obj = c * xj + 0.5 * xj * qx;
+    *obj = d.sense * (c * xj + 0.5 * xj * qx);
   }
 }
 
@@ -155,15 +187,16 @@ __global__ void __launch_bounds__(kQpThreads) k_qp_column(QpDev d, QpCtl* ctl, i
 // ---- Row pass ---------------------------------------------------------------------------
 
 template <int MODE>
-__device__ __forceinline__ double row_epilogue(const QpDev& d, double sigma, int i, double ax) {
+__device__ __forceinline__ double row_epilogue(const QpDev& d, double sigma, double inv_sigma,
+                                               int i, double ax) {
   if (MODE == kQpStep) {
     // y' = v - sigma proj(v / sigma), v = y + sigma (A xbar)_i (src/qp/qp_condat_vu.cpp:270-276).
     const double v = __dadd_rn(d.y[i], __dmul_rn(sigma, ax));
-    const double p = project(__ddiv_rn(v, sigma), d.row_lower[i], d.row_upper[i]);
+    const double p = box(divide(v, sigma, inv_sigma), d.row_lower[i], d.row_upper[i]);
     d.y[i] = __dsub_rn(v, __dmul_rn(sigma, p));
     return 0.0;
   }
-  const double projected = project(ax, d.row_lower[i], d.row_upper[i]);
+  const double projected = box(ax, d.row_lower[i], d.row_upper[i]);
   return fabs(__dsub_rn(ax, projected));
 }
 
@@ -171,7 +204,7 @@ template <int G, int MODE>
 __global__ void __launch_bounds__(kQpThreads) k_qp_row(QpDev d, QpCtl* ctl, int k, int src) {
   grid_dependency_wait();
   if (qp_skip(ctl, k)) return;
-  const double sigma = ctl->sigma;
+  const double sigma = ctl->sigma, inv_sigma = ctl->inv_sigma;
   const double* v = MODE == kQpStep ? d.xbar : (src ? d.x1 : d.x0);
   const int lane32 = threadIdx.x & 31;
   if (static_cast<int>(blockIdx.x) < d.row_short_blocks) {
@@ -191,7 +224,7 @@ __global__ void __launch_bounds__(kQpThreads) k_qp_row(QpDev d, QpCtl* ctl, int 
     for (int q = b + lane; q < e; q += G) ax = fma(d.a_rv[q], v[d.a_ci[q]], ax);
     ax = group_sum<G>(ax);
     double residual = 0.0;
-    if (active && lane == 0) residual = row_epilogue<MODE>(d, sigma, i, ax);
+    if (active && lane == 0) residual = row_epilogue<MODE>(d, sigma, inv_sigma, i, ax);
     if (MODE == kQpCheck) {
       const double w = warp_max(residual);
       if (lane32 == 0) max_bits(&ctl->primal_bits, w);
@@ -223,7 +256,7 @@ __global__ void __launch_bounds__(kQpThreads) k_qp_row(QpDev d, QpCtl* ctl, int 
     }
   }
   if (lane32 == 0) {
-    const double residual = row_epilogue<MODE>(d, sigma, i, ax);
+    const double residual = row_epilogue<MODE>(d, sigma, inv_sigma, i, ax);
     if (MODE == kQpCheck) max_bits(&ctl->primal_bits, residual);
   }
 }
@@ -285,17 +318,26 @@ __global__ void k_qp_advance(QpCtl* ctl, int graph_iterations) {
 
 // ---- Setup --------------------------------------------------------------------------------
 
+// G lanes per row, grid-stride over the rows (a long row is walked by its G lanes: the setup
+// products run forty times per solve).
+template <int G>
 __global__ void __launch_bounds__(kQpThreads) k_qp_spmv(int rows, const int* starts,
                                                         const int* index, const double* values,
                                                         const double* v, double* out) {
-  const int lane = threadIdx.x & 31;
-  const int warps = gridDim.x * (kQpThreads / 32);
-  for (int r = static_cast<int>(blockIdx.x) * (kQpThreads / 32) + static_cast<int>(threadIdx.x >> 5);
-       r < rows; r += warps) {
+  const int lane = static_cast<int>(threadIdx.x) % G;
+  const int groups = static_cast<int>(gridDim.x) * (kQpThreads / G);
+  const int first = (static_cast<int>(blockIdx.x) * kQpThreads + static_cast<int>(threadIdx.x)) / G;
+  // Every group runs the same number of rounds, so the lanes of a warp stay together for the
+  // shuffles of group_sum.
+  const int rounds = (rows + groups - 1) / groups;
+  for (int q = 0; q < rounds; ++q) {
+    const int r = first + q * groups;
     double s = 0.0;
-    for (int e = starts[r] + lane; e < starts[r + 1]; e += 32) s = fma(values[e], v[index[e]], s);
-    s = warp_sum(s);
-    if (lane == 0) out[r] = s;
+    if (r < rows) {
+      for (int e = starts[r] + lane; e < starts[r + 1]; e += G) s = fma(values[e], v[index[e]], s);
+    }
+    s = group_sum<G>(s);
+    if (r < rows && lane == 0) out[r] = s;
   }
 }
 
@@ -339,7 +381,7 @@ __global__ void k_qp_row_dual(QpDev d, double* row_dual) {
 __global__ void k_qp_init(QpDev d) {
   const int stride = static_cast<int>(gridDim.x * blockDim.x);
   for (int j = static_cast<int>(blockIdx.x * blockDim.x + threadIdx.x); j < d.n; j += stride) {
-    d.x0[j] = project(0.0, d.col_lower[j], d.col_upper[j]);
+    d.x0[j] = box(0.0, d.col_lower[j], d.col_upper[j]);
     d.x1[j] = 0.0;
     d.xbar[j] = 0.0;
   }
@@ -409,10 +451,18 @@ void qp_launch_advance(QpCtl* ctl, int graph_iterations, cudaStream_t s) {
 }
 
 void qp_launch_spmv(int rows, const int* starts, const int* index, const double* values,
-                    const double* v, double* out, cudaStream_t s) {
+                    const double* v, double* out, int lanes, cudaStream_t s) {
   if (rows <= 0) return;
-  const int grid = std::min((rows + 7) / 8, 4096);
-  k_qp_spmv<<<grid, kQpThreads, 0, s>>>(rows, starts, index, values, v, out);
+  const long long threads = static_cast<long long>(rows) * lanes;
+  const int grid = static_cast<int>(std::min<long long>((threads + kQpThreads - 1) / kQpThreads, 8192));
+  switch (lanes) {
+    case 1: k_qp_spmv<1><<<grid, kQpThreads, 0, s>>>(rows, starts, index, values, v, out); break;
+    case 2: k_qp_spmv<2><<<grid, kQpThreads, 0, s>>>(rows, starts, index, values, v, out); break;
+    case 4: k_qp_spmv<4><<<grid, kQpThreads, 0, s>>>(rows, starts, index, values, v, out); break;
+    case 8: k_qp_spmv<8><<<grid, kQpThreads, 0, s>>>(rows, starts, index, values, v, out); break;
+    case 16: k_qp_spmv<16><<<grid, kQpThreads, 0, s>>>(rows, starts, index, values, v, out); break;
+    default: k_qp_spmv<32><<<grid, kQpThreads, 0, s>>>(rows, starts, index, values, v, out); break;
+  }
   ++g_qp_launches;
 }
 
