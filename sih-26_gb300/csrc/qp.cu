@@ -79,6 +79,7 @@ QpEngine::QpEngine(int device) : device_(device) {
     throw EngineError{SANKHYA_GB300_ERROR_DEVICE, "no CUDA device " + std::to_string(device)};
   }
   SGB_CUDA(cudaSetDevice(device));
+  SGB_CUDA(qp_configure_kernels());
   SGB_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   SGB_CUDA(cudaMallocHost(&ctl_host_, sizeof(QpCtl)));
   SGB_CUDA(cudaMallocHost(&hist_host_, sizeof(QpHist) * kQpMaxPeriods));
@@ -308,6 +309,7 @@ QpDev QpEngine::dev() const {
   d.n = n_;
   d.col_lanes = col_lanes_;
   d.row_lanes = row_lanes_;
+  d.stage = stage_;
   d.sense = sense_;
   d.offset = offset_;
   d.a_cs = a_cs_.ptr;
@@ -405,7 +407,7 @@ double QpEngine::hessian_norm(unsigned seed) {
 
 void QpEngine::build_graph(int periods) {
   if (graph_ != nullptr && graph_periods_ == periods && graph_col_lanes_ == col_lanes_ &&
-      graph_row_lanes_ == row_lanes_) {
+      graph_row_lanes_ == row_lanes_ && graph_stage_ == stage_) {
     return;
   }
   destroy_graph();
@@ -436,6 +438,7 @@ void QpEngine::build_graph(int periods) {
   graph_periods_ = periods;
   graph_col_lanes_ = col_lanes_;
   graph_row_lanes_ = row_lanes_;
+  graph_stage_ = stage_;
 }
 
 void QpEngine::solve(const sankhya_gb300_qp_params& p, sankhya_gb300_qp_result* r) {
@@ -456,6 +459,7 @@ void QpEngine::solve(const sankhya_gb300_qp_params& p, sankhya_gb300_qp_result* 
   SGB_CUDA(cudaSetDevice(device_));
   solved_ = false;
   layout(col_lanes, row_lanes);
+  stage_ = p.no_staging ? 0 : 1;
   // Check periods per graph: about 2 ms of work by the bytes an iteration moves, at most 20.
   int periods = p.periods_per_poll;
   if (periods <= 0) {

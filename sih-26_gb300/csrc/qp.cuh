@@ -28,7 +28,13 @@
 namespace sgb {
 
 constexpr int kQpThreads = 256;
+constexpr int kQpWarps = kQpThreads / 32;
 constexpr int kQpChunk = 2048;
+// One-lane passes stage each warp's slice of the matrix (its 32 items' entries, contiguous)
+// in shared memory with coalesced loads, then every lane walks its own item there: at most
+// kQpStage entries per warp (a warp whose slice is longer reads its items directly).
+constexpr int kQpStage = 768;
+constexpr int kQpStageBytes = kQpWarps * kQpStage * 12;
 constexpr int kQpCheckEvery = 50;   // src/qp/qp_condat_vu.cpp:279
 constexpr int kQpMaxPeriods = 64;   // check periods per CUDA graph at most
 
@@ -68,6 +74,7 @@ struct QpHist {
 struct QpDev {
   int m, n;
   int col_lanes, row_lanes;
+  int stage;  // one-lane passes stage the warp's matrix slice in shared memory
   double sense, offset;
   // A by columns (CSC) and by rows (CSR); Q as the full symmetric matrix by rows.
   const int* a_cs;
@@ -131,5 +138,8 @@ void qp_launch_row_dual(const QpDev& d, double* row_dual, cudaStream_t s);
 // x0 = proj_box(0) (src/qp/qp_condat_vu.cpp:213-217), y = 0.
 void qp_launch_init(const QpDev& d, cudaStream_t s);
 long long qp_kernel_launch_count();
+// Opts the staged one-lane passes into kQpStageBytes of dynamic shared memory on the current
+// device; returns the CUDA error of the first attribute call that failed.
+cudaError_t qp_configure_kernels();
 
 }  // namespace sgb

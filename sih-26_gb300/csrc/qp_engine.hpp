@@ -53,6 +53,7 @@ class QpEngine {
 
   // Layout for the current lanes.
   int col_lanes_ = 0, row_lanes_ = 0;
+  int stage_ = 1;
   int col_short_blocks_ = 0, row_short_blocks_ = 0;
   int ncol_chunks_ = 0, nrow_chunks_ = 0, nlong_cols_ = 0, nlong_rows_ = 0;
   DeviceArray<QpChunk> col_chunks_, row_chunks_;
@@ -67,7 +68,7 @@ class QpEngine {
   long long final_iterations_ = 0;
 
   cudaGraphExec_t graph_ = nullptr;
-  int graph_periods_ = 0, graph_col_lanes_ = 0, graph_row_lanes_ = 0;
+  int graph_periods_ = 0, graph_col_lanes_ = 0, graph_row_lanes_ = 0, graph_stage_ = -1;
   long long graph_nodes_ = 0;
 };
 

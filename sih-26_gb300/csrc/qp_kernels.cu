@@ -63,6 +63,89 @@ __device__ __forceinline__ bool qp_skip(const QpCtl* ctl, int k) {
   return c->done != 0 || c->base + k + 1 > c->limit;
 }
 
+// ---- Staged one-lane sums ----------------------------------------------------------------
+// A warp's 32 consecutive items own one contiguous slice of each matrix array. The warp copies
+// the slice into its part of shared memory with coalesced loads, then each lane sums its own
+// item there in entry order: the same sums, in the same order, as the direct one-lane loop.
+// A lane with no item (past the end, or a long item of the chunked path) passes an empty
+// range. All 32 lanes must call.
+
+__device__ __forceinline__ void stage_slice(const double* values, const int* index, int begin,
+                                            int count, double* sv, int* si) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll 4
+  for (int k = lane; k < count; k += 32) {
+    sv[k] = __ldg(values + begin + k);
+    si[k] = __ldg(index + begin + k);
+  }
+}
+
+__device__ __forceinline__ double* stage_values() {
+  extern __shared__ __align__(16) unsigned char qp_smem[];
+  return reinterpret_cast<double*>(qp_smem) + (threadIdx.x >> 5) * kQpStage;
+}
+
+__device__ __forceinline__ int* stage_index() {
+  extern __shared__ __align__(16) unsigned char qp_smem[];
+  return reinterpret_cast<int*>(qp_smem + kQpWarps * kQpStage * sizeof(double)) +
+         (threadIdx.x >> 5) * kQpStage;
+}
+
+// (A v)_i over row i's entries [b, e) of the CSR.
+__device__ __forceinline__ double staged_row_sum(const QpDev& d, const double* v, int i, int b,
+                                                 int e) {
+  const int lane = threadIdx.x & 31;
+  const int r0 = i - lane;
+  int wb = 0, we = 0;
+  if (r0 < d.m) {
+    wb = d.a_rs[r0];
+    we = d.a_rs[min(r0 + 32, d.m)];
+  }
+  double ax = 0.0;
+  if (we - wb <= kQpStage) {
+    double* sv = stage_values();
+    int* si = stage_index();
+    stage_slice(d.a_rv, d.a_ci, wb, we - wb, sv, si);
+    __syncwarp();
+    for (int q = b - wb; q < e - wb; ++q) ax = fma(sv[q], v[si[q]], ax);
+  } else {
+    for (int q = b; q < e; ++q) ax = fma(d.a_rv[q], v[d.a_ci[q]], ax);
+  }
+  return ax;
+}
+
+// (Q x)_j over row j of Q's entries [qb, qe) and (A'y)_j over column j of A's [ab, ae).
+__device__ __forceinline__ void staged_column_sums(const QpDev& d, const double* x, int j, int qb,
+                                                   int qe, int ab, int ae, double* qx,
+                                                   double* aty) {
+  const int lane = threadIdx.x & 31;
+  const int c0 = j - lane;
+  int qwb = 0, qwe = 0, awb = 0, awe = 0;
+  if (c0 < d.n) {
+    const int cn = min(c0 + 32, d.n);
+    qwb = d.q_rs[c0];
+    qwe = d.q_rs[cn];
+    awb = d.a_cs[c0];
+    awe = d.a_cs[cn];
+  }
+  const int lq = qwe - qwb, la = awe - awb;
+  double sq = 0.0, sa = 0.0;
+  if (lq + la <= kQpStage) {
+    double* sv = stage_values();
+    int* si = stage_index();
+    stage_slice(d.q_v, d.q_ci, qwb, lq, sv, si);
+    stage_slice(d.a_cv, d.a_ri, awb, la, sv + lq, si + lq);
+    __syncwarp();
+    for (int q = qb - qwb; q < qe - qwb; ++q) sq = fma(sv[q], x[si[q]], sq);
+    for (int a = lq + ab - awb; a < lq + ae - awb; ++a) sa = fma(sv[a], d.y[si[a]], sa);
+  } else {
+    for (int q = qb; q < qe; ++q) sq = fma(d.q_v[q], x[d.q_ci[q]], sq);
+    for (int a = ab; a < ae; ++a) sa = fma(d.a_cv[a], d.y[d.a_ri[a]], sa);
+  }
+  *qx = sq;
+  *aty = sa;
+}
+
 // ---- Column pass ------------------------------------------------------------------------
 
 // The epilogue of column j, run by one lane. Returns the check's residual (check form) and the
@@ -118,10 +201,14 @@ __global__ void __launch_bounds__(kQpThreads) k_qp_column(QpDev d, QpCtl* ctl, i
       }
     }
     double qx = 0.0, aty = 0.0;
-    for (int e = qb + lane; e < qe; e += G) qx = fma(d.q_v[e], x[d.q_ci[e]], qx);
-    for (int e = ab + lane; e < ae; e += G) aty = fma(d.a_cv[e], d.y[d.a_ri[e]], aty);
-    qx = group_sum<G>(qx);
-    aty = group_sum<G>(aty);
+    if (G == 1 && d.stage) {
+      staged_column_sums(d, x, j, qb, qe, ab, ae, &qx, &aty);
+    } else {
+      for (int e = qb + lane; e < qe; e += G) qx = fma(d.q_v[e], x[d.q_ci[e]], qx);
+      for (int e = ab + lane; e < ae; e += G) aty = fma(d.a_cv[e], d.y[d.a_ri[e]], aty);
+      qx = group_sum<G>(qx);
+      aty = group_sum<G>(aty);
+    }
     double residual = 0.0, obj = 0.0;
     if (active && lane == 0) column_epilogue<MODE>(d, tau, j, x, xn, qx, aty, &residual, &obj);
     if (MODE != kQpStep) {
@@ -221,8 +308,12 @@ __global__ void __launch_bounds__(kQpThreads) k_qp_row(QpDev d, QpCtl* ctl, int 
       }
     }
     double ax = 0.0;
-    for (int q = b + lane; q < e; q += G) ax = fma(d.a_rv[q], v[d.a_ci[q]], ax);
-    ax = group_sum<G>(ax);
+    if (G == 1 && d.stage) {
+      ax = staged_row_sum(d, v, i, b, e);
+    } else {
+      for (int q = b + lane; q < e; q += G) ax = fma(d.a_rv[q], v[d.a_ci[q]], ax);
+      ax = group_sum<G>(ax);
+    }
     double residual = 0.0;
     if (active && lane == 0) residual = row_epilogue<MODE>(d, sigma, inv_sigma, i, ax);
     if (MODE == kQpCheck) {
@@ -396,8 +487,9 @@ template <int MODE>
 void column_pass(const QpDev& d, QpCtl* ctl, int k, int src, cudaStream_t s) {
   const int grid = d.col_short_blocks + (d.ncol_chunks + 7) / 8;
   if (grid == 0) return;
+  const int smem = d.stage ? kQpStageBytes : 0;
   switch (d.col_lanes) {
-    case 1: launch_after(k_qp_column<1, MODE>, grid, kQpThreads, 0, s, d, ctl, k, src); break;
+    case 1: launch_after(k_qp_column<1, MODE>, grid, kQpThreads, smem, s, d, ctl, k, src); break;
     case 2: launch_after(k_qp_column<2, MODE>, grid, kQpThreads, 0, s, d, ctl, k, src); break;
     case 4: launch_after(k_qp_column<4, MODE>, grid, kQpThreads, 0, s, d, ctl, k, src); break;
     case 8: launch_after(k_qp_column<8, MODE>, grid, kQpThreads, 0, s, d, ctl, k, src); break;
@@ -411,8 +503,9 @@ template <int MODE>
 void row_pass(const QpDev& d, QpCtl* ctl, int k, int src, cudaStream_t s) {
   const int grid = d.row_short_blocks + (d.nrow_chunks + 7) / 8;
   if (grid == 0) return;
+  const int smem = d.stage ? kQpStageBytes : 0;
   switch (d.row_lanes) {
-    case 1: launch_after(k_qp_row<1, MODE>, grid, kQpThreads, 0, s, d, ctl, k, src); break;
+    case 1: launch_after(k_qp_row<1, MODE>, grid, kQpThreads, smem, s, d, ctl, k, src); break;
     case 2: launch_after(k_qp_row<2, MODE>, grid, kQpThreads, 0, s, d, ctl, k, src); break;
     case 4: launch_after(k_qp_row<4, MODE>, grid, kQpThreads, 0, s, d, ctl, k, src); break;
     case 8: launch_after(k_qp_row<8, MODE>, grid, kQpThreads, 0, s, d, ctl, k, src); break;
@@ -493,5 +586,20 @@ void qp_launch_init(const QpDev& d, cudaStream_t s) {
 }
 
 long long qp_kernel_launch_count() { return g_qp_launches; }
+
+cudaError_t qp_configure_kernels() {
+  cudaError_t err = cudaSuccess;
+  const auto opt = [&](const void* f) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, kQpStageBytes);
+    if (err == cudaSuccess) err = e;
+  };
+  opt(reinterpret_cast<const void*>(k_qp_column<1, kQpStep>));
+  opt(reinterpret_cast<const void*>(k_qp_column<1, kQpCheck>));
+  opt(reinterpret_cast<const void*>(k_qp_column<1, kQpReport>));
+  opt(reinterpret_cast<const void*>(k_qp_row<1, kQpStep>));
+  opt(reinterpret_cast<const void*>(k_qp_row<1, kQpCheck>));
+  return err;
+}
 
 }  // namespace sgb

@@ -254,3 +254,20 @@ def test_qp_reference_demo_models(qp_engine, oracle, reference, name):
     assert_same(r, got, o)
     if name == "qp_blend.mps":
         assert np.allclose(got[0], [200.0 / 3.0, 100.0 / 3.0], rtol=1e-6)
+
+
+@pytest.mark.parametrize("make", [lambda: random_qp(61, 3000, 5000, per_column=6),
+                                  lambda: long_items_qp(7)], ids=["random", "long_items"])
+def test_qp_staging_gives_the_same_bits(qp_engine, make):
+    """The one-lane passes stage each warp's matrix slice in shared memory; the sums are the
+    same, in the same order, as reading the matrix directly."""
+    qp_engine.load(make())
+    a = qp_engine.solve(tolerance=1e-8, iteration_limit=3000, column_lanes=1, row_lanes=1)
+    xa = qp_engine.solution()
+    b = qp_engine.solve(tolerance=1e-8, iteration_limit=3000, column_lanes=1, row_lanes=1,
+                        staging=False)
+    xb = qp_engine.solution()
+    assert (a.status_name, a.iterations, a.objective) == (b.status_name, b.iterations,
+                                                          b.objective)
+    for u, v in zip(xa, xb):
+        assert np.array_equal(u, v)
