@@ -385,8 +385,9 @@ typedef struct sankhya_gb300_qp_params {
   int32_t periods_per_poll; /* 50-iteration check periods per CUDA-graph launch; 0 = auto */
   int32_t column_lanes;     /* threads per column in the column pass: 1..32, 0 = auto */
   int32_t row_lanes;        /* threads per row in the row pass: 1..32, 0 = auto */
-  int32_t no_staging;       /* 1: one-lane passes read the matrix directly instead of staging
-                               each warp's slice in shared memory (the sums are the same) */
+  int32_t staging;          /* 1: one-lane passes stage each warp's matrix slice in shared
+                               memory (the same sums; measured slower on GB300, so 0 is the
+                               default) */
   const volatile int32_t* interrupt; /* an interrupt flag, polled; may be NULL */
   sankhya_gb300_log_fn log;  /* every 5,000 iterations, as the reference logs; may be NULL */
   void* log_user;

@@ -459,7 +459,7 @@ void QpEngine::solve(const sankhya_gb300_qp_params& p, sankhya_gb300_qp_result* 
   SGB_CUDA(cudaSetDevice(device_));
   solved_ = false;
   layout(col_lanes, row_lanes);
-  stage_ = p.no_staging ? 0 : 1;
+  stage_ = p.staging ? 1 : 0;
   // Check periods per graph: about 2 ms of work by the bytes an iteration moves, at most 20.
   int periods = p.periods_per_poll;
   if (periods <= 0) {

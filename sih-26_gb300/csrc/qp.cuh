@@ -30,9 +30,13 @@ namespace sgb {
 constexpr int kQpThreads = 256;
 constexpr int kQpWarps = kQpThreads / 32;
 constexpr int kQpChunk = 2048;
-// One-lane passes stage each warp's slice of the matrix (its 32 items' entries, contiguous)
-// in shared memory with coalesced loads, then every lane walks its own item there: at most
-// kQpStage entries per warp (a warp whose slice is longer reads its items directly).
+// On request (sankhya_gb300_qp_params::staging), one-lane passes stage each warp's slice of the
+// matrix (its 32 items' entries, contiguous) in shared memory with coalesced loads, then every
+// lane walks its own item there: at most kQpStage entries per warp (a warp whose slice is
+// longer reads its items directly). Measured on GB300 it is slower, not faster: the 72 KB a
+// block needs halves the resident warps (35% active against 66%), and the copy phase no longer
+// overlaps the gathers (1M x 2M QP: column pass 250 against 135 us, row pass 230 against
+// 141 us). It stays as an option, with the same sums in the same order.
 constexpr int kQpStage = 768;
 constexpr int kQpStageBytes = kQpWarps * kQpStage * 12;
 constexpr int kQpCheckEvery = 50;   // src/qp/qp_condat_vu.cpp:279

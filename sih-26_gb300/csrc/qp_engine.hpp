@@ -53,7 +53,7 @@ class QpEngine {
 
   // Layout for the current lanes.
   int col_lanes_ = 0, row_lanes_ = 0;
-  int stage_ = 1;
+  int stage_ = 0;
   int col_short_blocks_ = 0, row_short_blocks_ = 0;
   int ncol_chunks_ = 0, nrow_chunks_ = 0, nlong_cols_ = 0, nlong_rows_ = 0;
   DeviceArray<QpChunk> col_chunks_, row_chunks_;

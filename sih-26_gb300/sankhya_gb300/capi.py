@@ -105,7 +105,7 @@ class CQpParams(ctypes.Structure):
     _fields_ = [("tolerance", ctypes.c_double), ("iteration_limit", ctypes.c_int64),
                 ("time_limit", ctypes.c_double), ("random_seed", ctypes.c_int64),
                 ("periods_per_poll", ctypes.c_int32), ("column_lanes", ctypes.c_int32),
-                ("row_lanes", ctypes.c_int32), ("no_staging", ctypes.c_int32),
+                ("row_lanes", ctypes.c_int32), ("staging", ctypes.c_int32),
                 ("interrupt", ctypes.POINTER(ctypes.c_int32)), ("log", LOG_FN),
                 ("log_user", ctypes.c_void_p), ("poll", POLL_FN),
                 ("poll_user", ctypes.c_void_p)]
@@ -428,14 +428,14 @@ class QpEngine:
               time_limit: Optional[float] = None, random_seed: int = 0,
               periods_per_poll: int = 0, column_lanes: int = 0, row_lanes: int = 0,
               interrupt: Optional[np.ndarray] = None, log: Optional[Callable] = None,
-              poll: Optional[Callable] = None, staging: bool = True) -> QpResult:
+              poll: Optional[Callable] = None, staging: bool = False) -> QpResult:
         cb = LOG_FN(lambda user, it, obj, p, d, s: log(it, obj, p, d, s)) if log else LOG_FN()
         pcb = POLL_FN(lambda user, it, obj: int(bool(poll(it, obj)))) if poll else POLL_FN()
         intr = (interrupt.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
                 if interrupt is not None else ctypes.POINTER(ctypes.c_int32)())
         params = CQpParams(tolerance, iteration_limit,
                            1e308 if time_limit is None else float(time_limit), random_seed,
-                           periods_per_poll, column_lanes, row_lanes, 0 if staging else 1,
+                           periods_per_poll, column_lanes, row_lanes, int(bool(staging)),
                            intr, cb, None, pcb, None)
         r = CQpResult()
         _check(self._lib.sankhya_gb300_qp_solve(self._h, ctypes.byref(params), ctypes.byref(r)))

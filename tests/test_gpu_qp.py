@@ -262,10 +262,10 @@ def test_qp_staging_gives_the_same_bits(qp_engine, make):
     """The one-lane passes stage each warp's matrix slice in shared memory; the sums are the
     same, in the same order, as reading the matrix directly."""
     qp_engine.load(make())
-    a = qp_engine.solve(tolerance=1e-8, iteration_limit=3000, column_lanes=1, row_lanes=1)
+    a = qp_engine.solve(tolerance=1e-8, iteration_limit=3000, column_lanes=1, row_lanes=1,
+                        staging=True)
     xa = qp_engine.solution()
-    b = qp_engine.solve(tolerance=1e-8, iteration_limit=3000, column_lanes=1, row_lanes=1,
-                        staging=False)
+    b = qp_engine.solve(tolerance=1e-8, iteration_limit=3000, column_lanes=1, row_lanes=1)
     xb = qp_engine.solution()
     assert (a.status_name, a.iterations, a.objective) == (b.status_name, b.iterations,
                                                           b.objective)
