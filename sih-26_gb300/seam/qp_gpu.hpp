@@ -4,9 +4,11 @@
 // src/qp/qp_condat_vu.cpp): minimise offset + c'x + 0.5 x'Qx over row_lower <= Ax <= row_upper
 // and the column bounds, a Hessian that is not provably convex refused with kModelError before
 // any arithmetic, the Solution filled as the CPU engine fills it. The iterations run on the
-// GPU (sankhya_gb300_qp_*, include/sankhya_gb300.h). SANKHYA's solve() routes a QP here
-// instead of the CPU engine when its `gpu` option is on (src/core/solve.cpp:975-981; the one
-// line to change is shown in the integration notes).
+// GPU (sankhya_gb300_qp_*, include/sankhya_gb300.h). For SANKHYA's solve() to route a QP
+// here when its `gpu` option is on, its QP branch (src/core/solve.cpp:975-981) calls
+//     options.get_bool("gpu") ? gpu::solve_convex_qp_gpu(target, opts, logger, control)
+//                             : qp::solve_convex_qp(target, opts, logger, control)
+// with opts = with_the_time_that_is_left(options).
 #pragma once
 
 #include "sankhya/logging.hpp"
