@@ -39,37 +39,7 @@ std::string qp_format(const char* fmt, ...) {
   return buf;
 }
 
-// Lanes per item from the mean entries per item: the smallest power of two that leaves each
-// lane at most 32 entries of a typical item. The passes are bound by the FP64 pipe, where a
-// lane that sits out the epilogue costs as much as a working one, so few lanes win: on the
-// 1M x 2M QP (15 entries per column, 20 per row) one lane per column and per row runs
-// 2.4 and 2.6 times faster than four and eight. Items longer than 64 lanes' worth go to the
-// chunked path whatever the lanes.
-int auto_lanes(double mean) {
-  int g = 1;
-  while (g < 32 && 32.0 * g < mean) g *= 2;
-  return g;
-}
-
 bool valid_lanes(int g) { return g == 1 || g == 2 || g == 4 || g == 8 || g == 16 || g == 32; }
-
-// Chunks of the items longer than 64 * lanes entries.
-void build_chunks(const std::vector<int>& len, int lanes, std::vector<QpChunk>* out,
-                  int* nlong) {
-  out->clear();
-  *nlong = 0;
-  for (int item = 0; item < static_cast<int>(len.size()); ++item) {
-    const int l = len[item];
-    if (l <= 64 * lanes) continue;
-    const int count = (l + kQpChunk - 1) / kQpChunk;
-    const int first = static_cast<int>(out->size());
-    for (int c = 0; c < count; ++c) {
-      out->push_back(QpChunk{item, c * kQpChunk, std::min(l, (c + 1) * kQpChunk), first, count,
-                             *nlong});
-    }
-    ++*nlong;
-  }
-}
 
 }  // namespace
 
@@ -174,103 +144,31 @@ void QpEngine::load(const sankhya_gb300_qp_problem& p) {
   sense_ = sense;
   offset_ = lp.objective_offset;
 
-  // A by rows: a counting-sort transpose in column order keeps each row's columns ascending.
-  std::vector<int> rptr(static_cast<size_t>(m) + 1, 0);
-  for (long long k = 0; k < nnz; ++k) ++rptr[static_cast<size_t>(lp.row_index[k]) + 1];
-  for (int i = 0; i < m; ++i) rptr[i + 1] += rptr[i];
-  std::vector<int> next(rptr.begin(), rptr.end() - 1);
-  std::vector<int> ridx(static_cast<size_t>(nnz));
-  std::vector<double> rval(static_cast<size_t>(nnz));
-  for (int j = 0; j < n; ++j) {
-    for (int k = lp.col_starts[j]; k < lp.col_starts[j + 1]; ++k) {
-      const int slot = next[lp.row_index[k]]++;
-      ridx[slot] = j;
-      rval[slot] = lp.values[k];
-    }
-  }
-  // Q by rows, both triangles: a stored entry (i, j) is Q_ij and, off the diagonal, Q_ji
-  // (src/qp/qp_condat_vu.cpp:145-160). Walking the columns in order puts each row's entries
-  // in ascending column order for a lower triangle; any other input is sorted per row.
-  std::vector<int> qptr(static_cast<size_t>(n) + 1, 0);
-  for (int j = 0; j < n && hz > 0; ++j) {
-    for (int k = p.hessian_starts[j]; k < p.hessian_starts[j + 1]; ++k) {
-      const int i = p.hessian_index[k];
-      ++qptr[static_cast<size_t>(i) + 1];
-      if (i != j) ++qptr[static_cast<size_t>(j) + 1];
-    }
-  }
-  for (int j = 0; j < n; ++j) qptr[j + 1] += qptr[j];
-  const long long qz = qptr[n];
-  std::vector<int> qnext(qptr.begin(), qptr.end() - 1);
-  std::vector<int> qidx(static_cast<size_t>(qz));
-  std::vector<double> qval(static_cast<size_t>(qz));
-  for (int j = 0; j < n && hz > 0; ++j) {
-    for (int k = p.hessian_starts[j]; k < p.hessian_starts[j + 1]; ++k) {
-      const int i = p.hessian_index[k];
-      const double v = p.hessian_values[k];
-      int slot = qnext[i]++;
-      qidx[slot] = j;
-      qval[slot] = sense * v;
-      if (i != j) {
-        slot = qnext[j]++;
-        qidx[slot] = i;
-        qval[slot] = sense * v;
-      }
-    }
-  }
-  for (int r = 0; r < n; ++r) {
-    const int b = qptr[r], e = qptr[r + 1];
-    bool sorted = true;
-    for (int k = b + 1; k < e && sorted; ++k) sorted = qidx[k - 1] <= qidx[k];
-    if (sorted) continue;
-    std::vector<std::pair<int, double>> row;
-    for (int k = b; k < e; ++k) row.push_back({qidx[k], qval[k]});
-    std::stable_sort(row.begin(), row.end(),
-                     [](const auto& a, const auto& c) { return a.first < c.first; });
-    for (int k = b; k < e; ++k) {
-      qidx[k] = row[k - b].first;
-      qval[k] = row[k - b].second;
-    }
-  }
+  // The host layouts (qp_layout.hpp): A by rows, sense Q by rows with both triangles, the
+  // items' lengths, the cost and bounds in the kernels' forms.
+  QpHostLayout h;
+  qp_build_layout(p, &h);
+  const long long qz = static_cast<long long>(h.q_cols.size());
   nnz_q_ = qz;
-  col_len_.assign(static_cast<size_t>(n), 0);
-  row_len_.assign(static_cast<size_t>(m), 0);
-  for (int j = 0; j < n; ++j) {
-    col_len_[j] = (qptr[j + 1] - qptr[j]) + (lp.col_starts[j + 1] - lp.col_starts[j]);
-  }
-  for (int i = 0; i < m; ++i) row_len_[i] = rptr[i + 1] - rptr[i];
+  col_len_ = h.col_len;
+  row_len_ = h.row_len;
 
   cudaStream_t s = stream_;
   const size_t z = static_cast<size_t>(nnz);
   a_cs_.upload(lp.col_starts, static_cast<size_t>(n) + 1, s);
   a_ri_.upload(lp.row_index, z, s);
   a_cv_.upload(lp.values, z, s);
-  a_rs_.upload(rptr.data(), rptr.size(), s);
-  a_ci_.upload(ridx.data(), z, s);
-  a_rv_.upload(rval.data(), z, s);
-  q_rs_.upload(qptr.data(), qptr.size(), s);
-  q_ci_.upload(qidx.data(), static_cast<size_t>(qz), s);
-  q_v_.upload(qval.data(), static_cast<size_t>(qz), s);
-  // The kernels' forms (qp_kernels.cu): the cost times the sense (Q was stored so above), and
-  // every absent bound as an infinity on its side.
-  constexpr double kInf = std::numeric_limits<double>::infinity();
-  const auto finite = [](double v) { return !(std::isinf(v) || std::fabs(v) >= 1e30); };
-  std::vector<double> cmin(static_cast<size_t>(n)), lo(static_cast<size_t>(n)),
-      hi(static_cast<size_t>(n)), rlo(static_cast<size_t>(m)), rhi(static_cast<size_t>(m));
-  for (int j = 0; j < n; ++j) {
-    cmin[j] = sense * lp.col_cost[j];
-    lo[j] = finite(lp.col_lower[j]) ? lp.col_lower[j] : -kInf;
-    hi[j] = finite(lp.col_upper[j]) ? lp.col_upper[j] : kInf;
-  }
-  for (int i = 0; i < m; ++i) {
-    rlo[i] = finite(lp.row_lower[i]) ? lp.row_lower[i] : -kInf;
-    rhi[i] = finite(lp.row_upper[i]) ? lp.row_upper[i] : kInf;
-  }
-  cost_.upload(cmin.data(), cmin.size(), s);
-  col_lower_.upload(lo.data(), lo.size(), s);
-  col_upper_.upload(hi.data(), hi.size(), s);
-  row_lower_.upload(rlo.data(), rlo.size(), s);
-  row_upper_.upload(rhi.data(), rhi.size(), s);
+  a_rs_.upload(h.row_starts.data(), h.row_starts.size(), s);
+  a_ci_.upload(h.row_cols.data(), z, s);
+  a_rv_.upload(h.row_values.data(), z, s);
+  q_rs_.upload(h.q_starts.data(), h.q_starts.size(), s);
+  q_ci_.upload(h.q_cols.data(), static_cast<size_t>(qz), s);
+  q_v_.upload(h.q_values.data(), static_cast<size_t>(qz), s);
+  cost_.upload(h.cost.data(), h.cost.size(), s);
+  col_lower_.upload(h.col_lower.data(), h.col_lower.size(), s);
+  col_upper_.upload(h.col_upper.data(), h.col_upper.size(), s);
+  row_lower_.upload(h.row_lower.data(), h.row_lower.size(), s);
+  row_upper_.upload(h.row_upper.data(), h.row_upper.size(), s);
   for (auto* a : {&x0_, &x1_, &xbar_, &col_dual_, &vec_n_}) a->allocate(static_cast<size_t>(n));
   for (auto* a : {&y_, &row_dual_, &vec_m_}) a->allocate(static_cast<size_t>(m));
   SGB_CUDA(cudaStreamSynchronize(s));
@@ -281,8 +179,8 @@ void QpEngine::layout(int col_lanes, int row_lanes) {
   if (col_lanes == col_lanes_ && row_lanes == row_lanes_) return;
   cudaStream_t s = stream_;
   std::vector<QpChunk> cc, rc;
-  build_chunks(col_len_, col_lanes, &cc, &nlong_cols_);
-  build_chunks(row_len_, row_lanes, &rc, &nlong_rows_);
+  qp_build_chunks(col_len_, col_lanes, &cc, &nlong_cols_);
+  qp_build_chunks(row_len_, row_lanes, &rc, &nlong_rows_);
   ncol_chunks_ = static_cast<int>(cc.size());
   nrow_chunks_ = static_cast<int>(rc.size());
   col_chunks_.upload(cc.data(), cc.size(), s);
@@ -372,9 +270,9 @@ double QpEngine::spectral_norm(unsigned seed) {
     if (std::sqrt(norm2) <= 0.0) return 0.0;
     qp_launch_scale(vec_n_.ptr, n_, dot_out_.ptr, stream_);
     qp_launch_spmv(m_, a_rs_.ptr, a_ci_.ptr, a_rv_.ptr, vec_n_.ptr, vec_m_.ptr,
-                   auto_lanes(double(nnz_a_) / m_), stream_);
+                   qp_auto_lanes(double(nnz_a_) / m_), stream_);
     qp_launch_spmv(n_, a_cs_.ptr, a_ri_.ptr, a_cv_.ptr, vec_m_.ptr, vec_n_.ptr,
-                   auto_lanes(double(nnz_a_) / n_), stream_);
+                   qp_auto_lanes(double(nnz_a_) / n_), stream_);
     estimate = std::sqrt(std::sqrt(dot(vec_n_.ptr, vec_n_.ptr, n_)));
   }
   return estimate;
@@ -397,7 +295,7 @@ double QpEngine::hessian_norm(unsigned seed) {
     const double norm2 = dot(a, a, n_);
     if (std::sqrt(norm2) <= 0.0) return 0.0;
     qp_launch_scale(a, n_, dot_out_.ptr, stream_);
-    qp_launch_spmv(n_, q_rs_.ptr, q_ci_.ptr, q_v_.ptr, a, b, auto_lanes(double(nnz_q_) / n_),
+    qp_launch_spmv(n_, q_rs_.ptr, q_ci_.ptr, q_v_.ptr, a, b, qp_auto_lanes(double(nnz_q_) / n_),
                    stream_);
     estimate = std::fabs(dot(b, a, n_));
     std::swap(a, b);
@@ -450,9 +348,9 @@ void QpEngine::solve(const sankhya_gb300_qp_params& p, sankhya_gb300_qp_result* 
     throw EngineError{SANKHYA_GB300_ERROR_OPTION, "qp_tolerance must be positive"};
   }
   const int col_lanes = p.column_lanes > 0 ? p.column_lanes
-                                           : auto_lanes(n_ > 0 ? double(nnz_a_ + nnz_q_) / n_ : 1.0);
+                                           : qp_auto_lanes(n_ > 0 ? double(nnz_a_ + nnz_q_) / n_ : 1.0);
   const int row_lanes = p.row_lanes > 0 ? p.row_lanes
-                                        : auto_lanes(m_ > 0 ? double(nnz_a_) / m_ : 1.0);
+                                        : qp_auto_lanes(m_ > 0 ? double(nnz_a_) / m_ : 1.0);
   if (!valid_lanes(col_lanes) || !valid_lanes(row_lanes)) {
     throw EngineError{SANKHYA_GB300_ERROR_OPTION, "lanes must be 1, 2, 4, 8, 16 or 32"};
   }

@@ -24,12 +24,12 @@
 #include <cuda_runtime.h>
 
 #include "common.cuh"
+#include "qp_layout.hpp"
 
 namespace sgb {
 
 constexpr int kQpThreads = 256;
 constexpr int kQpWarps = kQpThreads / 32;
-constexpr int kQpChunk = 2048;
 // On request (sankhya_gb300_qp_params::staging), one-lane passes stage each warp's slice of the
 // matrix (its 32 items' entries, contiguous) in shared memory with coalesced loads, then every
 // lane walks its own item there: at most kQpStage entries per warp (a warp whose slice is
@@ -44,16 +44,6 @@ constexpr int kQpMaxPeriods = 64;   // check periods per CUDA graph at most
 
 // Modes of the two passes.
 enum QpMode { kQpStep = 0, kQpCheck = 1, kQpReport = 2 };
-
-// One chunk of a long row or column: entries [begin, end) of the item's entry sequence (for
-// a column: the entries of row j of Q, then those of column j of A).
-struct QpChunk {
-  int item;
-  int begin, end;
-  int first;   // the item's first chunk (partials slot)
-  int count;   // the item's chunk count
-  int slot;    // the item's ticket and long-item slot
-};
 
 // Decision state, on the device.
 struct QpCtl {

@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(kQpThreads) k_qp_column(QpDev d, QpCtl* ctl, i
       qe = d.q_rs[j + 1];
       ab = d.a_cs[j];
       ae = d.a_cs[j + 1];
-      if ((qe - qb) + (ae - ab) > 64 * G) {  // a long column: the chunk path's
+      if ((qe - qb) + (ae - ab) > kQpLongPerLane * G) {  // a long column: the chunk path's
         active = false;
         qb = qe = ab = ae = 0;
       }
@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(kQpThreads) k_qp_row(QpDev d, QpCtl* ctl, int 
     if (active) {
       b = d.a_rs[i];
       e = d.a_rs[i + 1];
-      if (e - b > 64 * G) {
+      if (e - b > kQpLongPerLane * G) {
         active = false;
         b = e = 0;
       }

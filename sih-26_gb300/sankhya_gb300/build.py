@@ -23,7 +23,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_SOURCES = ["pdhg_kernels.cu", "mixed_kernels.cu", "batch_kernels.cu", "engine.cu", "layout.cu",
                 "batch.cu", "qp_kernels.cu", "qp.cu", "capi.cu"]
 HEADERS = ["common.cuh", "kernels.cuh", "tiles.cuh", "chunks.cuh", "decisions.cuh", "mixed.cuh",
-           "batch.cuh", "qp.cuh", "engine.hpp", "batch_engine.hpp", "qp_engine.hpp"]
+           "batch.cuh", "qp.cuh", "qp_layout.hpp", "engine.hpp", "batch_engine.hpp",
+           "qp_engine.hpp"]
 
 
 def _stale(target, sources):
