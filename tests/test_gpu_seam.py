@@ -148,3 +148,60 @@ def test_convex_qp_on_the_gpu(tmp_path, built):
     print(run.stdout[-3000:])
     assert run.returncode == 0, run.stdout[-3000:] + run.stderr[-2000:]
     assert run.stdout.strip().endswith("OK"), run.stdout
+
+
+def test_reference_python_package_on_the_gpu(tmp_path, built, engine, reference):
+    """The reference's own Python package (bindings/python/sankhya, which calls SANKHYA's C
+    API) on a libsankhya.so built from its core with the seam files and the engine's real
+    library in place of src/gpu: afiro solved with Options(gpu=True, algorithm="pdhg",
+    presolve=False) comes back as the engine's own solve of the same LP (the same iteration
+    count and x bit for bit), optimal, with the objective of the package's CPU route
+    (gpu=False) within 1e-6 relative."""
+    import json
+    import textwrap
+
+    import numpy as np
+    import pyoracle
+
+    flags, sources, core = core_link_args()
+    sources = [s for s in sources if not s.endswith("seam_standin.cpp")]
+    tree = pyoracle.reference_tree()
+    pkg = os.path.join(tree, "bindings", "python")
+    if not os.path.isdir(os.path.join(pkg, "sankhya")):
+        pytest.skip("the reference's Python package is not in its tree or staged copy")
+    afiro = os.path.join(tree, "data", "netlib", "afiro.mps")
+    lib_dir = os.path.join(ROOT, "sih-26_gb300", "lib")
+    lib = str(tmp_path / "libsankhya.so")
+    cmd = (["g++", "-shared"] + flags + sources +
+           ["-Wl,--whole-archive", core, "-Wl,--no-whole-archive", f"-L{lib_dir}",
+            "-lsankhya_gb300", f"-Wl,-rpath,{lib_dir}", "-Wl,--no-undefined", "-fopenmp", "-lz",
+            "-o", lib])
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    assert proc.returncode == 0, proc.stderr[-3000:]
+    script = textwrap.dedent(f"""
+        import json, sys
+        sys.path.insert(0, {pkg!r})
+        import sankhya
+        model = sankhya.Model.read({afiro!r})
+        kw = dict(algorithm="pdhg", pdhg_polish=False, presolve=False, log_to_console=False,
+                  pdhg_tolerance=1e-8)
+        gpu = model.solve(sankhya.Options(gpu=True, **kw))
+        cpu = model.solve(sankhya.Options(gpu=False, **kw))
+        print("RESULT " + json.dumps(dict(
+            gpu=[gpu.status, gpu.iterations, gpu.objective, [v.hex() for v in gpu.x]],
+            cpu=[cpu.status, cpu.iterations, cpu.objective])))
+        """)
+    run = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True,
+                         timeout=600, env=dict(os.environ, SANKHYA_LIBRARY=lib))
+    lines = [l for l in run.stdout.splitlines() if l.startswith("RESULT ")]
+    assert run.returncode == 0 and lines, run.stdout[-2000:] + run.stderr[-2000:]
+    got = json.loads(lines[-1][len("RESULT "):])
+    status, iterations, objective, x_hex = got["gpu"]
+    assert status == "optimal" and got["cpu"][0] == "optimal", got
+    assert abs(objective - got["cpu"][2]) <= 1e-6 * max(1.0, abs(got["cpu"][2]))
+    lp = reference.read_model(afiro)
+    engine.load(lp)
+    r = engine.solve(tolerance=1e-8)
+    x = engine.solution()[0]
+    assert iterations == r.iterations, (iterations, r.iterations)
+    assert np.array_equal(np.array([float.fromhex(v) for v in x_hex]), x)
