@@ -181,3 +181,22 @@ def test_reference_demo_qps(built, oracle, reference, name):
     if name == "qp_blend.mps":
         assert np.allclose(a.col_value, [200.0 / 3.0, 100.0 / 3.0], rtol=1e-6)
         assert abs(a.objective - 200.0 / 3.0) <= 1e-5
+
+
+@pytest.mark.parametrize("seed", range(100, 124))
+def test_oracle_matches_reference_build_on_random_qps(built, oracle, reference, seed):
+    """Twenty-four more seeded convex QPs of varied shape, density, band and sense: the
+    restatement and the reference's own build agree bit for bit."""
+    rng = np.random.default_rng(seed)
+    m = int(rng.integers(0, 60))
+    n = int(rng.integers(5, 90))
+    qp = random_qp(seed, m, n, per_column=int(rng.integers(1, 6)),
+                   hessian_band=int(rng.integers(0, 4)), maximise=bool(seed % 2))
+    options = dict(tolerance=float(10.0 ** -rng.integers(6, 10)), iteration_limit=20000,
+                   random_seed=int(rng.integers(0, 5)))
+    a = oracle.solve_qp(qp, **options)
+    b = reference.solve_qp(qp, **options)
+    assert (a.status_name, a.iterations) == (b.status_name, b.iterations), b.message
+    assert float(a.objective).hex() == float(b.objective).hex()
+    for k in ("col_value", "col_dual", "row_dual"):
+        assert np.array_equal(getattr(a, k), getattr(b, k)), k
