@@ -681,3 +681,40 @@ def solve_pdhg_gpu(lp: LP, options: Optional[dict] = None, device: int = 0,
     finally:
         if own:
             eng.close()
+
+
+def solve_convex_qp_gpu(qp, options: Optional[dict] = None, device: int = 0,
+                        engine: Optional["QpEngine"] = None, log: Optional[Callable] = None,
+                        interrupt: Optional[np.ndarray] = None) -> Solution:
+    """The GPU convex-QP engine behind sankhya::qp::solve_convex_qp's contract
+    (include/sankhya/qp.hpp:20, src/qp/qp_condat_vu.cpp:164-362), with the option registry's
+    names and defaults (src/util/options.cpp: qp_tolerance 1e-8, iteration_limit -1, no time
+    limit, random_seed 0). Never falls back to the CPU: a model defect (the engine's own
+    checks, its diagonal convexity test included) is status "model_error", a device failure
+    raises EngineError. The full convexity decision is the caller's (SANKHYA's seam runs the
+    reference's check_convexity). col_dual = c + Qx + sense A'y and row_dual = -sense y, as
+    the reference fills them; dual_bound is the objective only when optimal."""
+    o = {"qp_tolerance": 1e-8, "iteration_limit": -1, "time_limit": None, "random_seed": 0}
+    o.update(options or {})
+    own = engine is None
+    eng = engine or QpEngine(device)
+    try:
+        try:
+            eng.load(qp)
+        except EngineError as e:
+            if e.code == 3:
+                z = np.zeros
+                return Solution("model_error", 0.0, float("nan"), z(qp.cols), z(qp.cols),
+                                z(qp.rows), 0, str(e), "qp-condat-vu-gpu")
+            raise
+        r = eng.solve(tolerance=o["qp_tolerance"], iteration_limit=o["iteration_limit"],
+                      time_limit=o["time_limit"], random_seed=o["random_seed"],
+                      interrupt=interrupt, log=log)
+        x, d, y = eng.solution()
+        bound = (r.objective if r.status_name == "optimal"
+                 else (np.inf if qp.lp.sense < 0 else -np.inf))
+        return Solution(r.status_name, r.objective, bound, x, d, y, r.iterations, r.message,
+                        "qp-condat-vu-gpu", r)
+    finally:
+        if own:
+            eng.close()

@@ -271,3 +271,17 @@ def test_qp_staging_gives_the_same_bits(qp_engine, make):
                                                           b.objective)
     for u, v in zip(xa, xb):
         assert np.array_equal(u, v)
+
+
+def test_qp_python_mirror_on_the_gpu(built, oracle):
+    """sankhya_gb300.capi.solve_convex_qp_gpu on the real engine: the oracle's status,
+    iteration count and point, the bound only when optimal, a model error for a negative
+    diagonal."""
+    qp = random_qp(91, 200, 400)
+    s = capi.solve_convex_qp_gpu(qp, {"qp_tolerance": 1e-8})
+    o = oracle.solve_qp(qp, tolerance=1e-8)
+    assert (s.status, s.iterations) == (o.status_name, o.iterations)
+    assert close(s.col_value, o.col_value) and close(s.row_dual, o.row_dual)
+    assert s.status == "optimal" and s.dual_bound == s.objective
+    bad = qp_from_dense([0.0, 0.0], [-INF, -INF], [INF, INF], [(0, 0, 1.0), (1, 1, -1.0)])
+    assert capi.solve_convex_qp_gpu(bad).status == "model_error"

@@ -111,3 +111,74 @@ def test_model_defect_is_a_status(built, oracle):
     sol = capi.solve_pdhg_gpu(lp, {}, engine=OracleEngine(oracle))
     assert sol.status == "model_error" and sol.message
     assert sol.col_value.shape == (lp.cols,) and sol.row_dual.shape == (lp.rows,)
+
+
+class OracleQpEngine:
+    """QpEngine's interface over the oracle's QP restatement. Records each solve's settings."""
+
+    def __init__(self, oracle):
+        self.oracle = oracle
+        self.calls = []
+
+    def load(self, qp):
+        diag = [qp.hessian_values[k] * qp.lp.sense for j in range(qp.cols)
+                for k in range(qp.hessian_starts[j], qp.hessian_starts[j + 1])
+                if qp.hessian_index[k] == j]
+        if any(v < -1e-10 * max(1.0, max(abs(u) for u in diag)) for v in diag):
+            raise capi.EngineError(3, "the quadratic objective is not convex: a negative "
+                                      "diagonal")
+        self.qp = qp
+
+    def solve(self, tolerance, iteration_limit, time_limit, random_seed, interrupt=None,
+              log=None):
+        from types import SimpleNamespace
+
+        self.calls.append(dict(tolerance=tolerance, iteration_limit=iteration_limit,
+                               time_limit=time_limit, random_seed=random_seed))
+        self.last = self.oracle.solve_qp(self.qp, tolerance=tolerance,
+                                         iteration_limit=iteration_limit,
+                                         time_limit=time_limit, random_seed=random_seed)
+        return SimpleNamespace(status_name=self.last.status_name,
+                               objective=self.last.objective, iterations=self.last.iterations,
+                               message="")
+
+    def solution(self):
+        return self.last.col_value, self.last.col_dual, self.last.row_dual
+
+    def close(self):
+        pass
+
+
+@pytest.mark.parametrize("options", [
+    None,
+    {"qp_tolerance": 1e-6, "iteration_limit": 777, "random_seed": 3},
+    {"qp_tolerance": 1e-9, "time_limit": 0.0},
+], ids=["defaults", "set", "time0"])
+def test_qp_mirror_passes_the_options(built, oracle, options):
+    """solve_convex_qp_gpu hands the registry's QP rows (and their defaults) to the engine and
+    returns its point, with the bound only when optimal."""
+    from sankhya_gb300.model import random_qp
+
+    qp = random_qp(81, 30, 60, maximise=options is not None)
+    eng = OracleQpEngine(oracle)
+    s = capi.solve_convex_qp_gpu(qp, options, engine=eng)
+    want = {"tolerance": 1e-8, "iteration_limit": -1, "time_limit": None, "random_seed": 0}
+    for k, v in (options or {}).items():
+        want[{"qp_tolerance": "tolerance"}.get(k, k)] = v
+    assert eng.calls == [want]
+    o = oracle.solve_qp(qp, **{k: v for k, v in want.items() if v is not None})
+    assert (s.status, s.iterations) == (o.status_name, o.iterations)
+    assert np.array_equal(s.col_value, o.col_value) and np.array_equal(s.row_dual, o.row_dual)
+    assert s.algorithm == "qp-condat-vu-gpu"
+    if s.status == "optimal":
+        assert s.dual_bound == s.objective
+    else:
+        assert s.dual_bound == (np.inf if qp.lp.sense < 0 else -np.inf)
+
+
+def test_qp_mirror_model_error(built, oracle):
+    from sankhya_gb300.model import qp_from_dense
+
+    qp = qp_from_dense([0.0, 0.0], [-INF, -INF], [INF, INF], [(0, 0, 1.0), (1, 1, -1.0)])
+    s = capi.solve_convex_qp_gpu(qp, engine=OracleQpEngine(oracle))
+    assert s.status == "model_error" and "not convex" in s.message
