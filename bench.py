@@ -757,6 +757,10 @@ def cpu_reference(lp, iterations_sample, threads):
     r = o.solve(lp, tolerance=TOLERANCE, iteration_limit=iterations_sample)
     sampled = time.perf_counter() - t0
     per_it = max(sampled - setup, 0.0) / max(1, r.iterations)
+    if per_it <= 0.0:
+        # An LP so small that the sample's iterations are lost in the setup's timing noise:
+        # the whole sample per iteration, an upper bound.
+        per_it = sampled / max(1, r.iterations)
     return setup, per_it, sampled + setup, r
 
 
